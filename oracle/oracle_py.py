@@ -1,0 +1,223 @@
+"""ctypes wrapper around the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by bench.py's CPU-baseline / reference legs, never by the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+GR, GO, PKJ, IO = 0, 1, 2, 3
+H_MAX = 0.125
+
+
+class Desc(C.Structure):
+    _fields_ = [
+        ("type", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("ncomp", C.c_int),
+        ("rows", C.POINTER(C.c_double)), ("gj_pairs", C.POINTER(C.c_int)),
+        ("n_gj_pairs", C.c_int), ("jitter", C.POINTER(C.c_double)),
+        ("stim_comp", C.POINTER(C.c_int)), ("stim_amp", C.POINTER(C.c_double)),
+        ("stim_t0", C.POINTER(C.c_double)), ("stim_t1", C.POINTER(C.c_double)),
+        ("io_gap_g", C.POINTER(C.c_double)),
+        ("tol", C.c_double), ("hmin", C.c_double),
+        ("io_gap", C.c_int), ("go_gj", C.c_int), ("pkj_gj", C.c_int),
+    ]
+
+
+def build(out_dir: str | None = None) -> str:
+    out = out_dir or _HERE
+    subprocess.run(["make", "-s", "-C", _HERE, f"OUT={out}"], check=True)
+    return os.path.join(out, "liboracle.so")
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [C.POINTER(Desc)]
+        L.orc_destroy.argtypes = [P]
+        L.orc_init.argtypes = [P]
+        L.orc_advance.argtypes = [P, C.c_double]
+        for f in ("orc_vnew", "orc_elem_v", "orc_b", "orc_ca", "orc_cm", "orc_area",
+                  "orc_shell", "orc_rev_ca2", "orc_val"):
+            getattr(L, f).restype = C.POINTER(C.c_double)
+            getattr(L, f).argtypes = [P]
+        for f in ("orc_ion", "orc_cond"):
+            getattr(L, f).restype = C.POINTER(C.c_double)
+            getattr(L, f).argtypes = [P, C.c_int]
+        for f in ("orc_row", "orc_col"):
+            getattr(L, f).restype = C.POINTER(C.c_int)
+            getattr(L, f).argtypes = [P]
+        for f in ("orc_nc", "orc_n", "orc_nnz", "orc_ncond", "orc_nion"):
+            getattr(L, f).restype = C.c_int
+            getattr(L, f).argtypes = [P]
+        L.orc_ctl.argtypes = [P, C.POINTER(C.c_double)]
+        L.orc_stats.argtypes = [P, C.POINTER(C.c_longlong)]
+        L.orc_ion_update.argtypes = [P, C.POINTER(C.c_double), C.c_double]
+        L.orc_update_b.argtypes = [P, C.POINTER(C.c_double)]
+        L.orc_set_elem_v.argtypes = [P, C.POINTER(C.c_double)]
+        L.orc_set_ion.argtypes = [P, C.c_int, C.POINTER(C.c_double)]
+        L.orc_set_ca.argtypes = [P, C.POINTER(C.c_double)]
+        L.orc_draw_jitter.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double)]
+        _LIB = L
+    return _LIB
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def draw_jitter(cell_type: int, n: int) -> np.ndarray:
+    """Per-cell V0 jitter from libc rand() (caller seeds with srand)."""
+    out = np.zeros(n, dtype=np.float64)
+    lib().orc_draw_jitter(cell_type, n, _dp(out))
+    return out
+
+
+def libc_srand(seed: int) -> None:
+    C.CDLL(None).srand(C.c_uint(seed))
+
+
+class System:
+    """One RKC system of the oracle (all cells of one type on an nx x ny grid)."""
+
+    def __init__(self, cell_type, nx, ny, rows, jitter, stim=None, gj_pairs=None,
+                 tol=0.0, hmin=0.0, io_gap=True, go_gj=True, pkj_gj=True, io_gap_g=None):
+        L = lib()
+        self._keep = []
+        rows = np.ascontiguousarray(rows, dtype=np.float64)
+        n = nx * ny
+        jitter = np.ascontiguousarray(jitter, dtype=np.float64)
+        assert jitter.size == n
+        d = Desc()
+        d.type, d.nx, d.ny, d.ncomp = cell_type, nx, ny, rows.shape[0]
+        d.rows = _dp(rows)
+        d.jitter = _dp(jitter)
+        self._keep += [rows, jitter]
+        if gj_pairs is not None:
+            g = np.ascontiguousarray(gj_pairs, dtype=np.int32).reshape(-1)
+            d.gj_pairs, d.n_gj_pairs = _ip(g), g.size // 2
+            self._keep.append(g)
+        if stim is not None:
+            comp, amp, t0, t1 = stim
+            comp = np.ascontiguousarray(np.broadcast_to(comp, n), dtype=np.int32)
+            amp, t0, t1 = (np.ascontiguousarray(np.broadcast_to(a, n), dtype=np.float64)
+                           for a in (amp, t0, t1))
+            d.stim_comp, d.stim_amp, d.stim_t0, d.stim_t1 = _ip(comp), _dp(amp), _dp(t0), _dp(t1)
+            self._keep += [comp, amp, t0, t1]
+        if io_gap_g is not None:
+            gg = np.ascontiguousarray(io_gap_g, dtype=np.float64)
+            d.io_gap_g = _dp(gg)
+            self._keep.append(gg)
+        d.tol, d.hmin = tol, hmin
+        d.io_gap, d.go_gj, d.pkj_gj = int(io_gap), int(go_gj), int(pkj_gj)
+        self.h = L.orc_create(C.byref(d))
+        if not self.h:
+            raise RuntimeError("orc_create failed")
+        self.type, self.n, self.ncomp = cell_type, n, rows.shape[0]
+        self.nc = L.orc_nc(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def _arr(self, ptr, n=None):
+        n = self.nc if n is None else n
+        return np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+
+    def init(self) -> int:
+        return lib().orc_init(self.h)
+
+    def advance(self, t: float) -> int:
+        return lib().orc_advance(self.h, t)
+
+    def vnew(self):
+        return self._arr(lib().orc_vnew(self.h))
+
+    def elem_v(self):
+        return self._arr(lib().orc_elem_v(self.h))
+
+    def b(self):
+        return self._arr(lib().orc_b(self.h))
+
+    def ca(self):
+        return self._arr(lib().orc_ca(self.h))
+
+    def ion(self, k):
+        return self._arr(lib().orc_ion(self.h, k))
+
+    def cm(self):
+        return self._arr(lib().orc_cm(self.h))
+
+    def area(self):
+        return self._arr(lib().orc_area(self.h))
+
+    def shell(self):
+        return self._arr(lib().orc_shell(self.h))
+
+    def rev_ca2(self):
+        return self._arr(lib().orc_rev_ca2(self.h))
+
+    def cond(self, k):
+        return self._arr(lib().orc_cond(self.h, k))
+
+    def ncond(self):
+        return lib().orc_ncond(self.h)
+
+    def nion(self):
+        return lib().orc_nion(self.h)
+
+    def csr(self):
+        L = lib()
+        nnz = L.orc_nnz(self.h)
+        row = np.ctypeslib.as_array(L.orc_row(self.h), shape=(self.nc + 1,)).copy()
+        col = np.ctypeslib.as_array(L.orc_col(self.h), shape=(nnz,)).copy()
+        val = np.ctypeslib.as_array(L.orc_val(self.h), shape=(nnz,)).copy()
+        return row, col, val
+
+    def ctl(self):
+        out = np.zeros(8, dtype=np.float64)
+        lib().orc_ctl(self.h, _dp(out))
+        return dict(zip(["absh", "sprad", "naccpt", "errold", "hold", "lt", "tend", "sum_dt"], out))
+
+    def stats(self):
+        out = np.zeros(5, dtype=np.int64)
+        lib().orc_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_longlong)))
+        return dict(zip(["steps", "rejects", "stages", "rho_calls", "ion_updates"], out.tolist()))
+
+    def ion_update(self, vnew, dt):
+        v = np.ascontiguousarray(vnew, dtype=np.float64)
+        lib().orc_ion_update(self.h, _dp(v), dt)
+
+    def update_b(self, vy):
+        v = np.ascontiguousarray(vy, dtype=np.float64)
+        lib().orc_update_b(self.h, _dp(v))
+
+    def set_elem_v(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        lib().orc_set_elem_v(self.h, _dp(v))
+
+    def set_ion(self, k, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        lib().orc_set_ion(self.h, k, _dp(x))
+
+    def set_ca(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        lib().orc_set_ca(self.h, _dp(x))
