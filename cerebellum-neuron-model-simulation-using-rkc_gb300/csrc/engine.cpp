@@ -1,0 +1,864 @@
+// Host runtime of the RKC engine: model setup from reference-format
+// morphology rows (the reference's initialize_host_* and set_host_*_solve:
+// gr.cu:3-82, go.cu:3-88, pkj.cu:3-169, io.cu:3-102, *_solve.cu), packing of
+// systems into per-type pools, the Chebyshev coefficient table, device
+// allocation, and the C ABI of include/gbrkc.h.
+//
+// Built with -ffp-contract=off: the static per-compartment values (areas,
+// capacitances, conductances, axial conductances) are computed in the same
+// operation order as the reference, so they are bit-identical on every host.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <type_traits>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/gbrkc.h"
+#include "engine.h"
+#include "host_init.h"
+#include "model.h"
+
+namespace gbrkc {
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                     \
+  do {                                                                                  \
+    cudaError_t e_ = (x);                                                               \
+    if (e_ != cudaSuccess) return fail(GBRKC_ECUDA, "%s: %s", #x, cudaGetErrorString(e_)); \
+  } while (0)
+
+// ------------------------------------------------------------------ setup
+struct Template {
+  int type, ncomp;
+  std::vector<double> rows;
+  std::vector<double> area, cm, shell, invcm;
+  std::vector<int> ctype;
+  std::vector<std::vector<double>> cond;  // [k][comp]
+  // CSR of one cell with the diagonal kept (RKC sign), as the reference builds it
+  std::vector<int> row, col;
+  std::vector<double> val;
+};
+
+struct HostSystem {
+  int type, nx, ny, n, ncomp, nc;
+  int tmpl;
+  bool gap;
+  std::vector<int> gj_pairs;
+  std::vector<double> io_gap_g, jitter;
+  std::vector<int> stim_comp;
+  std::vector<double> stim_amp, stim_t0, stim_t1;
+  double tol, hmin;
+  // built
+  int csr = -1;                               // index into the system-CSR table
+  std::vector<int> gap_pre, gap_post;
+  std::vector<double> gap_g;
+  int pool_index = -1;
+};
+
+static double row_f(const std::vector<double> &r, int nf, int i, int f) { return r[(size_t)i * nf + f]; }
+
+// one cell of a type from its rows (initialize_host_* + the dense axial matrix)
+static int make_template(int type, int ncomp, const double *rows, Template &T) {
+  const int nf = ROW_FIELDS[type];
+  T.type = type;
+  T.ncomp = ncomp;
+  T.rows.assign(rows, rows + (size_t)ncomp * nf);
+  T.area.assign(ncomp, 0.0);
+  T.cm.assign(ncomp, 0.0);
+  T.shell.assign(ncomp, 0.0);
+  T.ctype.assign(ncomp, 0);
+  T.cond.assign(NCOND[type], std::vector<double>(ncomp, 0.0));
+  std::vector<double> rad(ncomp), len(ncomp), Ra(ncomp), mat((size_t)ncomp * ncomp, 0.0);
+  std::vector<int> parent(ncomp);
+  // Purkinje channel densities per class (pkj.cuh:29-65): NaF NaP CaP CaT KH KDR KM KA KC K2
+  static const double Gpk[4][10] = {{7500.0, 1.0, 0.0, 0.5, 0.3, 600.0, 0.040, 15.0, 0.0, 0.0},
+                                    {0.0, 0.0, 4.5, 0.5, 0.0, 60.0, 0.01, 2.0, 80.0, 0.39},
+                                    {0.0, 0.0, 4.5, 0.5, 0.0, 0.0, 0.013, 0.0, 80.0, 0.39},
+                                    {0.0, 0.0, 4.5, 0.5, 0.0, 0.0, 0.013, 0.0, 80.0, 0.39}};
+  // inferior-olive densities per class (io.cu:48-82)
+  static const double Gio[3][8] = {{0.016 / (1 * 1.0), 0.0, 0.0, 0.0, 0.0, 4.5 / (1 * 1.0), 35.0 / (1 * 1.0), 0.15 / (1 * 1.0)},
+                                   {0.016, 0.83, 120.0, 9.0, 5.0, 0.0, 0.0, 0.0},
+                                   {0.016, 0.0, 240.0, 0.0, 20.0, 0.0, 0.0, 0.0}};
+  for (int i = 0; i < ncomp; i++) {
+    if ((int)row_f(T.rows, nf, i, 0) != i) return fail(GBRKC_EINVAL, "morphology row %d has index %d", i, (int)row_f(T.rows, nf, i, 0));
+    parent[i] = (int)row_f(T.rows, nf, i, 1);
+    if (parent[i] < -1 || parent[i] >= ncomp || parent[i] == i)
+      return fail(GBRKC_EINVAL, "morphology row %d has parent %d", i, parent[i]);
+    if (type == GR || type == GO) {
+      double d1 = row_f(T.rows, nf, i, 2), d2 = row_f(T.rows, nf, i, 3), d3 = row_f(T.rows, nf, i, 4), d4 = row_f(T.rows, nf, i, 5);
+      int i3 = (int)row_f(T.rows, nf, i, 6);
+      if (i3 < 0 || i3 > 8) return fail(GBRKC_EINVAL, "compartment type %d out of range", i3);
+      rad[i] = 0.5 * d1 * 1e-4; len[i] = d2 * 1e-4; Ra[i] = d3 * 1e-3;
+      T.ctype[i] = i3;
+      T.area[i] = 2.0 * M_PI * rad[i] * len[i];
+      double a = T.area[i];
+      T.cm[i] = d4 * a;
+      for (int k = 0; k < NCOND[type]; k++) T.cond[k][i] = row_f(T.rows, nf, i, 7 + k) * a;
+    } else if (type == PKJ) {
+      double x = row_f(T.rows, nf, i, 2), y = row_f(T.rows, nf, i, 3), z = row_f(T.rows, nf, i, 4), dd = row_f(T.rows, nf, i, 5);
+      int i3 = (int)row_f(T.rows, nf, i, 6);
+      if (i3 < 0 || i3 > 3) return fail(GBRKC_EINVAL, "Purkinje compartment type %d out of range", i3);
+      double a;
+      rad[i] = 0.5 * dd * 1e-4;
+      Ra[i] = PKJ_RI;
+      T.ctype[i] = i3;
+      if (i3 == 0) {
+        len[i] = dd * 1e-4;
+        T.area[i] = 4.0 * M_PI * rad[i] * rad[i];
+        a = T.area[i];
+        T.cm[i] = PKJ_CM * a;
+        T.shell[i] = (PKJ_SHELLD - 2 * pow(PKJ_SHELLD, 2) / (dd * 1e-4) + 4 * pow(PKJ_SHELLD, 3) / (3 * pow(dd * 1e-4, 2))) * T.area[i];
+        T.cond[PK_g_leak][i] = 1.0 / PKJ_RM_S * a;
+      } else {
+        len[i] = sqrt(pow(x, 2) + pow(y, 2) + pow(z, 2)) * 1e-4;
+        T.area[i] = 2.0 * M_PI * rad[i] * len[i];
+        a = T.area[i];
+        T.shell[i] = (PKJ_SHELLD - pow(PKJ_SHELLD, 2) / (dd * 1e-4)) * T.area[i];
+        if (i3 == 3) {
+          double other = a + len[i] * PKJ_SPINE_AREA * PKJ_SPINE_DENS;
+          T.cm[i] = PKJ_CM * other;
+          T.cond[PK_g_leak][i] = 1.0 / PKJ_RM_D * other;
+        } else {
+          T.cm[i] = PKJ_CM * a;
+          T.cond[PK_g_leak][i] = 1.0 / PKJ_RM_D * a;
+        }
+      }
+      for (int k = 0; k < 10; k++) T.cond[1 + k][i] = Gpk[i3][k] * a;
+    } else {
+      double d1 = row_f(T.rows, nf, i, 2), d2 = row_f(T.rows, nf, i, 3), d4 = row_f(T.rows, nf, i, 4);
+      int i3 = (int)row_f(T.rows, nf, i, 5);
+      if (i3 < 0 || i3 > 2) return fail(GBRKC_EINVAL, "IO compartment type %d out of range", i3);
+      rad[i] = 0.5 * d1 * 1e-4; len[i] = d2 * 1e-4;
+      T.ctype[i] = i3;
+      T.area[i] = 2.0 * M_PI * rad[i] * len[i];
+      T.cm[i] = d4;
+      for (int k = 0; k < 8; k++) T.cond[k][i] = Gio[i3][k];
+    }
+  }
+  if (type == IO) {
+    // io_solve.cu:37-65: asymmetric dendrite / soma / axon coupling
+    for (int i = 0; i < ncomp; i++) {
+      int d = parent[i], i3 = T.ctype[i];
+      double lg = 0.0, lgr = 0.0;
+      if (d >= 0) {
+        if (i3 == 0 && d == 1) { lg = (G_INT_IO / (1.0 - G_P_DS_IO)); lgr = (G_INT_IO / (G_P_DS_IO)); }
+        else if (i3 == 1 && d == 2) { lg = (G_INT_IO / (G_P_SA_IO)); lgr = (G_INT_IO / (1.0 - G_P_SA_IO)); }
+        else if (i3 == 0 && d < 1) { lg = lgr = (G_INT_IO / (0.5)); }
+        mat[d + (size_t)ncomp * i] = lg;
+        mat[i + (size_t)ncomp * d] = lgr;
+      }
+    }
+  } else {
+    // gr_solve.cu:37-43 and siblings: 2 / (R_i + R_parent) with R = Ra len / (pi r^2)
+    for (int i = 0; i < ncomp; i++) {
+      int d = parent[i];
+      if (d >= 0) {
+        mat[d + (size_t)ncomp * i] = (2.0 / ((Ra[i] * len[i]) / (rad[i] * rad[i] * M_PI) + (Ra[d] * len[d]) / (rad[d] * rad[d] * M_PI)));
+        mat[i + (size_t)ncomp * d] = mat[d + (size_t)ncomp * i];
+      }
+    }
+  }
+  // dense -> CSR with explicit diagonal, values in the RKC sign convention
+  // (pkj_solve.cu:152-183 then 244-251): off-diagonal +g, diagonal -(sum g)
+  T.row.assign(ncomp + 1, 0);
+  T.col.clear();
+  T.val.clear();
+  for (int r = 0; r < ncomp; r++) {
+    int dig = -1;
+    for (int c = 0; c < ncomp; c++) {
+      double m = mat[(size_t)r * ncomp + c];
+      if (m > 0.0) { T.val.push_back(-m); T.col.push_back(c); }
+      else if (r == c) { dig = (int)T.val.size(); T.val.push_back(0.0); T.col.push_back(c); }
+    }
+    for (int c = 0; c < ncomp; c++)
+      if (c != r) T.val[dig] += mat[(size_t)r * ncomp + c];
+    T.row[r + 1] = (int)T.val.size();
+  }
+  for (double &v : T.val) v = -v;
+  T.invcm.resize(ncomp);
+  for (int i = 0; i < ncomp; i++) T.invcm[i] = 1.0 / T.cm[i];
+  return 0;
+}
+
+// full system CSR of a multi-cell GO/PKJ system with its linear gap junctions
+// (go_solve.cu:51-81,160-196; pkj_solve.cu:4-26,79-120,200-236)
+struct SysCsr {
+  std::vector<int> row, col;
+  std::vector<double> val, invcm;
+};
+
+static int build_system_csr(const HostSystem &S, const Template &T, SysCsr &C) {
+  const int N = S.ncomp, n = S.n, nc = S.nc;
+  std::vector<int> gpre, gpost;
+  double ggj = 0.0;
+  if (S.type == GO) {
+    int gx = S.nx, gy = S.ny;
+    for (int y = 0; y < gy; y++)
+      for (int x = 0; x < gx - 1; x++) { gpre.push_back((y * gx + x) * N); gpre.push_back((y * gx + x + 1) * N); }
+    for (int x = 0; x < gx; x++)
+      for (int y = 0; y < gy - 1; y++) { gpre.push_back((y * gx + x) * N); gpre.push_back(((y + 1) * gx + x) * N); }
+    ggj = G_GJ_GO;
+  } else {
+    int px = S.nx, py = S.ny, G = (int)S.gj_pairs.size() / 2;
+    for (int y = 0; y < py; y++)
+      for (int x = 0; x < px - 1; x++)
+        for (int i = 0; i < G; i++) {
+          int a = S.gj_pairs[2 * i], b = S.gj_pairs[2 * i + 1];
+          if (a < 0 || a >= N || b < 0 || b >= N) return fail(GBRKC_EINVAL, "gap-junction pair (%d,%d) out of range", a, b);
+          gpre.push_back(a + (x + y * px) * N);
+          gpre.push_back(b + ((x + 1) + y * px) * N);
+        }
+    ggj = G_GJ_PKJ;
+  }
+  const int n_gj = (int)gpre.size();
+  gpost.assign(n_gj, 0);
+  for (int i = 0; i < n_gj; i += 2) { gpost[i + 1] = gpre[i]; gpost[i] = gpre[i + 1]; }
+  const int nnz_cell = (int)T.val.size();
+  C.row.assign(nc + 1, 0);
+  C.col.assign((size_t)nnz_cell * n + n_gj, 0);
+  C.val.assign((size_t)nnz_cell * n + n_gj, 0.0);
+  for (int ci = 0; ci < n; ci++) {
+    for (int j = 0; j < nnz_cell; j++) {
+      C.val[j + (size_t)nnz_cell * ci] = T.val[j];
+      C.col[j + (size_t)nnz_cell * ci] = T.col[j] + N * ci;
+    }
+    for (int j = 0; j < N; j++) C.row[j + N * ci] = T.row[j] + nnz_cell * ci;
+  }
+  C.row[nc] = nnz_cell * n;
+  for (int i = 0; i < n_gj; i++) {
+    const int pre = gpre[i], post = gpost[i];
+    for (int j = C.row[pre]; j < C.row[pre + 1]; j++)
+      if (C.col[j] == pre) { C.val[j] -= ggj; break; }
+    int pos = C.row[pre + 1];
+    for (int j = C.row[pre]; j < C.row[pre + 1]; j++) {
+      if (C.col[j] == post) return fail(GBRKC_EINVAL, "duplicate gap junction %d->%d", pre, post);
+      if (C.col[j] > post) { pos = j; break; }
+    }
+    const int used = C.row[nc];
+    for (int j = used; j > pos; j--) { C.col[j] = C.col[j - 1]; C.val[j] = C.val[j - 1]; }
+    C.col[pos] = post;
+    C.val[pos] = ggj;
+    for (int r = pre + 1; r <= nc; r++) C.row[r]++;
+  }
+  C.invcm.resize(nc);
+  for (int i = 0; i < nc; i++) C.invcm[i] = T.invcm[i % N];
+  return 0;
+}
+
+// IO nonlinear gap network (gap.cu:4-120), including idy = id / ny
+static int build_io_gap(HostSystem &S) {
+  const int nx = S.nx, ny = S.ny, n = S.n;
+  if (nx != ny) return fail(GBRKC_EINVAL, "IO gap network needs a square grid (the reference indexes rows by id / ny)");
+  S.gap_pre.assign(4 * n, 0);
+  S.gap_post.assign(4 * n, 0);
+  S.gap_g.assign(4 * n, G_C_IO);
+  for (int id = 0; id < n; id++) {
+    int idx = id % nx, idy = id / ny;
+    int L = id - 1, U = id - nx, R = id + 1, D = id + nx;
+    if (idx == 0 && idy == 0) { L = -1; U = -1; }
+    else if (idx == nx - 1 && idy == 0) { U = -1; R = -1; }
+    else if (idx == 0 && idy == ny - 1) { L = -1; D = -1; }
+    else if (idx == nx - 1 && idy == ny - 1) { R = -1; D = -1; }
+    else if (idy == 0) { U = -1; }
+    else if (idy == ny - 1) { D = -1; }
+    else if (idx == 0) { L = -1; }
+    else if (idx == nx - 1) { R = -1; }
+    const int nb[4] = {L, U, R, D};
+    for (int k = 0; k < 4; k++) {
+      if (nb[k] >= n) return fail(GBRKC_EINVAL, "IO gap neighbour out of range");
+      S.gap_post[id * 4 + k] = id * S.ncomp;
+      S.gap_pre[id * 4 + k] = nb[k] * S.ncomp;
+      if (!S.io_gap_g.empty()) S.gap_g[id * 4 + k] = S.io_gap_g[id * 4 + k];
+    }
+  }
+  return 0;
+}
+
+// Chebyshev stage coefficients per stage count m, computed exactly as the
+// reference's step() does (solve_rkc.cu:826-870), so the device reproduces
+// them bit for bit without transcendental functions.
+static void coef_table(int mmax, std::vector<double> &coef, std::vector<long> &off) {
+  off.assign(mmax + 2, 0);
+  coef.clear();
+  for (int m = 1; m <= mmax; m++) {
+    off[m] = (long)coef.size();
+    double w0 = 1.0 + 2.0 / (13.0 * m * m);
+    double temp1 = w0 * w0 - 1.0;
+    double temp2 = sqrt(temp1);
+    double arg = m * log(w0 + temp2);
+    double w1 = sinh(arg) * temp1 / (cosh(arg) * m * temp2 - w0 * sinh(arg));
+    double bjm1 = 1.0 / ((2.0 * w0) * (2.0 * w0));
+    double bjm2 = bjm1;
+    double mus = w1 * bjm1;
+    coef.push_back(mus);
+    double zjm1 = w0, zjm2 = 1.0, dzjm1 = 1.0, dzjm2 = 0.0, d2zjm1 = 0.0, d2zjm2 = 0.0;
+    for (int j = 1; j < m; j++) {
+      double zj = 2.0 * w0 * zjm1 - zjm2;
+      double dzj = 2.0 * w0 * dzjm1 - dzjm2 + 2.0 * zjm1;
+      double d2zj = 2.0 * w0 * d2zjm1 - d2zjm2 + 4.0 * dzjm1;
+      double bj = d2zj / (dzj * dzj);
+      double ajm1 = 1.0 - zjm1 * bjm1;
+      double mu = 2.0 * w0 * bj / bjm1;
+      double nu = -bj / bjm2;
+      mus = mu * w1 / w0;
+      coef.push_back(mu);
+      coef.push_back(nu);
+      coef.push_back((1.0 - mu - nu));
+      coef.push_back(mus);
+      coef.push_back(ajm1);
+      bjm2 = bjm1; bjm1 = bj; zjm2 = zjm1; zjm1 = zj; dzjm2 = dzjm1; dzjm1 = dzj;
+      d2zjm2 = d2zjm1; d2zjm1 = d2zj;
+    }
+  }
+  off[mmax + 1] = (long)coef.size();
+}
+
+// ----------------------------------------------------------------- pools
+struct DeviceMem {
+  std::vector<void *> ptrs;
+  ~DeviceMem() {
+    for (void *p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  int upload(const std::vector<T> &h, T **d) {
+    size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void **)d, bytes);
+    if (e != cudaSuccess) return fail(GBRKC_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    ptrs.push_back(*d);
+    if (!h.empty()) {
+      e = cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return fail(GBRKC_ECUDA, "cudaMemcpy: %s", cudaGetErrorString(e));
+    }
+    return 0;
+  }
+};
+
+struct PoolHost {
+  int type;
+  std::vector<int> systems;            // engine system ids
+  long nc = 0;
+  int ncell = 0;
+  // per system
+  std::vector<int> sys_off, sys_nc, sys_ncell, sys_ncomp, sys_tmpl, sys_csr, sys_cell0, sys_gap0, sys_ngap;
+  std::vector<long> sys_ws;
+  std::vector<Ctl> ctl;
+  // per compartment
+  std::vector<double> v, ca, ca2, rev, ca_old, iext, shell, area, ion, cond;
+  std::vector<uint8_t> ctype, flags;
+  // templates used by this pool
+  std::vector<int> t_row0, t_nz0, t_cm0, t_row, t_col;
+  std::vector<double> t_g, t_invcm;
+  std::map<int, int> tmpl_local;
+  std::vector<int> s_row0, s_nz0, s_cm0, s_row, s_col;
+  std::vector<double> s_g, s_invcm;
+  std::vector<int> gap_pre, gap_post;
+  std::vector<double> gap_g;
+  std::vector<int> stim_comp, cell_soma;
+  std::vector<double> stim_amp, stim_t0, stim_t1;
+  long ws_total = 0;
+  int max_nc = 0;
+  // launch configuration
+  int team = TEAM_BLOCK, block = 256, grid = 1;
+  size_t smem = 0;
+  int ws_in_smem = 0;
+  long ws_tile = 0;
+  // device views
+  PoolView<double> vd{};
+  PoolView<float> vf{};
+  double *d_ws = nullptr, *d_vnew = nullptr, *d_v = nullptr, *d_ca = nullptr, *d_rev = nullptr, *d_ede = nullptr;
+  void *d_ion = nullptr;
+  Ctl *d_ctl = nullptr;
+  double *d_soma = nullptr;
+  int soma_cap = 0;
+};
+
+}  // namespace gbrkc
+
+using namespace gbrkc;
+
+struct gbrkc_engine {
+  int precision = GBRKC_FP64;
+  bool built = false;
+  std::vector<Template> templates;
+  std::map<std::pair<int, std::vector<double>>, int> tmpl_index;
+  std::vector<HostSystem> systems;
+  std::vector<SysCsr> csrs;
+  PoolHost pools[NTYPES];
+  DeviceMem mem;
+  cudaStream_t streams[NTYPES] = {};
+  std::vector<double> coef;
+  std::vector<long> coef_off;
+  double *d_coef = nullptr;
+  long *d_coef_off = nullptr;
+  int coef_mmax = 0;
+  int soma_cap = 0;
+  int soma_iv = 0;   // intervals recorded so far
+  ~gbrkc_engine() {
+    for (auto &s : streams)
+      if (s) cudaStreamDestroy(s);
+  }
+};
+
+extern "C" const char *gbrkc_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int gbrkc_engine_create(int precision, gbrkc_engine **out) {
+  if (!out || (precision != GBRKC_FP64 && precision != GBRKC_MIXED)) return fail(GBRKC_EINVAL, "bad arguments");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(GBRKC_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  std::unique_ptr<gbrkc_engine> E(new gbrkc_engine());
+  E->precision = precision;
+  for (auto &s : E->streams) CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *out = E.release();
+  return 0;
+}
+
+extern "C" void gbrkc_engine_destroy(gbrkc_engine *e) { delete e; }
+
+extern "C" int gbrkc_add_system(gbrkc_engine *E, const gbrkc_system_desc *d, int *sys_id) {
+  if (!E || !d || !d->rows || !d->jitter) return fail(GBRKC_EINVAL, "null argument");
+  if (E->built) return fail(GBRKC_ESTATE, "engine already built");
+  if (d->cell_type < 0 || d->cell_type >= NTYPES || d->nx <= 0 || d->ny <= 0 || d->ncomp <= 0)
+    return fail(GBRKC_EINVAL, "bad system shape");
+  HostSystem S;
+  S.type = d->cell_type; S.nx = d->nx; S.ny = d->ny; S.n = d->nx * d->ny; S.ncomp = d->ncomp;
+  S.nc = S.n * S.ncomp;
+  S.gap = d->gap_junctions != 0;
+  const int nf = ROW_FIELDS[S.type];
+  std::vector<double> rows(d->rows, d->rows + (size_t)d->ncomp * nf);
+  auto key = std::make_pair(S.type, rows);
+  auto it = E->tmpl_index.find(key);
+  if (it == E->tmpl_index.end()) {
+    Template T;
+    int rc = make_template(S.type, S.ncomp, d->rows, T);
+    if (rc) return rc;
+    E->templates.push_back(std::move(T));
+    it = E->tmpl_index.emplace(key, (int)E->templates.size() - 1).first;
+  }
+  S.tmpl = it->second;
+  if (d->gj_pairs && d->n_gj_pairs > 0) S.gj_pairs.assign(d->gj_pairs, d->gj_pairs + 2 * d->n_gj_pairs);
+  if (d->io_gap_g) S.io_gap_g.assign(d->io_gap_g, d->io_gap_g + 4 * (size_t)S.n);
+  S.jitter.assign(d->jitter, d->jitter + S.n);
+  S.stim_comp.assign(S.n, -1);
+  S.stim_amp.assign(S.n, 0.0); S.stim_t0.assign(S.n, 0.0); S.stim_t1.assign(S.n, 0.0);
+  if (d->stim_comp) {
+    if (!d->stim_amp || !d->stim_t0 || !d->stim_t1) return fail(GBRKC_EINVAL, "incomplete stimulus");
+    for (int c = 0; c < S.n; c++) {
+      if (d->stim_comp[c] >= S.ncomp) return fail(GBRKC_EINVAL, "stimulus compartment out of range");
+      S.stim_comp[c] = d->stim_comp[c];
+      S.stim_amp[c] = d->stim_amp[c]; S.stim_t0[c] = d->stim_t0[c]; S.stim_t1[c] = d->stim_t1[c];
+    }
+  }
+  S.tol = d->tol > 0 ? d->tol : TOL_DEFAULT[S.type];
+  S.hmin = d->hmin > 0 ? d->hmin : pow(2.0, (double)HMIN_LOG2_DEFAULT[S.type]);
+  if (S.n > 1 && S.gap) {
+    if (S.type == IO) {
+      int rc = build_io_gap(S);
+      if (rc) return rc;
+    } else if (S.type == GO || (S.type == PKJ && !S.gj_pairs.empty())) {
+      SysCsr C;
+      int rc = build_system_csr(S, E->templates[S.tmpl], C);
+      if (rc) return rc;
+      E->csrs.push_back(std::move(C));
+      S.csr = (int)E->csrs.size() - 1;
+    }
+  }
+  E->systems.push_back(std::move(S));
+  if (sys_id) *sys_id = (int)E->systems.size() - 1;
+  return 0;
+}
+
+namespace {
+
+int assemble_pool(gbrkc_engine *E, PoolHost &P) {
+  const int type = P.type;
+  const int nion = NION[type], ncond = NCOND[type];
+  // count compartments
+  long nc = 0;
+  int ncell = 0;
+  for (int id : P.systems) { nc += E->systems[id].nc; ncell += E->systems[id].n; }
+  P.nc = nc;
+  P.ncell = ncell;
+  P.v.assign(nc, 0.0); P.ca.assign(nc, 0.0); P.ca2.assign(nc, 0.0); P.rev.assign(nc, 0.0);
+  P.ca_old.assign(nc, 0.0); P.iext.assign(nc, 0.0); P.shell.assign(nc, 0.0); P.area.assign(nc, 0.0);
+  P.ctype.assign(nc, 0); P.flags.assign(nc, 0);
+  P.ion.assign((size_t)nion * nc, 0.0);
+  P.cond.assign((size_t)ncond * nc, 0.0);
+  long off = 0, ws = 0;
+  int cell0 = 0;
+  for (int id : P.systems) {
+    HostSystem &S = E->systems[id];
+    const Template &T = E->templates[S.tmpl];
+    S.pool_index = (int)P.sys_off.size();
+    P.sys_off.push_back((int)off);
+    P.sys_nc.push_back(S.nc);
+    P.sys_ncell.push_back(S.n);
+    P.sys_ncomp.push_back(S.ncomp);
+    P.sys_cell0.push_back(cell0);
+    P.max_nc = std::max(P.max_nc, S.nc);
+    // template (pool-local)
+    auto tl = P.tmpl_local.find(S.tmpl);
+    if (tl == P.tmpl_local.end()) {
+      int li = (int)P.t_row0.size();
+      P.t_row0.push_back((int)P.t_row.size());
+      P.t_nz0.push_back((int)P.t_col.size());
+      P.t_cm0.push_back((int)P.t_invcm.size());
+      // drop the diagonal (it multiplies y_i - y_i = 0); keep column order
+      int cnt = 0;
+      for (int r = 0; r < T.ncomp; r++) {
+        P.t_row.push_back(cnt);
+        for (int j = T.row[r]; j < T.row[r + 1]; j++)
+          if (T.col[j] != r) { P.t_col.push_back(T.col[j]); P.t_g.push_back(T.val[j]); cnt++; }
+      }
+      P.t_row.push_back(cnt);
+      for (double x : T.invcm) P.t_invcm.push_back(x);
+      tl = P.tmpl_local.emplace(S.tmpl, li).first;
+    }
+    P.sys_tmpl.push_back(tl->second);
+    if (S.csr >= 0) {
+      const SysCsr &C = E->csrs[S.csr];
+      P.sys_csr.push_back((int)P.s_row0.size());
+      P.s_row0.push_back((int)P.s_row.size());
+      P.s_nz0.push_back((int)P.s_col.size());
+      P.s_cm0.push_back((int)P.s_invcm.size());
+      int cnt = 0;
+      for (int r = 0; r < S.nc; r++) {
+        P.s_row.push_back(cnt);
+        for (int j = C.row[r]; j < C.row[r + 1]; j++)
+          if (C.col[j] != r) { P.s_col.push_back(C.col[j]); P.s_g.push_back(C.val[j]); cnt++; }
+      }
+      P.s_row.push_back(cnt);
+      for (double x : C.invcm) P.s_invcm.push_back(x);
+    } else {
+      P.sys_csr.push_back(-1);
+    }
+    P.sys_gap0.push_back((int)P.gap_pre.size());
+    P.sys_ngap.push_back((int)S.gap_pre.size());
+    for (size_t e = 0; e < S.gap_pre.size(); e++) {
+      P.gap_pre.push_back(S.gap_pre[e]);
+      P.gap_post.push_back(S.gap_post[e]);
+      P.gap_g.push_back(S.gap_g[e]);
+    }
+    P.sys_ws.push_back(ws);
+    ws += (long)WS_VECS * ((S.nc + 1) & ~1);
+    // per compartment static data and the initial state (*_initialize_ion)
+    const double gcah = (type == IO) ? 0.0 : 0.0;
+    (void)gcah;
+    for (int i = 0; i < S.nc; i++) {
+      const int j = i % S.ncomp, cell = i / S.ncomp;
+      const long g = off + i;
+      P.ctype[g] = (uint8_t)T.ctype[j];
+      P.area[g] = T.area[j];
+      P.shell[g] = T.shell[j];
+      for (int k = 0; k < ncond; k++) P.cond[(size_t)k * nc + g] = T.cond[k][j];
+      CompInit ci;
+      initial_state(type, S.jitter[cell], T.ctype[j], (type == IO) ? T.cond[IO_g_CaH][j] : 0.0, &ci);
+      P.v[g] = ci.v; P.ca[g] = ci.ca; P.ca2[g] = ci.ca2; P.rev[g] = ci.rev; P.ca_old[g] = ci.ca_old;
+      for (int k = 0; k < nion; k++) P.ion[(size_t)k * nc + g] = ci.x[k];
+      if (type == PKJ && (i % 1599 == 0)) P.flags[g] |= 1;  // pkj_ion.cu:329
+    }
+    for (int c = 0; c < S.n; c++) {
+      P.stim_comp.push_back(S.stim_comp[c]);
+      P.stim_amp.push_back(S.stim_amp[c]);
+      P.stim_t0.push_back(S.stim_t0[c]);
+      P.stim_t1.push_back(S.stim_t1[c]);
+      int sc;
+      if (type == PKJ) sc = S.ncomp - 1;
+      else if (type == GO) sc = std::min(30, S.ncomp - 1);
+      else if (type == GR) sc = (S.ncomp == 578) ? 16 : std::min(1, S.ncomp - 1);
+      else sc = std::min(1, S.ncomp - 1);
+      P.cell_soma.push_back((int)(off + (long)c * S.ncomp + sc));
+    }
+    Ctl c{};
+    for (int k = 0; k < 5; k++) c.map[k] = k;
+    c.tend = H_MAX;
+    c.last = 1; c.newspc = 1; c.jacatt = 0;
+    c.tol = S.tol;
+    c.hmin = S.hmin;
+    c.integ = pow(2.0, log10(S.tol));
+    P.ctl.push_back(c);
+    off += S.nc;
+    cell0 += S.n;
+  }
+  P.ws_total = ws;
+  // launch configuration: team shape by system size, workspace in shared
+  // memory when it fits
+  if (P.max_nc <= 8) { P.team = TEAM_TILE4; P.block = 128; }
+  else if (P.max_nc <= 320) { P.team = TEAM_WARP; P.block = 128; }
+  else { P.team = TEAM_BLOCK; P.block = 256; }
+  const int teams = (P.team == TEAM_BLOCK) ? 1 : P.block / P.team;
+  P.ws_tile = (long)WS_VECS * ((P.max_nc + 1) & ~1);
+  const size_t need = (size_t)teams * P.ws_tile * sizeof(double);
+  P.ws_in_smem = need <= 200 * 1024;
+  P.smem = P.ws_in_smem ? need : 0;
+  const int nsys = (int)P.systems.size();
+  P.grid = (nsys + teams - 1) / teams;
+  return 0;
+}
+
+template <typename R>
+int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
+  DeviceMem &M = E->mem;
+  int rc = 0;
+  V.type = P.type;
+  V.nsys = (int)P.systems.size();
+  V.stride = P.nc;
+#define UP(host, dev)                                    \
+  do {                                                   \
+    auto *tmp_ = (decltype(dev))nullptr;                 \
+    using T_ = typename std::remove_const<typename std::remove_pointer<decltype(tmp_)>::type>::type; \
+    T_ *d_ = nullptr;                                    \
+    if ((rc = M.upload<T_>(host, &d_))) return rc;       \
+    dev = d_;                                            \
+  } while (0)
+  UP(P.sys_off, V.sys_off); UP(P.sys_nc, V.sys_nc); UP(P.sys_ncell, V.sys_ncell);
+  UP(P.sys_ncomp, V.sys_ncomp); UP(P.sys_tmpl, V.sys_tmpl); UP(P.sys_csr, V.sys_csr);
+  UP(P.sys_cell0, V.sys_cell0); UP(P.sys_gap0, V.sys_gap0); UP(P.sys_ngap, V.sys_ngap);
+  UP(P.sys_ws, V.sys_ws); UP(P.ctl, V.ctl);
+  std::vector<double> zws(P.ws_total, 0.0);
+  UP(zws, V.ws);
+  std::vector<double> zero(P.nc, 0.0);
+  UP(zero, V.ede); UP(zero, V.vnew);
+  UP(P.v, V.v); UP(P.ca, V.ca); UP(P.ca2, V.ca2); UP(P.rev, V.rev); UP(P.ca_old, V.ca_old);
+  UP(P.iext, V.iext); UP(P.shell, V.shell); UP(P.area, V.area);
+  UP(P.ctype, V.ctype); UP(P.flags, V.flags);
+  std::vector<R> ion(P.ion.begin(), P.ion.end()), cond(P.cond.begin(), P.cond.end());
+  UP(ion, V.ion); UP(cond, V.cond);
+  UP(P.t_row0, V.t_row0); UP(P.t_nz0, V.t_nz0); UP(P.t_cm0, V.t_cm0); UP(P.t_row, V.t_row);
+  UP(P.t_col, V.t_col); UP(P.t_g, V.t_g); UP(P.t_invcm, V.t_invcm);
+  UP(P.s_row0, V.s_row0); UP(P.s_nz0, V.s_nz0); UP(P.s_cm0, V.s_cm0); UP(P.s_row, V.s_row);
+  UP(P.s_col, V.s_col); UP(P.s_g, V.s_g); UP(P.s_invcm, V.s_invcm);
+  UP(P.gap_pre, V.gap_pre); UP(P.gap_post, V.gap_post); UP(P.gap_g, V.gap_g);
+  UP(P.stim_comp, V.stim_comp); UP(P.stim_amp, V.stim_amp); UP(P.stim_t0, V.stim_t0);
+  UP(P.stim_t1, V.stim_t1); UP(P.cell_soma, V.cell_soma);
+#undef UP
+  bool any_stim = false;
+  for (int c : P.stim_comp) any_stim |= (c >= 0);
+  V.stim_on = any_stim;
+  V.coef = E->d_coef;
+  V.coef_off = E->d_coef_off;
+  V.coef_mmax = E->coef_mmax;
+  // granule Na parameters per compartment type (gr_ion.cu:56-70)
+  static const double n1[9] = {1, 1, 1, 1, 1, 5.422, 5.422, 5.422, 5.422};
+  static const double n2[9] = {1, 1, 1, 1, 1, 3.279, 3.279, 3.279, 3.279};
+  static const double n3[9] = {1, 1, 1, 1, 1, 1.83, 1.83, 1.83, 1.83};
+  static const double n4[9] = {1, 1, 1, 1, 1, 0.738, 0.738, 0.738, 0.738};
+  static const double Aa[9] = {1, 1, 1, 1, 1, 8.85, 8.85, 8.85, 8.85};
+  static const double Ab[9] = {1, 1, 1, 1, 1, 0.0318, 0.0318, 0.0318, 0.0318};
+  static const double Vs[9] = {1, 1, 1, 1, 1, -22.0, -22.0, -25.0, -25.0};
+  static const double Con[9] = {1, 1, 1, 1, 1, 0.003464, 0.003464, 0.09353, 0.09353};
+  static const double Coff[9] = {1, 1, 1, 1, 1, 0.4157, 0.4157, 0.04676, 0.04676};
+  static const double Oon[9] = {1, 1, 1, 1, 1, 1.8186, 1.8186, 2.5981, 2.5981};
+  static const double Ooff[9] = {1, 1, 1, 1, 1, 0.006928, 0.006928, 0.000173, 0.000173};
+  for (int t = 0; t < 9; t++) {
+    NaPar &p = V.na[t];
+    p.n1 = n1[t]; p.n2 = n2[t]; p.n3 = n3[t]; p.n4 = n4[t]; p.Aa = Aa[t]; p.Ab = Ab[t]; p.vshift = Vs[t];
+    p.Con = Con[t]; p.Coff = Coff[t]; p.Oon = Oon[t]; p.Ooff = Ooff[t];
+    p.a = pow((Oon[t] / Con[t]), 0.25);
+    p.b = pow((Ooff[t] / Coff[t]), 0.25);
+    p.a4 = pow(p.a, 4.0);
+    p.b4 = pow(p.b, 4.0);
+  }
+  V.soma_out = nullptr;
+  V.ncell_pool = P.ncell;
+  V.ws_in_smem = P.ws_in_smem;
+  V.ws_tile_doubles = P.ws_tile;
+  P.d_ws = V.ws; P.d_vnew = V.vnew; P.d_v = V.v; P.d_ca = V.ca; P.d_rev = V.rev; P.d_ede = V.ede;
+  P.d_ion = (void *)V.ion; P.d_ctl = V.ctl;
+  return prepare_pool_kernel<R>(P.type, P.team, P.smem) ? fail(GBRKC_ECUDA, "cudaFuncSetAttribute failed") : 0;
+}
+
+int launch_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty()) continue;
+    int rc;
+    if (E->precision == GBRKC_FP64)
+      rc = launch_pool<double>(t, P.vd, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
+    else
+      rc = launch_pool<float>(t, P.vf, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
+    if (rc) return fail(GBRKC_ECUDA, "launch (type %d): %s", t, cudaGetErrorString((cudaError_t)rc));
+  }
+  for (int t = 0; t < NTYPES; t++) CUDA_TRY(cudaStreamSynchronize(E->streams[t]));
+  return 0;
+}
+
+int system_loc(gbrkc_engine *E, int id, PoolHost **P, HostSystem **S) {
+  if (!E || id < 0 || id >= (int)E->systems.size()) return fail(GBRKC_EINVAL, "bad system id");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  *S = &E->systems[id];
+  *P = &E->pools[(*S)->type];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int gbrkc_build(gbrkc_engine *E) {
+  if (!E) return fail(GBRKC_EINVAL, "null engine");
+  if (E->built) return fail(GBRKC_ESTATE, "already built");
+  if (E->systems.empty()) return fail(GBRKC_EINVAL, "no systems");
+  E->coef_mmax = 1024;
+  coef_table(E->coef_mmax, E->coef, E->coef_off);
+  {
+    int rc = E->mem.upload(E->coef, &E->d_coef);
+    if (rc) return rc;
+    rc = E->mem.upload(E->coef_off, &E->d_coef_off);
+    if (rc) return rc;
+  }
+  for (int t = 0; t < NTYPES; t++) { E->pools[t] = PoolHost(); E->pools[t].type = t; }
+  for (int id = 0; id < (int)E->systems.size(); id++) E->pools[E->systems[id].type].systems.push_back(id);
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty()) continue;
+    int rc = assemble_pool(E, P);
+    if (rc) return rc;
+    rc = (E->precision == GBRKC_FP64) ? upload_pool<double>(E, P, P.vd) : upload_pool<float>(E, P, P.vf);
+    if (rc) return rc;
+  }
+  E->built = true;
+  int rc = launch_all(E, 0.0, 0, 0, 1);
+  if (rc) { E->built = false; return rc; }
+  return 0;
+}
+
+extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
+  if (!E || n_iv < 0) return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  int iv0 = E->soma_iv;
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    double *so = (E->soma_cap > 0 && iv0 + n_iv <= E->soma_cap) ? P.d_soma : nullptr;
+    P.vd.soma_out = so;
+    P.vf.soma_out = so;
+  }
+  int rc = launch_all(E, t0, n_iv, iv0, 0);
+  if (rc) return rc;
+  if (E->soma_cap > 0) E->soma_iv += n_iv;
+  // a stopped system is reported (its state stays readable)
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty()) continue;
+    std::vector<Ctl> c(P.systems.size());
+    CUDA_TRY(cudaMemcpy(c.data(), P.d_ctl, c.size() * sizeof(Ctl), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < c.size(); i++)
+      if (c[i].status) return fail(GBRKC_ESOLVER, "system %d (type %d) stopped with status %d", P.systems[i], t, c[i].status);
+  }
+  return 0;
+}
+
+extern "C" int gbrkc_read(gbrkc_engine *E, int id, int field, int k, double *host, long n) {
+  PoolHost *P;
+  HostSystem *S;
+  int rc = system_loc(E, id, &P, &S);
+  if (rc) return rc;
+  if (!host || n < 0 || n > S->nc) return fail(GBRKC_EINVAL, "bad buffer");
+  const long off = P->sys_off[S->pool_index];
+  const double *src = nullptr;
+  switch (field) {
+    case GBRKC_F_VNEW: src = P->d_vnew; break;
+    case GBRKC_F_V: src = P->d_v; break;
+    case GBRKC_F_CA: src = P->d_ca; break;
+    case GBRKC_F_REV: src = P->d_rev; break;
+    case GBRKC_F_B:
+    case GBRKC_F_YN: {
+      Ctl c;
+      CUDA_TRY(cudaMemcpy(&c, P->d_ctl + S->pool_index, sizeof c, cudaMemcpyDeviceToHost));
+      const long ncp = (S->nc + 1) & ~1;
+      const long slot = (field == GBRKC_F_B) ? WS_B : c.map[1];
+      CUDA_TRY(cudaMemcpy(host, P->d_ws + P->sys_ws[S->pool_index] + slot * ncp, n * sizeof(double), cudaMemcpyDeviceToHost));
+      return 0;
+    }
+    case GBRKC_F_ION: {
+      if (k < 0 || k >= NION[S->type]) return fail(GBRKC_EINVAL, "bad ion slot");
+      if (E->precision == GBRKC_FP64) {
+        CUDA_TRY(cudaMemcpy(host, (double *)P->d_ion + (size_t)k * P->nc + off, n * sizeof(double), cudaMemcpyDeviceToHost));
+      } else {
+        std::vector<float> tmp(n);
+        CUDA_TRY(cudaMemcpy(tmp.data(), (float *)P->d_ion + (size_t)k * P->nc + off, n * sizeof(float), cudaMemcpyDeviceToHost));
+        for (long i = 0; i < n; i++) host[i] = tmp[i];
+      }
+      return 0;
+    }
+    default: return fail(GBRKC_EINVAL, "bad field");
+  }
+  CUDA_TRY(cudaMemcpy(host, src + off, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int gbrkc_system_ctl(gbrkc_engine *E, int id, double *ctl8, long long *stats6, int *status) {
+  PoolHost *P;
+  HostSystem *S;
+  int rc = system_loc(E, id, &P, &S);
+  if (rc) return rc;
+  Ctl c;
+  CUDA_TRY(cudaMemcpy(&c, P->d_ctl + S->pool_index, sizeof c, cudaMemcpyDeviceToHost));
+  if (ctl8) {
+    ctl8[0] = c.absh; ctl8[1] = c.sprad; ctl8[2] = c.naccpt; ctl8[3] = c.errold;
+    ctl8[4] = c.hold; ctl8[5] = c.lt; ctl8[6] = c.tend; ctl8[7] = c.sum_dt;
+  }
+  if (stats6) {
+    stats6[0] = c.n_steps; stats6[1] = c.n_rej; stats6[2] = c.n_stage; stats6[3] = c.n_rho;
+    stats6[4] = c.n_ion; stats6[5] = c.n_rho_iter;
+  }
+  if (status) *status = c.status;
+  return 0;
+}
+
+extern "C" int gbrkc_system_nc(gbrkc_engine *E, int id) {
+  if (!E || id < 0 || id >= (int)E->systems.size()) return fail(GBRKC_EINVAL, "bad system id");
+  return E->systems[id].nc;
+}
+
+extern "C" long gbrkc_total_compartments(gbrkc_engine *E) {
+  if (!E) return 0;
+  long n = 0;
+  for (auto &s : E->systems) n += s.nc;
+  return n;
+}
+
+extern "C" int gbrkc_record_soma(gbrkc_engine *E, int n_max) {
+  if (!E || n_max < 0) return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  E->soma_cap = n_max;
+  E->soma_iv = 0;
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty() || n_max == 0) { P.d_soma = nullptr; continue; }
+    std::vector<double> z((size_t)n_max * P.ncell, 0.0);
+    int rc = E->mem.upload(z, &P.d_soma);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) {
+  PoolHost *P;
+  HostSystem *S;
+  int rc = system_loc(E, id, &P, &S);
+  if (rc) return rc;
+  if (!P->d_soma || n_iv > E->soma_iv || !host) return fail(GBRKC_EINVAL, "no such recording");
+  const int c0 = P->sys_cell0[S->pool_index];
+  std::vector<double> all((size_t)n_iv * P->ncell);
+  CUDA_TRY(cudaMemcpy(all.data(), P->d_soma, all.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < n_iv; k++)
+    for (int c = 0; c < S->n; c++) host[(size_t)k * S->n + c] = all[(size_t)k * P->ncell + c0 + c];
+  return 0;
+}

@@ -1,0 +1,103 @@
+// Device-side data layout of the RKC engine (shared by the host runtime and
+// the kernels).  All cells of one type live in a "pool"; a pool holds many
+// independent RKC systems (a system is what the reference integrates with one
+// step size: all cells of a reference type block, or one cell, or one
+// inferior-olive gap-junction network).
+//
+// Layout in HBM, per pool:
+//   * per-system workspace, system-major: [PHYS0..PHYS4, B, SCRATCH] x nc
+//     FP64 -- the five rotating RKC vectors (y, yn, fn, vtemp1, vtemp2 of
+//     param.h:21, rotated by index like the reference's pointer swaps), the
+//     frozen current b and a reduction scratch.  Staged into shared memory
+//     for the whole launch when it fits.
+//   * per-compartment SoA state: elem v, Ca, Ca2, rev_ca2, Ca_old, i_ext
+//     (FP64), gating slots ion[k][i] and conductances cond[k][i] (R = FP64 or
+//     FP32), the eigenvector estimate ede and the output v_new (FP64).
+//   * per-template CSR of one cell's axial operator (diagonal dropped, rows
+//     sorted by column, RKC sign), 1/Cm per template compartment; multi-cell
+//     systems with linear gap junctions carry a system CSR instead.
+#pragma once
+#include <stdint.h>
+
+#include "model.h"
+
+namespace gbrkc {
+
+enum { WS_PHYS = 5, WS_B = 5, WS_SCRATCH = 6, WS_VECS = 7 };
+
+// status bits written by the kernel (never a trap)
+enum Status : int {
+  ST_OK = 0,
+  ST_NAN = 1,          // non-finite error norm or step
+  ST_LOOP_CAP = 2,     // step loop exceeded its iteration bound
+  ST_COEF_TABLE = 4,   // stage count beyond the coefficient table
+  ST_IDID = 8,         // rkclow returned an idid other than 1/2 (solve_rkc.cu:1155)
+};
+
+// Controller state of one RKC system (h_others / h_work / h_bool of
+// solve_rkc.cu, plus the driver's static sum_dt and counters).
+struct Ctl {
+  double absh, sprad, naccpt, errold, hold, lt, tend, gt, gt_old, idid, mmax, hw0, hw1;
+  double sum_dt, integ, hmin, tol;
+  int map[5];          // logical {y, yn, fn, vtemp1, vtemp2} -> physical buffer
+  int newspc, jacatt, last, status;
+  long long n_steps, n_rej, n_stage, n_rho, n_rho_iter, n_ion;
+};
+
+// Everything a kernel needs for one pool (passed by value).
+template <typename R>
+struct PoolView {
+  int type, nsys;
+  long stride;                        // pool compartment count (SoA stride)
+  // per system
+  const int *sys_off, *sys_nc, *sys_ncell, *sys_ncomp, *sys_tmpl, *sys_csr, *sys_cell0;
+  const int *sys_gap0, *sys_ngap;
+  const long *sys_ws;                 // workspace offset (doubles)
+  Ctl *ctl;
+  double *ws;
+  // per compartment
+  double *ede, *vnew, *v, *ca, *ca2, *rev, *ca_old, *iext;
+  const double *shell, *area;
+  const uint8_t *ctype, *flags;       // compartment type; bit0 = PKJ fixed Nernst
+  R *ion;
+  const R *cond;
+  // templates
+  const int *t_row0, *t_nz0, *t_cm0;  // per template offsets
+  const int *t_row, *t_col;
+  const double *t_g, *t_invcm;
+  // system CSRs (multi-cell systems with linear gap junctions)
+  const int *s_row0, *s_nz0, *s_cm0;
+  const int *s_row, *s_col;
+  const double *s_g, *s_invcm;
+  // IO nonlinear gap junctions: per system edge list (post compartment, pre or -1)
+  const int *gap_pre, *gap_post;
+  const double *gap_g;
+  // per cell (pool cell index)
+  const int *stim_comp;
+  const double *stim_amp, *stim_t0, *stim_t1;
+  int stim_on;
+  // stage coefficients, per m: [h*mus factor of stage 1, then (mu, nu, 1-mu-nu, mus, ajm1) per stage]
+  const double *coef;
+  const long *coef_off;
+  int coef_mmax;
+  NaPar na[9];
+  // outputs
+  double *soma_out;                   // [interval][pool cell] or null
+  const int *cell_soma;               // per pool cell: compartment index in pool
+  int ncell_pool;
+  int ws_in_smem;                     // stage the workspace in shared memory
+  long ws_tile_doubles;               // shared-memory workspace per team
+};
+
+// Team shapes the kernels are instantiated for: 4 or 32 lanes per system, or
+// a whole block per system.
+enum TeamKind { TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0 };
+
+// Launch the advance / initialise kernel of one pool (kernels.cu).
+template <typename R>
+int launch_pool(int type, const PoolView<R> &P, int team, int grid, int block, size_t smem,
+                void *stream, double t0, int n_iv, int iv0, int init);
+template <typename R>
+int prepare_pool_kernel(int type, int team, size_t smem);
+
+}  // namespace gbrkc

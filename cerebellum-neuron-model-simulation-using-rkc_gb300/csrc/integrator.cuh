@@ -1,0 +1,547 @@
+// Device-resident RKC integrator (Sommeijer, Shampine & Verwer 1998) as the
+// reference drives it: initial vectors and step (RKC_vec_initialize,
+// solve_rkc.cu:438-560,757-791), nonlinear power method for the spectral
+// radius (rkcrho, 563-754), Chebyshev stages (step, 816-906), error norm and
+// step control (rkclow, 909-1096), dense output (rkcint, 795-813) and the
+// per-interval driver with its ion-update clock (*_solve_by_rkc, 1122-1362).
+//
+// One "team" of threads integrates one system; the same code runs with a
+// tile of 1..32 lanes (small cells, many per block) or a whole block (large
+// cells / networks).  Every scalar of the controller is computed redundantly
+// and identically by all team members, so control flow stays uniform within
+// a team and needs no broadcast.  Every sum is the pairwise tree over
+// compartment indices, the FP64 vector updates use the same explicit fused
+// multiply-adds as the oracle's canonical mode, and the translation unit is
+// built with -fmad=false: the plain-FP64 path reproduces the oracle bit for
+// bit.
+#pragma once
+#include "engine.h"
+#include "physics.cuh"
+
+namespace gbrkc {
+
+struct BlockTeam {
+  __device__ __forceinline__ int rank() const { return threadIdx.x; }
+  __device__ __forceinline__ int size() const { return blockDim.x; }
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+
+template <int T>
+struct TileTeam {
+  unsigned mask;
+  int r;
+  __device__ __forceinline__ int rank() const { return r; }
+  __device__ __forceinline__ int size() const { return T; }
+  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+};
+
+// logical vectors of the reference (param.h:21)
+enum { LY = 0, LYN = 1, LFN = 2, LV1 = 3, LV2 = 4 };
+
+constexpr int RKCLOW_LOOP_CAP = 1000;        // solve_rkc.cu:939
+constexpr long STEPS_PER_INTERVAL_CAP = 200000;   // step attempts per 0.125 ms interval
+constexpr int RHO_ITMAX = 1000;              // solve_rkc.cu:572
+
+template <int CT, typename R, class Team>
+struct Sys {
+  const PoolView<R> &P;
+  const Team &tm;
+  int s, nc, ncp, ncell, ncomp, off, cell0;
+  bool csr;
+  const int *row, *col;
+  const double *g, *invcm;
+  double *W;
+  Ctl c;
+
+  __device__ Sys(const PoolView<R> &P_, const Team &tm_, int s_, double *W_) : P(P_), tm(tm_), s(s_), W(W_) {
+    nc = P.sys_nc[s];
+    ncp = (nc + 1) & ~1;
+    ncell = P.sys_ncell[s];
+    ncomp = P.sys_ncomp[s];
+    off = P.sys_off[s];
+    cell0 = P.sys_cell0[s];
+    const int k = P.sys_csr[s];
+    csr = k >= 0;
+    if (csr) {
+      row = P.s_row + P.s_row0[k];
+      col = P.s_col + P.s_nz0[k];
+      g = P.s_g + P.s_nz0[k];
+      invcm = P.s_invcm + P.s_cm0[k];
+    } else {
+      const int t = P.sys_tmpl[s];
+      row = P.t_row + P.t_row0[t];
+      col = P.t_col + P.t_nz0[t];
+      g = P.t_g + P.t_nz0[t];
+      invcm = P.t_invcm + P.t_cm0[t];
+    }
+  }
+
+  __device__ __forceinline__ double *vec(int logical) const { return W + (long)c.map[logical] * ncp; }
+  __device__ __forceinline__ double *bvec() const { return W + (long)WS_B * ncp; }
+  __device__ __forceinline__ double *scratch() const { return W + (long)WS_SCRATCH * ncp; }
+
+  // dydt at compartment i (solve_rkc.cu:178-196): (-b + sum g (y_j - y_i)) / Cm
+  __device__ __forceinline__ double rhs(const double *__restrict__ y, int i) const {
+    double d = -(bvec()[i]);
+    const double yi = y[i];
+    int r0, r1, base, j;
+    if (csr || ncell == 1) {
+      j = i;
+      base = 0;
+    } else {
+      const int cidx = i / ncomp;
+      j = i - cidx * ncomp;
+      base = cidx * ncomp;
+    }
+    r0 = __ldg(row + j);
+    r1 = __ldg(row + j + 1);
+    for (int k = r0; k < r1; k++) d = fma(__ldg(g + k), y[base + __ldg(col + k)] - yi, d);
+    return d * __ldg(invcm + j);
+  }
+
+  // pairwise tree over a[0..n): stride doubling, identical to the oracle
+  __device__ double tree_sum(double *a, int n) const {
+    tm.sync();
+    for (int stride = 1; stride < n; stride *= 2) {
+      const int step = 2 * stride;
+      for (int i = tm.rank() * step; i + stride < n; i += tm.size() * step) a[i] = a[i] + a[i + stride];
+      tm.sync();
+    }
+    const double r = a[0];
+    tm.sync();
+    return r;
+  }
+
+  __device__ double sumsq(const double *a) const {
+    double *sc = scratch();
+    for (int i = tm.rank(); i < nc; i += tm.size()) sc[i] = a[i] * a[i];
+    return tree_sum(sc, nc);
+  }
+
+  // ---------------------------------------------------------------- rkcrho
+  __device__ void rkcrho() {
+    const double uround = UROUND, sqrtu = sqrt(UROUND), small = 1.0 / 0.125;
+    double *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
+    double *ede = P.ede + off, *sc = scratch();
+    double sprad_old[3] = {0.0, 0.0, 0.0};
+    c.n_rho++;
+    const double ynrm = sqrt(sumsq(yn));
+    const double vnrm = sqrt(sumsq(ede));
+    double dynrm;
+    if (ynrm != 0.0 && vnrm != 0.0) {
+      dynrm = ynrm * sqrtu;
+      const double al = dynrm / vnrm;
+      for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = fma(al, ede[i], yn[i]);
+    } else if (ynrm != 0.0) {
+      dynrm = ynrm * sqrtu;
+      for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = fma(sqrtu, yn[i], yn[i]);
+    } else if (vnrm != 0.0) {
+      dynrm = uround;
+      const double al = dynrm / vnrm;
+      for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = al * ede[i];
+    } else {
+      dynrm = uround;
+      for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = dynrm;
+    }
+    tm.sync();
+    double sigma = 0.0, sigmal;
+    for (int iter = 0; iter < RHO_ITMAX; iter++) {
+      c.n_rho_iter++;
+      // v2 = F(v1); dam = v2 - fn; squares into the scratch
+      for (int i = tm.rank(); i < nc; i += tm.size()) {
+        const double f = rhs(v1, i);
+        v2[i] = f;
+        const double dm = -1.0 * fn[i] + f;
+        sc[i] = dm * dm;
+      }
+      const double dfnrm = sqrt(tree_sum(sc, nc));
+      sigmal = sigma;
+      sigma = dfnrm / dynrm;
+      sprad_old[0] = sprad_old[1];
+      sprad_old[1] = sprad_old[2];
+      sprad_old[2] = c.sprad;
+      c.sprad = 1.2 * sigma;
+      if (iter >= 1 && fabs(sigma - sigmal) <= ((sigma > small) ? sigma : small) * 0.001) {
+        for (int i = tm.rank(); i < nc; i += tm.size()) ede[i] = -1.0 * yn[i] + v1[i];
+        tm.sync();
+        return;
+      }
+      if (iter > RHO_ITMAX / 2) {
+        if ((fabs(sprad_old[2] - sprad_old[0]) < 0.00001) && (fabs(sprad_old[1] - c.sprad) < 0.00001)) {
+          c.sprad = (c.sprad + sprad_old[2]) / 2.0;
+          for (int i = tm.rank(); i < nc; i += tm.size()) ede[i] = -1.0 * yn[i] + v1[i];
+          tm.sync();
+          return;
+        }
+      }
+      if (dfnrm != 0.0) {
+        const double al = dynrm / dfnrm;
+        for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = fma(al, fn[i] - v2[i], yn[i]);
+      } else {
+        const int idx = iter % nc;
+        if (tm.rank() == 0) v1[idx] = 2.0 * yn[idx] - v1[idx];
+      }
+      tm.sync();
+    }
+    c.idid = 6;
+  }
+
+  // ----------------------------------------------------------------- step
+  __device__ bool step(double h, int m) {
+    if (m > P.coef_mmax) {
+      c.status |= ST_COEF_TABLE;
+      return false;
+    }
+    const double *T = P.coef + P.coef_off[m];
+    {
+      double *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
+      const double hm = h * __ldg(T);
+      for (int i = tm.rank(); i < nc; i += tm.size()) {
+        v2[i] = yn[i];
+        v1[i] = fma(hm, fn[i], yn[i]);
+      }
+    }
+    tm.sync();
+    for (int j = 1; j < m; j++) {
+      const double *q = T + 1 + 5 * (j - 1);
+      const double mu = __ldg(q), nu = __ldg(q + 1), omn = __ldg(q + 2), mus = __ldg(q + 3), ajm1 = __ldg(q + 4);
+      const double hm = h * mus;
+      double *y = vec(LY), *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
+      for (int i = tm.rank(); i < nc; i += tm.size()) {
+        const double f = rhs(v1, i);
+        double t = mu * v1[i];
+        t = fma(nu, v2[i], t);
+        t = fma(omn, yn[i], t);
+        const double u = fma(-ajm1, fn[i], f);
+        y[i] = fma(hm, u, t);
+      }
+      const int t2 = c.map[LV2];
+      c.map[LV2] = c.map[LV1];
+      c.map[LV1] = c.map[LY];
+      c.map[LY] = t2;
+      tm.sync();
+    }
+    const int t3 = c.map[LY];
+    c.map[LY] = c.map[LV1];
+    c.map[LV1] = c.map[LV2];
+    c.map[LV2] = t3;
+    c.n_stage += m;
+    return true;
+  }
+
+  // --------------------------------------------------------------- rkclow
+  __device__ void rkclow() {
+    const double hmax = H_MAX, hmin = c.hmin;
+    for (int loop = 1; loop <= RKCLOW_LOOP_CAP; loop++) {
+      if (c.newspc) {
+        rkcrho();
+        c.jacatt = 1;
+      }
+      c.last = 0;
+      if (1.1 * c.absh >= fabs(c.tend - c.lt)) {
+        c.absh = fabs(c.tend - c.lt);
+        c.last = 1;
+      }
+      const double marg = sqrt(1.54 * c.absh * c.sprad + 1.0);
+      if (!(marg < 1.0e9)) {
+        c.status |= ST_NAN;
+        return;
+      }
+      int m = 1 + (int)(marg);
+      if (m > c.mmax) {
+        m = (int)c.mmax;
+        c.absh = (m * m - 1) / (1.54 * c.sprad);
+        c.last = 0;
+      }
+      double h = 1.0 * c.absh;
+      if (h <= hmin) h = hmin;
+      if (!step(h, m)) return;
+      c.n_steps++;
+      // F(y) into vtemp1 and the error terms, fused
+      {
+        double *y = vec(LY), *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *sc = scratch();
+        const double h04 = 0.4 * h;
+        for (int i = tm.rank(); i < nc; i += tm.size()) {
+          const double f = rhs(y, i);
+          v1[i] = f;
+          const double ay = fabs(y[i]), ayn = fabs(yn[i]);
+          const double wt = fma(c.tol, (ay > ayn) ? ay : ayn, c.tol);
+          const double est = fma(h04, fn[i] + f, 0.8 * (yn[i] - y[i]));
+          const double qv = est / wt;
+          sc[i] = qv * qv;
+        }
+      }
+      double err = tree_sum(scratch(), nc);
+      err = sqrt(err / (double)nc);
+      if (!(err == err)) {
+        c.status |= ST_NAN;
+        return;
+      }
+      if (err > 1.0) {
+        c.absh = 0.8 * c.absh / (cm_pow(err, 1.0 / 3.0));
+        c.n_rej++;
+        if (c.absh < hmin) {
+          c.idid = 4;
+        } else {
+          c.newspc = !c.jacatt;
+          continue;
+        }
+      }
+      c.naccpt += 1;
+      c.lt += h;
+      c.gt = c.lt;
+      c.jacatt = 0;
+      c.newspc = 0;  // nstsig never advances (solve_rkc.cu:1024-1026)
+      c.hw0 = h;
+      c.hw1 = c.lt;
+      {
+        const int tmp = c.map[LV2];
+        c.map[LV2] = c.map[LFN];
+        c.map[LFN] = c.map[LV1];
+        c.map[LV1] = c.map[LYN];
+        c.map[LYN] = c.map[LY];
+        c.map[LY] = tmp;
+      }
+      double fac = 10.0, temp1, temp2;
+      if (c.naccpt == 1) {
+        temp2 = cm_pow(err, 1.0 / 3.0);
+        if (0.8 < fac * temp2) fac = 0.8 / temp2;
+      } else {
+        temp1 = 0.8 * c.absh * cm_pow(c.errold, 1.0 / 3.0);
+        temp2 = fabs(c.hold) * cm_pow(err, 2.0 / 3.0);
+        if (temp1 < fac * temp2) fac = temp1 / temp2;
+      }
+      c.absh = ((0.1 > fac) ? 0.1 : fac) * c.absh;
+      {
+        const double mn = fmin(hmax, c.absh);
+        c.absh = (hmin > mn) ? hmin : mn;
+      }
+      c.errold = err;
+      c.hold = h;
+      c.idid = c.last ? 1 : 2;
+      tm.sync();
+      return;
+    }
+    c.status |= ST_LOOP_CAP;
+  }
+
+  // ------------------------------------------ ion update + current vector b
+  __device__ void ion_and_b(double sum_dt, bool update_ion, bool with_gap = true) {
+    const double *vy = vec(LY);
+    double *b = bvec();
+    const Slots<R> sl0{P.ion, P.cond, P.stride, 0};
+    for (int i = tm.rank(); i < nc; i += tm.size()) {
+      const long gi = off + i;
+      Slots<R> sl = sl0;
+      sl.i = gi;
+      const double vyi = vy[i];
+      double bi;
+      if (CT == PKJ) {
+        if (update_ion) {
+          double ve = P.v[gi], ca = P.ca[gi], rv = P.rev[gi];
+          Pkj<R>::ion(sl, ve, ca, rv, P.shell[gi], (P.flags[gi] & 1) != 0, vyi, sum_dt);
+          P.v[gi] = ve; P.ca[gi] = ca; P.rev[gi] = rv;
+        }
+        bi = (double)Pkj<R>::b(sl, vyi, P.iext[gi], P.rev[gi]);
+      } else if (CT == IO) {
+        if (update_ion) {
+          double ve = P.v[gi], ca = P.ca[gi];
+          Io<R>::ion(sl, ve, ca, P.ctype[gi], vyi, sum_dt);
+          P.v[gi] = ve; P.ca[gi] = ca;
+        }
+        bi = (double)Io<R>::b(sl, vyi, P.iext[gi]);
+      } else if (CT == GR) {
+        if (update_ion) {
+          const int t = P.ctype[gi];
+          double ve = P.v[gi];
+          if (t >= 5) gr_na<R>(sl, P.na[t], vyi, ve, sum_dt);
+          Gr<R>::ion(sl, ve, P.ca[gi], vyi, sum_dt);
+          P.v[gi] = ve;
+        }
+        bi = (double)Gr<R>::b(sl, vyi, P.iext[gi]);
+      } else {  // GO
+        if (update_ion) {
+          double ve = P.v[gi], ca = P.ca[gi], ca2 = P.ca2[gi], rv = P.rev[gi], cao = P.ca_old[gi];
+          Go<R>::ion(sl, ve, ca, ca2, rv, P.area[gi], vyi, sum_dt);
+          Go<R>::kahp(sl, ca, cao, sum_dt);
+          P.v[gi] = ve; P.ca[gi] = ca; P.ca2[gi] = ca2; P.rev[gi] = rv; P.ca_old[gi] = cao;
+        }
+        bi = (double)Go<R>::b(sl, vyi, P.iext[gi], P.rev[gi]);
+      }
+      b[i] = bi;
+    }
+    if (CT == IO && with_gap && P.sys_ngap[s] > 0) {
+      // io_gap_update + add_io_gap_val: per receiving dendrite, its four
+      // edges in order (the reference adds them with atomics)
+      tm.sync();
+      const int e0 = P.sys_gap0[s], ne = P.sys_ngap[s];
+      for (int cell = tm.rank(); cell < ne / 4; cell += tm.size()) {
+        const int post = P.gap_post[e0 + 4 * cell];
+        double acc = b[post];
+        for (int k = 0; k < 4; k++) {
+          const int e = e0 + 4 * cell + k;
+          const int pre = P.gap_pre[e];
+          const double diff = (pre > -1) ? (P.v[off + post] - P.v[off + pre]) : 0.0;
+          acc += io_gap_current(P.gap_g[e], diff);
+        }
+        b[post] = acc;
+      }
+    }
+    if (update_ion) c.n_ion++;
+    tm.sync();
+  }
+
+  // ----------------------------------------------------- initialisation
+  // RKC_vec_initialize: b from the initial V, vectors, rho, first step
+  __device__ void initialize() {
+    double *y = vec(LY), *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
+    double *ede = P.ede + off;
+    for (int i = tm.rank(); i < nc; i += tm.size()) {
+      const double v0 = P.v[off + i];
+      P.vnew[off + i] = v0;
+      y[i] = v0;
+      yn[i] = v0;
+      v1[i] = 0.0;
+      v2[i] = 0.0;
+    }
+    tm.sync();
+    // b from the initial voltage (update_matrix only, no gap currents):
+    // the b pass reads vec(LY) = initial V
+    ion_and_b(0.0, false, false);
+    for (int i = tm.rank(); i < nc; i += tm.size()) {
+      const double f = rhs(yn, i);
+      fn[i] = f;
+      ede[i] = f;
+    }
+    tm.sync();
+    rkcrho();
+    // set_initial_absh (solve_rkc.cu:493-560)
+    double absh = H_MAX;
+    if (c.sprad * absh > 1.0) absh = 1.0 / c.sprad;
+    absh = (absh > c.hmin) ? absh : c.hmin;
+    for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = fma(absh, fn[i], yn[i]);
+    tm.sync();
+    double *sc = scratch();
+    int bad = 0;
+    for (int i = tm.rank(); i < nc; i += tm.size()) {
+      const double f = rhs(v1, i);
+      v2[i] = f;
+      const double wt = fma(c.tol, fabs(yn[i]), c.tol);
+      if (wt == 0.0) bad = 1;
+      const double dm = (f - fn[i]) * (1.0 / wt);
+      sc[i] = dm * dm;
+    }
+    double est = tree_sum(sc, nc);
+    if (bad) c.idid = 3.0;
+    est = absh * sqrt(est / nc);
+    if (0.1 * absh < H_MAX * sqrt(est)) {
+      const double a2 = 0.1 * absh / sqrt(est);
+      absh = (a2 > c.hmin) ? a2 : c.hmin;
+    } else {
+      absh = H_MAX;
+    }
+    c.absh = absh;
+    {
+      const double x = sqrt(c.tol / (10.0 * UROUND));
+      c.mmax = (x - (double)(int)x < 0.5) ? (double)(int)x : (double)(int)(x + 0.9);
+    }
+  }
+
+  // ---------------------------------------------------- one output interval
+  // *_set_current at t, then *_solve_by_rkc (solve_rkc.cu:1122-1362)
+  __device__ bool interval(double t) {
+    if (P.stim_on) {
+      for (int cc = tm.rank(); cc < ncell; cc += tm.size()) {
+        const int pc = cell0 + cc;
+        const int comp = P.stim_comp[pc];
+        if (comp >= 0) {
+          const long gi = off + (long)cc * ncomp + comp;
+          P.iext[gi] = 0;
+          if (P.stim_t0[pc] <= t && t < P.stim_t1[pc]) P.iext[gi] = P.stim_amp[pc];
+        }
+      }
+      tm.sync();
+    }
+    const bool ge = (CT == GO || CT == PKJ);
+    if (c.sum_dt != 0.0) {
+      ion_and_b(c.sum_dt, true);
+      c.sum_dt = 0.0;
+    }
+    const long attempts0 = c.n_steps;
+    for (;;) {
+      rkclow();
+      if (c.status) return false;
+      if (c.n_steps - attempts0 > STEPS_PER_INTERVAL_CAP) {
+        c.status |= ST_LOOP_CAP;
+        return false;
+      }
+      c.sum_dt += c.gt - c.gt_old;
+      c.gt_old = c.gt;
+      const bool trig = ge ? (c.sum_dt >= c.integ) : (c.sum_dt > c.integ);
+      if (trig && c.idid == 2.0) {
+        ion_and_b(c.sum_dt, true);
+        c.sum_dt = 0.0;
+      }
+      if (c.idid == 2.0) {
+        continue;
+      } else if (c.idid == 1.0) {
+        break;
+      } else {
+        c.status |= ST_IDID;
+        return false;
+      }
+    }
+    // rkcint
+    {
+      const double hlast = c.hw0, tlast = c.hw1 - hlast;
+      const double sv = (c.gt_old - tlast) / hlast;
+      const double a1 = (1.0 + 2.0 * sv) * (sv - 1.0) * (sv - 1.0);
+      const double a2 = (3.0 - 2.0 * sv) * sv * sv;
+      const double b1 = hlast * sv * (sv - 1.0) * (sv - 1.0);
+      const double b2 = hlast * (sv - 1.0) * sv * sv;
+      const double *v1 = vec(LV1), *v2 = vec(LV2), *yn = vec(LYN), *fn = vec(LFN);
+      for (int i = tm.rank(); i < nc; i += tm.size())
+        P.vnew[off + i] = fma(b2, fn[i], fma(b1, v2[i], fma(a2, yn[i], a1 * v1[i])));
+    }
+    c.tend += H_MAX;
+    tm.sync();
+    return true;
+  }
+};
+
+// Stage a system's workspace between HBM and shared memory.
+template <class Team>
+__device__ void ws_copy(const Team &tm, double *dst, const double *src, long n) {
+  for (long i = tm.rank(); i < n; i += tm.size()) dst[i] = src[i];
+  tm.sync();
+}
+
+// Advance one system by n_iv intervals starting at t0 (or initialise it).
+template <int CT, typename R, class Team>
+__device__ void run_system(const PoolView<R> &P, const Team &tm, int s, double *smem_ws, double t0,
+                           int n_iv, int iv0_global, bool init) {
+  const long wsn = (long)WS_VECS * (long)((P.sys_nc[s] + 1) & ~1);
+  double *gws = P.ws + P.sys_ws[s];
+  double *W = P.ws_in_smem ? smem_ws : gws;
+  if (P.ws_in_smem) ws_copy(tm, W, gws, wsn);
+  Sys<CT, R, Team> S(P, tm, s, W);
+  S.c = P.ctl[s];
+  if (init) {
+    S.initialize();
+  } else if (S.c.status == 0) {
+    for (int k = 0; k < n_iv; k++) {
+      if (!S.interval(t0 + k * H_MAX)) break;
+      if (P.soma_out) {
+        for (int cc = tm.rank(); cc < S.ncell; cc += tm.size()) {
+          const int pc = S.cell0 + cc;
+          P.soma_out[(long)(iv0_global + k) * P.ncell_pool + pc] = P.vnew[P.cell_soma[pc]];
+        }
+      }
+    }
+  }
+  tm.sync();
+  if (P.ws_in_smem) ws_copy(tm, gws, W, wsn);
+  if (tm.rank() == 0) P.ctl[s] = S.c;
+}
+
+}  // namespace gbrkc

@@ -1,0 +1,6 @@
+// Plain-FP64 instantiations of the advance kernel (FP64 gating).
+#include "kernels.cu"
+namespace gbrkc {
+template int launch_pool<double>(int, const PoolView<double> &, int, int, int, size_t, void *, double, int, int, int);
+template int prepare_pool_kernel<double>(int, int, size_t);
+}  // namespace gbrkc

@@ -1,0 +1,173 @@
+"""Python binding of the gbrkc C ABI (include/gbrkc.h) over ctypes.
+
+Thin by design: every call goes straight to libgbrkc.so; there is no Python or
+CPU fallback.  If the native library is missing or no CUDA device is present
+the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbrkc.so")
+
+GR, GO, PKJ, IO = 0, 1, 2, 3
+FP64, MIXED = 0, 1
+F_VNEW, F_V, F_CA, F_B, F_ION, F_REV, F_YN = 0, 1, 2, 3, 4, 5, 6
+H_MAX = 0.125
+STATUS_BITS = {1: "non-finite error norm", 2: "step loop bound", 4: "stage count beyond table",
+               8: "unexpected idid"}
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [
+        ("cell_type", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("ncomp", C.c_int),
+        ("rows", C.POINTER(C.c_double)), ("gj_pairs", C.POINTER(C.c_int)), ("n_gj_pairs", C.c_int),
+        ("gap_junctions", C.c_int), ("io_gap_g", C.POINTER(C.c_double)),
+        ("jitter", C.POINTER(C.c_double)), ("stim_comp", C.POINTER(C.c_int)),
+        ("stim_amp", C.POINTER(C.c_double)), ("stim_t0", C.POINTER(C.c_double)),
+        ("stim_t1", C.POINTER(C.c_double)), ("tol", C.c_double), ("hmin", C.c_double),
+    ]
+
+
+_LIB = None
+
+
+def lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} not built: run __graft_entry__.build() (no fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        L.gbrkc_engine_create.argtypes = [C.c_int, C.POINTER(P)]
+        L.gbrkc_engine_destroy.argtypes = [P]
+        L.gbrkc_add_system.argtypes = [P, C.POINTER(SystemDesc), C.POINTER(C.c_int)]
+        L.gbrkc_build.argtypes = [P]
+        L.gbrkc_advance.argtypes = [P, C.c_double, C.c_int]
+        L.gbrkc_read.argtypes = [P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_long]
+        L.gbrkc_system_ctl.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
+                                       C.POINTER(C.c_int)]
+        L.gbrkc_system_nc.argtypes = [P, C.c_int]
+        L.gbrkc_record_soma.argtypes = [P, C.c_int]
+        L.gbrkc_read_soma.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.gbrkc_total_compartments.argtypes = [P]
+        L.gbrkc_total_compartments.restype = C.c_long
+        L.gbrkc_last_error.restype = C.c_char_p
+        _LIB = L
+    return _LIB
+
+
+class GbrkcError(RuntimeError):
+    pass
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise GbrkcError(f"gbrkc error {rc}: {lib().gbrkc_last_error().decode()}")
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class Engine:
+    """A set of RKC systems advanced together on the GPU."""
+
+    def __init__(self, precision: int = FP64):
+        self.h = C.c_void_p()
+        _check(lib().gbrkc_engine_create(precision, C.byref(self.h)))
+        self.precision = precision
+        self._keep = []
+        self.ncomp = {}
+
+    def close(self):
+        if self.h:
+            lib().gbrkc_engine_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_system(self, cell_type, nx, ny, rows, jitter, stim=None, gj_pairs=None, gap=True,
+                   io_gap_g=None, tol=0.0, hmin=0.0) -> int:
+        n = nx * ny
+        rows = np.ascontiguousarray(rows, dtype=np.float64)
+        jitter = np.ascontiguousarray(jitter, dtype=np.float64)
+        assert jitter.size == n
+        d = SystemDesc()
+        d.cell_type, d.nx, d.ny, d.ncomp = cell_type, nx, ny, rows.shape[0]
+        d.rows, d.jitter = _dp(rows), _dp(jitter)
+        keep = [rows, jitter]
+        if gj_pairs is not None:
+            g = np.ascontiguousarray(gj_pairs, dtype=np.int32).reshape(-1)
+            d.gj_pairs, d.n_gj_pairs = _ip(g), g.size // 2
+            keep.append(g)
+        d.gap_junctions = int(gap)
+        if io_gap_g is not None:
+            gg = np.ascontiguousarray(io_gap_g, dtype=np.float64)
+            d.io_gap_g = _dp(gg)
+            keep.append(gg)
+        if stim is not None:
+            comp, amp, t0, t1 = stim
+            comp = np.ascontiguousarray(np.broadcast_to(comp, n), dtype=np.int32)
+            amp, t0, t1 = (np.ascontiguousarray(np.broadcast_to(a, n), dtype=np.float64) for a in (amp, t0, t1))
+            d.stim_comp, d.stim_amp, d.stim_t0, d.stim_t1 = _ip(comp), _dp(amp), _dp(t0), _dp(t1)
+            keep += [comp, amp, t0, t1]
+        d.tol, d.hmin = tol, hmin
+        sid = C.c_int()
+        _check(lib().gbrkc_add_system(self.h, C.byref(d), C.byref(sid)))
+        self._keep.append(keep)
+        self.ncomp[sid.value] = (cell_type, n, rows.shape[0])
+        return sid.value
+
+    def build(self):
+        _check(lib().gbrkc_build(self.h))
+        self._keep = []
+
+    def advance(self, t0: float, n_intervals: int):
+        _check(lib().gbrkc_advance(self.h, t0, n_intervals))
+
+    def nc(self, sid: int) -> int:
+        return lib().gbrkc_system_nc(self.h, sid)
+
+    def read(self, sid: int, field: int, k: int = 0) -> np.ndarray:
+        n = self.nc(sid)
+        out = np.empty(n, dtype=np.float64)
+        _check(lib().gbrkc_read(self.h, sid, field, k, _dp(out), n))
+        return out
+
+    def vnew(self, sid):
+        return self.read(sid, F_VNEW)
+
+    def ctl(self, sid):
+        c = np.zeros(8)
+        st = np.zeros(6, dtype=np.int64)
+        status = C.c_int()
+        _check(lib().gbrkc_system_ctl(self.h, sid, _dp(c), st.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                      C.byref(status)))
+        ctl = dict(zip(["absh", "sprad", "naccpt", "errold", "hold", "lt", "tend", "sum_dt"], c))
+        stats = dict(zip(["steps", "rejects", "stages", "rho_calls", "ion_updates", "rho_iters"], st.tolist()))
+        return ctl, stats, status.value
+
+    def record_soma(self, n_max: int):
+        _check(lib().gbrkc_record_soma(self.h, n_max))
+
+    def read_soma(self, sid: int, n_intervals: int) -> np.ndarray:
+        _, n, _ = self.ncomp[sid]
+        out = np.empty((n_intervals, n), dtype=np.float64)
+        _check(lib().gbrkc_read_soma(self.h, sid, n_intervals, _dp(out)))
+        return out
+
+    def total_compartments(self) -> int:
+        return lib().gbrkc_total_compartments(self.h)

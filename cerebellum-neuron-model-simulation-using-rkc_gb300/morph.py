@@ -136,8 +136,12 @@ def pkj_synthetic(seed: int, ncomp: int = 1600) -> np.ndarray:
     dendrite of ncomp-1 segments: segment length U[5,20] um along a random
     direction, diameter lognormal (median 1.5 um, sigma_ln 0.5) clipped to
     [0.5, 8] um; compartment type by depth: main (1) for depth <= 3, smooth (2)
-    for depth <= 8, spiny (3) beyond.  Parents always carry a higher index
-    than their children, as in the reference file."""
+    for depth <= 8, spiny (3) beyond.  The lognormal median is tapered by
+    class like the reference tree (main x5.5, smooth x3, spiny x1: mean
+    diameters 8.4 / 4.6 / 1.5 um in Pkj.txt); without the thick trunk the soma
+    is too weakly loaded for the frozen-current RKC splitting at 0.5 nA.
+    Parents always carry a higher index than their children, as in the
+    reference file."""
     rng = np.random.default_rng(seed)
     nd = ncomp - 1
     parent, depth = _random_binary_tree(rng, nd, root_children=1)
@@ -152,9 +156,9 @@ def pkj_synthetic(seed: int, ncomp: int = 1600) -> np.ndarray:
         u = rng.standard_normal(3)
         u /= np.linalg.norm(u)
         x, y, z = (L * u).tolist()
-        dd = _lognormal_diam(rng)
         dep = depth[old]
         ctype = 1 if dep <= 3 else (2 if dep <= 8 else 3)
+        dd = _lognormal_diam(rng, median=1.5 * {1: 5.5, 2: 3.0, 3: 1.0}[ctype])
         rows[i] = [i, pi, x, y, z, dd, ctype]
     rows[ncomp - 1] = [ncomp - 1, -1, 0.0, 0.0, 0.0, 29.8, 0]
     return rows

@@ -1,0 +1,106 @@
+/*
+ * gbrkc: GB300-native explicit Runge-Kutta-Chebyshev (RKC) solver for the
+ * reference's cerebellar multi-compartment cell models -- C ABI.
+ *
+ * An engine owns device memory for many RKC "systems".  A system is what the
+ * reference integrates with one step size: the nx*ny cells of one type with
+ * their gap junctions (the reference's per-type block, main.cu:105-134), or a
+ * single cell, or one inferior-olive gap-junction network.  Every system
+ * keeps its own step size, stage count, spectral radius and ion-update clock,
+ * exactly as the reference's *_solve_by_rkc does for its one system per type
+ * (solve_rkc.cu:1122-1362); batching only changes packing.
+ *
+ * All functions return 0 on success or a negative GBRKC_E* code; the message
+ * is available from gbrkc_last_error().  Plain pointers and sizes only.
+ */
+#ifndef GBRKC_H
+#define GBRKC_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gbrkc_engine gbrkc_engine;
+
+enum { GBRKC_GR = 0, GBRKC_GO = 1, GBRKC_PKJ = 2, GBRKC_IO = 3 };
+enum { GBRKC_FP64 = 0, GBRKC_MIXED = 1 };
+enum {
+  GBRKC_OK = 0,
+  GBRKC_EINVAL = -1,   /* bad argument */
+  GBRKC_ECUDA = -2,    /* CUDA error (no device, launch failure, ...) */
+  GBRKC_ESTATE = -3,   /* call out of order (e.g. add after build) */
+  GBRKC_ENOMEM = -4,   /* device allocation failed */
+  GBRKC_ESOLVER = -5   /* a system stopped: see gbrkc_system_ctl status */
+};
+/* fields readable with gbrkc_read */
+enum {
+  GBRKC_F_VNEW = 0,    /* vec[v_new]: voltage at the end of the last interval */
+  GBRKC_F_V = 1,       /* elem[v]: voltage the gating last saw */
+  GBRKC_F_CA = 2,      /* elem[Ca] */
+  GBRKC_F_B = 3,       /* frozen current vector b */
+  GBRKC_F_ION = 4,     /* gating slot k (as FP64) */
+  GBRKC_F_REV = 5,     /* Ca reversal potential (GO, PKJ) */
+  GBRKC_F_YN = 6       /* RKC solution vector yn */
+};
+
+typedef struct gbrkc_system_desc {
+  int cell_type;            /* GBRKC_GR .. GBRKC_IO */
+  int nx, ny;               /* cells of the system, on an nx x ny grid */
+  int ncomp;                /* compartments per cell */
+  const double *rows;       /* ncomp rows in the reference's parameter-file layout
+                               (Gr.txt 17, Go_131.txt 20, Pkj.txt 7, IO.txt 6 fields) */
+  const int *gj_pairs;      /* PKJ: (pre, post) compartment pairs between x-neighbours */
+  int n_gj_pairs;
+  int gap_junctions;        /* 1: the reference's gap junctions for this type when
+                               nx*ny > 1 (GO and PKJ linear in the operator, IO nonlinear) */
+  const double *io_gap_g;   /* IO: 4*nx*ny edge conductances, or NULL for the reference's */
+  const double *jitter;     /* nx*ny initial-voltage jitters (init_v_rand of *_initialize_ion) */
+  const int *stim_comp;     /* nx*ny stimulated compartment per cell or -1; NULL: no stimulus */
+  const double *stim_amp;   /* step current amplitude ... */
+  const double *stim_t0;    /* ... switched on at t0 (ms) ... */
+  const double *stim_t1;    /* ... and off at t1, evaluated at each interval start */
+  double tol;               /* RKC rtol = atol; <= 0: reference per-type value */
+  double hmin;              /* minimum step (ms); <= 0: reference per-type value */
+} gbrkc_system_desc;
+
+/* Create an engine on the current CUDA device.  precision: GBRKC_FP64 (plain
+ * FP64 everywhere) or GBRKC_MIXED (FP32 gating, channel currents and b; FP64
+ * voltage, stages, spectral radius and step control). */
+int gbrkc_engine_create(int precision, gbrkc_engine **out);
+void gbrkc_engine_destroy(gbrkc_engine *e);
+
+/* Register a system (host copies are taken); returns its id. */
+int gbrkc_add_system(gbrkc_engine *e, const gbrkc_system_desc *d, int *sys_id);
+
+/* Allocate and upload everything, then initialise every system on the device
+ * (RKC_vec_initialize, solve_rkc.cu:757-791). */
+int gbrkc_build(gbrkc_engine *e);
+
+/* Advance every system by n_intervals output intervals of 0.125 ms, the
+ * first one starting at time t0 (ms), in one device-resident launch per cell
+ * type.  Equivalent to the reference's main loop calling *_set_current and
+ * *_solve_update_v once per interval (main.cu:182-311). */
+int gbrkc_advance(gbrkc_engine *e, double t0, int n_intervals);
+
+/* Copy n values of a per-compartment field of one system to host memory. */
+int gbrkc_read(gbrkc_engine *e, int sys_id, int field, int k, double *host, long n);
+
+/* Controller scalars (absh sprad naccpt errold hold lt tend sum_dt), counters
+ * (steps rejects stages rho_calls ion_updates rho_iterations) and status. */
+int gbrkc_system_ctl(gbrkc_engine *e, int sys_id, double *ctl8, long long *stats6, int *status);
+int gbrkc_system_nc(gbrkc_engine *e, int sys_id);
+
+/* Record the soma voltage of every cell at the end of each interval for the
+ * next n_intervals_max intervals (0 disables); read them per system as
+ * [interval][cell]. */
+int gbrkc_record_soma(gbrkc_engine *e, int n_intervals_max);
+int gbrkc_read_soma(gbrkc_engine *e, int sys_id, int n_intervals, double *host);
+
+/* Total compartments, and the CUDA stream pools launch on (one per type). */
+long gbrkc_total_compartments(gbrkc_engine *e);
+const char *gbrkc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

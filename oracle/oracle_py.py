@@ -28,6 +28,7 @@ class Desc(C.Structure):
         ("io_gap_g", C.POINTER(C.c_double)),
         ("tol", C.c_double), ("hmin", C.c_double),
         ("io_gap", C.c_int), ("go_gj", C.c_int), ("pkj_gj", C.c_int),
+        ("canon", C.c_int),
     ]
 
 
@@ -98,7 +99,8 @@ class System:
     """One RKC system of the oracle (all cells of one type on an nx x ny grid)."""
 
     def __init__(self, cell_type, nx, ny, rows, jitter, stim=None, gj_pairs=None,
-                 tol=0.0, hmin=0.0, io_gap=True, go_gj=True, pkj_gj=True, io_gap_g=None):
+                 tol=0.0, hmin=0.0, io_gap=True, go_gj=True, pkj_gj=True, io_gap_g=None,
+                 canon=False):
         L = lib()
         self._keep = []
         rows = np.ascontiguousarray(rows, dtype=np.float64)
@@ -127,6 +129,7 @@ class System:
             self._keep.append(gg)
         d.tol, d.hmin = tol, hmin
         d.io_gap, d.go_gj, d.pkj_gj = int(io_gap), int(go_gj), int(pkj_gj)
+        d.canon = int(canon)
         self.h = L.orc_create(C.byref(d))
         if not self.h:
             raise RuntimeError("orc_create failed")
@@ -198,9 +201,10 @@ class System:
         return dict(zip(["absh", "sprad", "naccpt", "errold", "hold", "lt", "tend", "sum_dt"], out))
 
     def stats(self):
-        out = np.zeros(5, dtype=np.int64)
+        out = np.zeros(6, dtype=np.int64)
         lib().orc_stats(self.h, out.ctypes.data_as(C.POINTER(C.c_longlong)))
-        return dict(zip(["steps", "rejects", "stages", "rho_calls", "ion_updates"], out.tolist()))
+        return dict(zip(["steps", "rejects", "stages", "rho_calls", "ion_updates", "rho_iters"],
+                        out.tolist()))
 
     def ion_update(self, vnew, dt):
         v = np.ascontiguousarray(vnew, dtype=np.float64)

@@ -7,6 +7,7 @@
  * Every function names the reference file:line it restates.
  */
 #include "rkc_oracle.h"
+#include "canon_math.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -129,11 +130,30 @@ struct orc_sys {
   int ngap;
   int *gap_pre, *gap_post;
   double *gap_cur, *gap_g;
+  int canon;
+  double *invcm, *scratch;
   /* counters */
-  long long n_steps, n_rej, n_stage, n_rho, n_ion;
+  long long n_steps, n_rej, n_stage, n_rho, n_ion, n_rho_iter;
 };
 
 #define VEC(s, L) ((s)->phys[(s)->map[L]])
+
+/* Canonical mode (see canon_math.h): the platform exp/log/pow are replaced by
+ * the agreed implementations, the vector updates use the GPU path's explicit
+ * fused multiply-adds, 1/Cm is a multiply, and every sum is the pairwise
+ * tree below.  Reference mode keeps the reference's literal expressions. */
+static int g_canon = 0;
+#define EXP(x) (g_canon ? cm_exp(x) : exp(x))
+#define LOG(x) (g_canon ? cm_log(x) : log(x))
+#define POW(x, y) (g_canon ? cm_pow((x), (y)) : pow((x), (y)))
+
+/* pairwise tree over indices 0..n-1 (stride doubling, in place) */
+static double tree_sum(double *a, int n) {
+  if (n <= 0) return 0.0;
+  for (int stride = 1; stride < n; stride *= 2)
+    for (int i = 0; i + stride < n; i += 2 * stride) a[i] = a[i] + a[i + stride];
+  return a[0];
+}
 
 static double *zalloc(size_t n) { return (double *)calloc(n ? n : 1, sizeof(double)); }
 static int *ialloc(size_t n) { return (int *)calloc(n ? n : 1, sizeof(int)); }
@@ -152,7 +172,7 @@ int orc_row_fields(int type) {
 /* PKJ rate functions (pkj_ion.cu:4-91)                                 */
 /* ------------------------------------------------------------------ */
 static double pk_l(double v, double A, double B, double C, double D) {
-  return A / (B + exp((v + C) / D));
+  return A / (B + EXP((v + C) / D));
 }
 static double pk_am_NaF(double v) { return pk_l(v, 35.0, 0.0, 5.0, -10.0); }
 static double pk_ah_NaF(double v) { return pk_l(v, 0.225, 1.0, 80.0, 10.0); }
@@ -194,28 +214,28 @@ static double pk_m_KC_inf(double v) { return 7.5 / (7.5 + pk_bm_KC(v)); }
 static double pk_m_KC_tau(double v) { return 1.0 / (7.5 + pk_bm_KC(v)); }
 static double pk_m_K2_inf(double v) { return 25.0 / (25.0 + pk_bm_K2(v)); }
 static double pk_m_K2_tau(double v) { return 1.0 / (25.0 + pk_bm_K2(v)); }
-static double pk_m_Kh1_inf(double v) { return 0.8 / (1.0 + exp((v + 82.0) / 7.0)); }
-static double pk_m_Kh2_inf(double v) { return 0.2 / (1.0 + exp((v + 82.0) / 7.0)); }
+static double pk_m_Kh1_inf(double v) { return 0.8 / (1.0 + EXP((v + 82.0) / 7.0)); }
+static double pk_m_Kh2_inf(double v) { return 0.2 / (1.0 + EXP((v + 82.0) / 7.0)); }
 static double pk_m_Kdr_tau(double v) {
   double a;
-  if (fabs(v + 12.0) > 1e-6) a = -0.0235 * (v + 12.0) / (exp(-(v + 12.0) / 12.0) - 1.0);
+  if (fabs(v + 12.0) > 1e-6) a = -0.0235 * (v + 12.0) / (EXP(-(v + 12.0) / 12.0) - 1.0);
   else a = 0.0235 * 12.0;
-  double b = 5.0 * exp(-(v + 147.0) / 30.0);
+  double b = 5.0 * EXP(-(v + 147.0) / 30.0);
   return 1.0 / (a + b);
 }
 static double pk_m_Kdr_inf(double v) {
   double a;
-  if (fabs(v - 8.0) > 1e-6) a = -0.0235 * (v - 8.0) / (exp(-(v - 8.0) / 12.0) - 1.0);
+  if (fabs(v - 8.0) > 1e-6) a = -0.0235 * (v - 8.0) / (EXP(-(v - 8.0) / 12.0) - 1.0);
   else a = 0.0235 * 12.0;
-  double b = 5.0 * exp(-(v + 127.0) / 30.0);
+  double b = 5.0 * EXP(-(v + 127.0) / 30.0);
   return a / (a + b);
 }
 static double pk_h_Kdr_tau(double v) { return (v < -25.0) ? 1200.0 : 10.0; }
-static double pk_h_Kdr_inf(double v) { return 1.0 / (1.0 + exp((v + 25.0) / 4.0)); }
+static double pk_h_Kdr_inf(double v) { return 1.0 / (1.0 + EXP((v + 25.0) / 4.0)); }
 static double pk_m_KM_tau(double v) {
-  return 200.0 / (3.3 * (exp((v + 35.0) / 20.0)) + exp(-(v + 35.0) / 20.0));
+  return 200.0 / (3.3 * (EXP((v + 35.0) / 20.0)) + EXP(-(v + 35.0) / 20.0));
 }
-static double pk_m_KM_inf(double v) { return 1.0 / (1.0 + exp(-(v + 35.0) / 10.0)); }
+static double pk_m_KM_inf(double v) { return 1.0 / (1.0 + EXP(-(v + 35.0) / 10.0)); }
 static double pk_z_KC_inf(double ca) { return 1.0 / (1.0 + 4.00 / ca); }
 static double pk_z_K2_inf(double ca) { return 1.0 / (1.0 + 0.20 / ca); }
 
@@ -227,37 +247,37 @@ static double trap(double dt, double inf, double tau, double x) {
 /* ------------------------------------------------------------------ */
 /* IO rate functions (io_ion.cu:5-51)                                  */
 /* ------------------------------------------------------------------ */
-static double io_ar(double v) { return (1.7) / (1.0 + exp((-(v - 5.0)) / 13.9)); }
+static double io_ar(double v) { return (1.7) / (1.0 + EXP((-(v - 5.0)) / 13.9)); }
 static double io_as(double x) { return fmin(0.00002 * x, 0.01); }
-static double io_ax(double v) { return (0.13 * (v + 25.0)) / (1.0 - exp(-(v + 25.0) / 10.0)); }
-static double io_br(double v) { return (0.02 * (v + 8.5)) / (exp((v + 8.5) / 5.0) - 1.0); }
-static double io_bx(double v) { return 1.69 * exp(-0.0125 * (v + 35.0)); }
+static double io_ax(double v) { return (0.13 * (v + 25.0)) / (1.0 - EXP(-(v + 25.0) / 10.0)); }
+static double io_br(double v) { return (0.02 * (v + 8.5)) / (EXP((v + 8.5) / 5.0) - 1.0); }
+static double io_bx(double v) { return 1.69 * EXP(-0.0125 * (v + 35.0)); }
 static double io_h_inf(double v, int e) {
   double h = 1.0;
-  if (e == 1) h = 1.0 / (1.0 + exp((-v - 70.0) / (-5.8)));
-  if (e == 2) h = 1.0 / (1.0 + exp((-v - 60.0) / (-5.8)));
+  if (e == 1) h = 1.0 / (1.0 + EXP((-v - 70.0) / (-5.8)));
+  if (e == 2) h = 1.0 / (1.0 + EXP((-v - 60.0) / (-5.8)));
   return h;
 }
-static double io_k_inf(double v) { return 1.0 / (1.0 + exp((-v - 61.0) / 4.2)); }
-static double io_l_inf(double v) { return 1.0 / (1.0 + exp((v + 85.5) / (8.5))); }
-static double io_m_inf(double v) { return 1.0 / (1.0 + exp((-v - 30.0) / (5.5))); }
-static double io_n_inf(double v) { return 1.0 / (1.0 + exp((-v - 3.0) / (10.0))); }
-static double io_p_inf(double v) { return 1.0 / (1.0 + exp((-v - 51.0) / (-12.0))); }
-static double io_q_inf(double v) { return 1.0 / (1.0 + exp((v + 80.0) / 4.0)); }
+static double io_k_inf(double v) { return 1.0 / (1.0 + EXP((-v - 61.0) / 4.2)); }
+static double io_l_inf(double v) { return 1.0 / (1.0 + EXP((v + 85.5) / (8.5))); }
+static double io_m_inf(double v) { return 1.0 / (1.0 + EXP((-v - 30.0) / (5.5))); }
+static double io_n_inf(double v) { return 1.0 / (1.0 + EXP((-v - 3.0) / (10.0))); }
+static double io_p_inf(double v) { return 1.0 / (1.0 + EXP((-v - 51.0) / (-12.0))); }
+static double io_q_inf(double v) { return 1.0 / (1.0 + EXP((v + 80.0) / 4.0)); }
 static double io_r_inf(double v) { return io_ar(v) / (io_ar(v) + io_br(v)); }
 static double io_s_inf(double x) { return io_as(x) / (io_as(x) + 0.015); }
 static double io_x_inf(double v) { return io_ax(v) / (io_ax(v) + io_bx(v)); }
 static double io_h_tau(double v, int e) {
   double h = 1.0;
-  if (e == 1) h = 3.0 * exp((-v - 40.0) / 33.0);
-  if (e == 2) h = 1.5 * exp((-v - 40.0) / 33.0);
+  if (e == 1) h = 3.0 * EXP((-v - 40.0) / 33.0);
+  if (e == 2) h = 1.5 * EXP((-v - 40.0) / 33.0);
   return h;
 }
 static double io_l_tau(double v) {
-  return ((20.0 * exp((v + 160.0) / 30.0)) / (1.0 + exp((v + 84.0) / 7.3))) + 35.0;
+  return ((20.0 * EXP((v + 160.0) / 30.0)) / (1.0 + EXP((v + 84.0) / 7.3))) + 35.0;
 }
-static double io_n_tau(double v) { return 47.0 * exp((-(-v - 50.0)) / 900.0) + 5.0; }
-static double io_q_tau(double v) { return 1.0 / (exp(-0.086 * v - 14.6) + exp(0.07 * v - 1.87)); }
+static double io_n_tau(double v) { return 47.0 * EXP((-(-v - 50.0)) / 900.0) + 5.0; }
+static double io_q_tau(double v) { return 1.0 / (EXP(-0.086 * v - 14.6) + EXP(0.07 * v - 1.87)); }
 static double io_r_tau(double v) { return 5.0 / (io_ar(v) + io_br(v)); }
 static double io_s_tau(double x) { return 1.0 / (io_as(x) + 0.015); }
 static double io_x_tau(double v) { return 1.0 / (io_ax(v) + io_bx(v)); }
@@ -266,113 +286,113 @@ static double io_x_tau(double v) { return 1.0 / (io_ax(v) + io_bx(v)); }
 /* GR rate functions (gr_ion.cu:3-43)                                  */
 /* ------------------------------------------------------------------ */
 static double gr_a_nKV(double v) {
-  return (fabs(v + 25.0) > 1.0e-6) ? -0.017 * ((v + 25.0) / (exp(-(v + 25.0) / 10.0) - 1.0))
+  return (fabs(v + 25.0) > 1.0e-6) ? -0.017 * ((v + 25.0) / (EXP(-(v + 25.0) / 10.0) - 1.0))
                                    : -0.17 * (1.0 + (v + 25.0) / 20.0);
 }
-static double gr_b_nKV(double v) { return 0.2223 * exp(-(v + 35.0) / 80.0); }
+static double gr_b_nKV(double v) { return 0.2223 * EXP(-(v + 35.0) / 80.0); }
 AB_GATE(gr_nKV, gr_a_nKV, gr_b_nKV)
-static double gr_a_aKA(double v) { return 0.771 / (1.0 + exp(-(v + 9.17203) / 23.32708)); }
-static double gr_b_aKA(double v) { return 0.1567 / exp((v + 18.27914) / 19.47175); }
-static double gr_aKA_inf(double v) { return 1.0 / (1.0 + exp(-(v + 38.0) / 17.0)); }
+static double gr_a_aKA(double v) { return 0.771 / (1.0 + EXP(-(v + 9.17203) / 23.32708)); }
+static double gr_b_aKA(double v) { return 0.1567 / EXP((v + 18.27914) / 19.47175); }
+static double gr_aKA_inf(double v) { return 1.0 / (1.0 + EXP(-(v + 38.0) / 17.0)); }
 static double gr_aKA_tau(double v) { return (1.0 / (gr_a_aKA(v) + gr_b_aKA(v))); }
-static double gr_a_bKA(double v) { return 0.0348 / (1.0 + exp((v + 111.33208) / 12.8433)); }
-static double gr_b_bKA(double v) { return 0.0327 / (1.0 + exp(-(v + 49.9537) / 8.90123)); }
-static double gr_bKA_inf(double v) { return 1.0 / (1.0 + exp((v + 78.8) / 8.4)); }
+static double gr_a_bKA(double v) { return 0.0348 / (1.0 + EXP((v + 111.33208) / 12.8433)); }
+static double gr_b_bKA(double v) { return 0.0327 / (1.0 + EXP(-(v + 49.9537) / 8.90123)); }
+static double gr_bKA_inf(double v) { return 1.0 / (1.0 + EXP((v + 78.8) / 8.4)); }
 static double gr_bKA_tau(double v) { return (1.0 / (gr_a_bKA(v) + gr_b_bKA(v))); }
-static double gr_a_ir(double v) { return 0.2302 * exp(-(v + 83.94) / 24.3902); }
-static double gr_b_ir(double v) { return 0.2943 * exp((v + 83.94) / 35.714); }
+static double gr_a_ir(double v) { return 0.2302 * EXP(-(v + 83.94) / 24.3902); }
+static double gr_b_ir(double v) { return 0.2943 * EXP((v + 83.94) / 35.714); }
 AB_GATE(gr_ir, gr_a_ir, gr_b_ir)
-static double gr_a_sKM(double v) { return 0.0046 * exp((v + 30.0) / 40.0); }
-static double gr_b_sKM(double v) { return 0.0046 * exp(-(v + 30.0) / 20.0); }
-static double gr_sKM_inf(double v) { return 1.0 / (1.0 + exp(-(v + 35.0) / 6.0)); }
+static double gr_a_sKM(double v) { return 0.0046 * EXP((v + 30.0) / 40.0); }
+static double gr_b_sKM(double v) { return 0.0046 * EXP(-(v + 30.0) / 20.0); }
+static double gr_sKM_inf(double v) { return 1.0 / (1.0 + EXP(-(v + 35.0) / 6.0)); }
 static double gr_sKM_tau(double v) { return (1.0 / (gr_a_sKM(v) + gr_b_sKM(v))); }
-static double gr_a_cKCa(double v, double ca) { return 1.4433 / (1.0 + (1.5e-3 * exp(-v / 11.765)) / ca); }
-static double gr_b_cKCa(double v, double ca) { return 0.8660 / (1.0 + ca / (1.5e-4 * exp(-v / 11.765))); }
+static double gr_a_cKCa(double v, double ca) { return 1.4433 / (1.0 + (1.5e-3 * EXP(-v / 11.765)) / ca); }
+static double gr_b_cKCa(double v, double ca) { return 0.8660 / (1.0 + ca / (1.5e-4 * EXP(-v / 11.765))); }
 static double gr_cKCa_inf(double v, double ca) {
   return gr_a_cKCa(v, ca) / (gr_a_cKCa(v, ca) + gr_b_cKCa(v, ca));
 }
 static double gr_cKCa_tau(double v, double ca) { return (1.0 / (gr_a_cKCa(v, ca) + gr_b_cKCa(v, ca))); }
-static double gr_a_ch(double v) { return 0.0856 * exp((v + 29.6) / 15.873); }
-static double gr_b_ch(double v) { return 0.1437 * exp(-(v + 18.66) / 25.641); }
-static double gr_a_ci(double v) { return 0.0023 * exp(-(v + 48.0) / 18.183); }
-static double gr_b_ci(double v) { return 0.0025 * exp((v + 48.0) / 83.33); }
+static double gr_a_ch(double v) { return 0.0856 * EXP((v + 29.6) / 15.873); }
+static double gr_b_ch(double v) { return 0.1437 * EXP(-(v + 18.66) / 25.641); }
+static double gr_a_ci(double v) { return 0.0023 * EXP(-(v + 48.0) / 18.183); }
+static double gr_b_ci(double v) { return 0.0025 * EXP((v + 48.0) / 83.33); }
 static double gr_ch_inf(double v) { return (gr_a_ch(v) / (gr_a_ch(v) + gr_b_ch(v))); }
 static double gr_ci_inf(double v) { return (gr_a_ci(v) / (gr_a_ci(v) + gr_b_ci(v))); }
 
 /* ------------------------------------------------------------------ */
 /* GO rate functions (go_ion.cu:3-86)                                  */
 /* ------------------------------------------------------------------ */
-static double go_am_NaT(double v) { return 0.417 * (v + 25.0) / (1 - exp(-(v + 25.0) / 10.0)); }
-static double go_bm_NaT(double v) { return 16.68 * exp(-0.055 * (v + 50.0)); }
+static double go_am_NaT(double v) { return 0.417 * (v + 25.0) / (1 - EXP(-(v + 25.0) / 10.0)); }
+static double go_bm_NaT(double v) { return 16.68 * EXP(-0.055 * (v + 50.0)); }
 AB_GATE(go_m_NaT, go_am_NaT, go_bm_NaT)
-static double go_ah_NaT(double v) { return 0.292 * exp(-0.3 * (v + 50.0)); }
-static double go_bh_NaT(double v) { return 4.17 / (1 + exp(-(v + 17.0) / 5.0)); }
+static double go_ah_NaT(double v) { return 0.292 * EXP(-0.3 * (v + 50.0)); }
+static double go_bh_NaT(double v) { return 4.17 / (1 + EXP(-(v + 17.0) / 5.0)); }
 AB_GATE(go_h_NaT, go_ah_NaT, go_bh_NaT)
 static double go_ar_NaR(double v) {
-  return ((1.11 - 68.5 * (v - 4.48) / (exp(-(v - 4.48) / 6.8) - 1.0)) * 1.0e-4);
+  return ((1.11 - 68.5 * (v - 4.48) / (EXP(-(v - 4.48) / 6.8) - 1.0)) * 1.0e-4);
 }
 static double go_br_NaR(double v) {
   double x = (v + 44.0) / 0.11;
   if (x > 200.0) x = 200.0;
-  return ((66.0 + 21.7 * (v + 44) / (exp(x) - 1.0)) * 1.0e-3);
+  return ((66.0 + 21.7 * (v + 44) / (EXP(x) - 1.0)) * 1.0e-3);
 }
 AB_GATE(go_r_NaR, go_ar_NaR, go_br_NaR)
-static double go_as_NaR(double v) { return (0.443 * exp(-(v + 80.0) / 62.5)); }
-static double go_bs_NaR(double v) { return (0.014 * exp((v + 83.3) / 16.1)); }
+static double go_as_NaR(double v) { return (0.443 * EXP(-(v + 80.0) / 62.5)); }
+static double go_bs_NaR(double v) { return (0.014 * EXP((v + 83.3) / 16.1)); }
 AB_GATE(go_s_NaR, go_as_NaR, go_bs_NaR)
-static double go_ap_NaP(double v) { return (0.421 * (v + 40.0) / (1.0 - exp(-(v + 40.0) / 5.0))); }
-static double go_bp_NaP(double v) { return (-0.287 * (v + 40.0) / (1.0 - exp((v + 40.0) / 5.0))); }
-static double go_p_NaP_inf(double v) { return (1 / (1.0 + exp(-(v + 43.0) / 5.0))); }
+static double go_ap_NaP(double v) { return (0.421 * (v + 40.0) / (1.0 - EXP(-(v + 40.0) / 5.0))); }
+static double go_bp_NaP(double v) { return (-0.287 * (v + 40.0) / (1.0 - EXP((v + 40.0) / 5.0))); }
+static double go_p_NaP_inf(double v) { return (1 / (1.0 + EXP(-(v + 43.0) / 5.0))); }
 static double go_p_NaP_tau(double v) { return (5.0 / (go_ap_NaP(v) + go_bp_NaP(v))); }
-static double go_ach(double v) { return (0.0687 * exp(0.063 * (v + 29.0))); }
-static double go_bch(double v) { return (0.115 * exp(-0.039 * (v + 18.66))); }
+static double go_ach(double v) { return (0.0687 * EXP(0.063 * (v + 29.0))); }
+static double go_bch(double v) { return (0.115 * EXP(-0.039 * (v + 18.66))); }
 AB_GATE(go_ch, go_ach, go_bch)
-static double go_aci(double v) { return (1.8e-3 * exp(-(v + 48.0) / 18.0)); }
-static double go_bci(double v) { return (1.8e-3 * exp((v + 48.0) / 83.0)); }
+static double go_aci(double v) { return (1.8e-3 * EXP(-(v + 48.0) / 18.0)); }
+static double go_bci(double v) { return (1.8e-3 * EXP((v + 48.0) / 83.0)); }
 AB_GATE(go_ci, go_aci, go_bci)
-static double go_cl_inf(double v) { return (1.0 / (1.0 + exp(-(v + 52.0) / 7.4))); }
+static double go_cl_inf(double v) { return (1.0 / (1.0 + EXP(-(v + 52.0) / 7.4))); }
 static double go_cl_tau(double v) {
-  return ((3.0 + 1.0 / (exp((v + 27.0) / 10.0) + exp(-(v + 102.0) / 15.0))) / 0.85);
+  return ((3.0 + 1.0 / (EXP((v + 27.0) / 10.0) + EXP(-(v + 102.0) / 15.0))) / 0.85);
 }
-static double go_cm_inf(double v) { return (1.0 / (1.0 + exp((v + 80.0) / 5.0))); }
+static double go_cm_inf(double v) { return (1.0 / (1.0 + EXP((v + 80.0) / 5.0))); }
 static double go_cm_tau(double v) {
-  return ((85.0 + 1.0 / (exp((v + 48.0) / 4.0) + exp(-(v + 407.0) / 50.0))) / 0.9);
+  return ((85.0 + 1.0 / (EXP((v + 48.0) / 4.0) + EXP(-(v + 407.0) / 50.0))) / 0.9);
 }
-static double go_an_KV(double v) { return 0.062 * (v + 26.0) / (1.0 - exp(-(v + 26.0) / 10.0)); }
-static double go_bn_KV(double v) { return 0.78 * exp(-(v + 36.0) / 80.0); }
+static double go_an_KV(double v) { return 0.062 * (v + 26.0) / (1.0 - EXP(-(v + 26.0) / 10.0)); }
+static double go_bn_KV(double v) { return 0.78 * EXP(-(v + 36.0) / 80.0); }
 AB_GATE(go_n_KV, go_an_KV, go_bn_KV)
-static double go_aa_KA(double v) { return (0.62 / (1.0 + exp(-(v + 9.17) / 23.32))); }
-static double go_ba_KA(double v) { return (0.126 / (exp((v + 18.28) / 19.47))); }
-static double go_a_KA_inf(double v) { return (1.0 / (1.0 + exp(-(v + 38.0) / 17.0))); }
+static double go_aa_KA(double v) { return (0.62 / (1.0 + EXP(-(v + 9.17) / 23.32))); }
+static double go_ba_KA(double v) { return (0.126 / (EXP((v + 18.28) / 19.47))); }
+static double go_a_KA_inf(double v) { return (1.0 / (1.0 + EXP(-(v + 38.0) / 17.0))); }
 static double go_a_KA_tau(double v) { return (1.0 / (go_aa_KA(v) + go_ba_KA(v))); }
-static double go_ab_KA(double v) { return (0.028 / (1.0 + exp((v + 111.0) / 12.84))); }
-static double go_bb_KA(double v) { return (0.026 / (1.0 + exp(-(v + 49.95) / 8.9))); }
-static double go_b_KA_inf(double v) { return (1.0 / (1.0 + exp((v + 78.8) / 8.4))); }
+static double go_ab_KA(double v) { return (0.028 / (1.0 + EXP((v + 111.0) / 12.84))); }
+static double go_bb_KA(double v) { return (0.026 / (1.0 + EXP(-(v + 49.95) / 8.9))); }
+static double go_b_KA_inf(double v) { return (1.0 / (1.0 + EXP((v + 78.8) / 8.4))); }
 static double go_b_KA_tau(double v) { return (1.0 / (go_ab_KA(v) + go_bb_KA(v))); }
-static double go_ac_KC(double v, double ca) { return (3.2 / (1.0 + 0.0015 * exp(-(v) / 11.7) / ca)); }
-static double go_bc_KC(double v, double ca) { return (0.46 / (1.0 + ca / (1.5e-4 * exp(-(v) / 11.7)))); }
+static double go_ac_KC(double v, double ca) { return (3.2 / (1.0 + 0.0015 * EXP(-(v) / 11.7) / ca)); }
+static double go_bc_KC(double v, double ca) { return (0.46 / (1.0 + ca / (1.5e-4 * EXP(-(v) / 11.7)))); }
 static double go_c_KC_inf(double v, double ca) {
   return (go_ac_KC(v, ca) / (go_ac_KC(v, ca) + go_bc_KC(v, ca)));
 }
 static double go_c_KC_tau(double v, double ca) { return (1.0 / (go_ac_KC(v, ca) + go_bc_KC(v, ca))); }
-static double go_asl(double v) { return (0.0037 * exp((v + 30.0) / 40.0)); }
-static double go_bsl(double v) { return (0.0037 * exp(-(v + 30.0) / 20.0)); }
-static double go_sl_inf(double v) { return (1.0 / (1.0 + exp(-(v + 35.0) / 6.0))); }
+static double go_asl(double v) { return (0.0037 * EXP((v + 30.0) / 40.0)); }
+static double go_bsl(double v) { return (0.0037 * EXP(-(v + 30.0) / 20.0)); }
+static double go_sl_inf(double v) { return (1.0 / (1.0 + EXP(-(v + 35.0) / 6.0))); }
 static double go_sl_tau(double v) { return (1.0 / (go_asl(v) + go_bsl(v))); }
 static double go_r1(double v) { return (0.0021 * (v) + 0.97); }
-static double go_hf1_inf(double v) { return (go_r1(v) * (1.0 / (1.0 + exp((v + 72.5) * 0.11)))); }
-static double go_hs1_inf(double v) { return ((1.0 - go_r1(v)) * (1.0 / (1.0 + exp((v + 72.5) * 0.11)))); }
-static double go_hf1_tau(double v) { return (exp((0.0137 * v + 3.37) * 2.3)); }
-static double go_hs1_tau(double v) { return (exp((0.0145 * v + 4.06) * 2.3)); }
+static double go_hf1_inf(double v) { return (go_r1(v) * (1.0 / (1.0 + EXP((v + 72.5) * 0.11)))); }
+static double go_hs1_inf(double v) { return ((1.0 - go_r1(v)) * (1.0 / (1.0 + EXP((v + 72.5) * 0.11)))); }
+static double go_hf1_tau(double v) { return (EXP((0.0137 * v + 3.37) * 2.3)); }
+static double go_hs1_tau(double v) { return (EXP((0.0145 * v + 4.06) * 2.3)); }
 static double go_r2(double v) {
   if (v >= -64.70) return 0.0;
   else if (v <= -108.70) return 1.0;
   else return (-0.0227 * (v) - 1.47);
 }
-static double go_hf2_inf(double v) { return (go_r2(v) * (1.0 / (1.0 + exp((v + 81.9) * 0.16)))); }
-static double go_hs2_inf(double v) { return ((1.0 - go_r2(v)) * (1.0 / (1.0 + exp((v + 81.9) * 0.16)))); }
-static double go_hf2_tau(double v) { return (exp((0.027 * v + 5.6) * 2.3)); }
-static double go_hs2_tau(double v) { return (exp((0.015 * v + 5.3) * 2.3)); }
+static double go_hf2_inf(double v) { return (go_r2(v) * (1.0 / (1.0 + EXP((v + 81.9) * 0.16)))); }
+static double go_hs2_inf(double v) { return ((1.0 - go_r2(v)) * (1.0 / (1.0 + EXP((v + 81.9) * 0.16)))); }
+static double go_hf2_tau(double v) { return (EXP((0.027 * v + 5.6) * 2.3)); }
+static double go_hs2_tau(double v) { return (EXP((0.015 * v + 5.3) * 2.3)); }
 
 /* ------------------------------------------------------------------ */
 /* small dense solver: partial pivoting Gaussian elimination as in      */
@@ -482,8 +502,8 @@ static void gr_na_update(orc_sys *s, int id, double v_new, double v_old, double 
   if (t < 5) return; /* GR_hill = 5 */
   const double vs = GRNA_Vs[t];
   double M[144], vc[12], vcb[12];
-  double alpha = GRNA_Aa[t] * exp((v_old - vs) / 10.0);
-  double beta = GRNA_Ab[t] * exp(-(v_old - vs) / 10.0);
+  double alpha = GRNA_Aa[t] * EXP((v_old - vs) / 10.0);
+  double beta = GRNA_Ab[t] * EXP(-(v_old - vs) / 10.0);
   grna_matrix(M, t, alpha, beta, DT, -1.0);
   static const int slot[12] = {GR_c1, GR_c2, GR_c3, GR_c4, GR_c5, GR_i1,
                                GR_i2, GR_i3, GR_i4, GR_i5, GR_i6, GR_o_Na};
@@ -492,8 +512,8 @@ static void gr_na_update(orc_sys *s, int id, double v_new, double v_old, double 
     vcb[i] = 0.0;
     for (int j = 0; j < 12; j++) vcb[i] -= vc[j] * M[i * 12 + j];
   }
-  alpha = GRNA_Aa[t] * exp((v_new - vs) / 10.0);
-  beta = GRNA_Ab[t] * exp(-(v_new - vs) / 10.0);
+  alpha = GRNA_Aa[t] * EXP((v_new - vs) / 10.0);
+  beta = GRNA_Ab[t] * EXP(-(v_new - vs) / 10.0);
   grna_matrix(M, t, alpha, beta, DT, +1.0);
   if (!pivot_solve(12, M, vcb)) return;
   for (int k = 0; k < 12; k++) s->ion[slot[k]][id] = vcb[k];
@@ -553,8 +573,8 @@ static void pkj_ion_one(orc_sys *s, int id, double vnew, double DT) {
   k1 = Ca_val + (k1 + k2 * 2.0 + k3 * 2.0 + k4) / 6.0;
   s->ca[id] = k1;
   Ca_val = 0.5 * (Ca_val + k1);
-  if (s->rev_fixed[id]) s->rev_ca2[id] = 12.5 * log(Ca1OUT_PKJ / Ca1_0_PKJ);
-  else s->rev_ca2[id] = 13.361624877 * log(Ca1OUT_PKJ / Ca_val);
+  if (s->rev_fixed[id]) s->rev_ca2[id] = 12.5 * LOG(Ca1OUT_PKJ / Ca1_0_PKJ);
+  else s->rev_ca2[id] = 13.361624877 * LOG(Ca1OUT_PKJ / Ca_val);
   Ca_val = floor((Ca_val * 1000 - 0.04) / 0.099986667) * 0.099986667 + 0.04;
 #define G(k, name) x[k][id] = trap(DT, name##_inf(v_val), name##_tau(v_val), x[k][id])
   G(PK_m_NaF, pk_m_NaF); G(PK_h_NaF, pk_h_NaF); G(PK_m_NaP, pk_m_NaP);
@@ -633,7 +653,7 @@ static void go_ion_one(orc_sys *s, int id, double vnew, double DT) {
   k3 = DT * (-I2 / (2.0 * F_GO * SHELL1_D_GO) - B_Ca1_GO * (Ca2_val + k2 / 2.0 - Ca1_0_GO));
   k4 = DT * (-I2 / (2.0 * F_GO * SHELL1_D_GO) - B_Ca1_GO * (Ca2_val + k3 - Ca1_0_GO));
   s->ca2[id] += (k1 + k2 * 2.0 + k3 * 2.0 + k4) / 6.0;
-  s->rev_ca2[id] = (1e3) * (8.313424 * (23.0 + 273.15)) / (2 * F_GO) * log(Ca1OUT_GO / s->ca2[id]);
+  s->rev_ca2[id] = (1e3) * (8.313424 * (23.0 + 273.15)) / (2 * F_GO) * LOG(Ca1OUT_GO / s->ca2[id]);
   Ca_val = (Ca_val + s->ca[id]) / 2.0;
 #define G(k, name) x[k][id] = trap(DT, name##_inf(v_val), name##_tau(v_val), x[k][id])
   G(GO_m_NaT, go_m_NaT); G(GO_h_NaT, go_h_NaT); G(GO_r_NaR, go_r_NaR);
@@ -649,6 +669,7 @@ static void go_ion_one(orc_sys *s, int id, double vnew, double DT) {
 /* *_update_ion_and_matrix minus b (solve_rkc.cu:1100-1117,1169-1185,1230-1251,1299-1317) */
 void orc_ion_update(orc_sys *s, const double *vy, double DT) {
   int nc = s->nc;
+  g_canon = s->canon;
   switch (s->type) {
     case ORC_GR:
       /* gr_Na_update_2order runs first, with elem[v] still the old V */
@@ -671,6 +692,7 @@ void orc_ion_update(orc_sys *s, const double *vy, double DT) {
 /* *_update_matrix (solve_rkc.cu:227-250, 289-312, 370-398, 413-435) */
 void orc_update_b(orc_sys *s, const double *vy) {
   double **g = s->cond, **x = s->ion;
+  g_canon = s->canon;
   for (int id = 0; id < s->nc; id++) {
     double lv = vy[id], r;
     switch (s->type) {
@@ -736,7 +758,7 @@ static void io_gap_apply(orc_sys *s) {
   for (int e = 0; e < s->ngap; e++) {
     int pre = s->gap_pre[e], post = s->gap_post[e];
     double diff = (pre > -1) ? (s->v[post] - s->v[pre]) : 0.0;
-    s->gap_cur[e] = s->gap_g[e] * (0.8 * exp(-0.01 * diff * diff) + 0.2) * (diff);
+    s->gap_cur[e] = s->gap_g[e] * (0.8 * EXP(-0.01 * diff * diff) + 0.2) * (diff);
   }
   for (int e = 0; e < s->ngap; e++) s->b[s->gap_post[e]] += s->gap_cur[e];
 }
@@ -1113,6 +1135,9 @@ orc_sys *orc_create(const orc_desc *d) {
   }
   alloc_state(s);
   if (setup_cells(s, d) != 0) { orc_destroy(s); return NULL; }
+  /* the reference computes the initial gating on the host with libm
+   * (*_initialize_ion), so both modes use the platform exp here */
+  g_canon = 0;
   init_state(s, d->jitter);
   if (s->type == ORC_IO && d->io_gap && s->n > 1) io_gap_build(s, d);
   s->stim_comp = ialloc(s->n); s->stim_amp = zalloc(s->n);
@@ -1125,6 +1150,10 @@ orc_sys *orc_create(const orc_desc *d) {
   }
   static const double tol_def[4] = {1.0e-9, 1.0e-6, 1.0e-6, 1.0e-6};   /* solve_rkc.cuh:28-31 */
   const double hmin_def[4] = {pow(2.0, -12.0), pow(2.0, -10.0), pow(2.0, -10.0), pow(2.0, -10.0)};
+  s->canon = d->canon;
+  s->invcm = zalloc(s->nc);
+  s->scratch = zalloc(s->nc);
+  for (int i = 0; i < s->nc; i++) s->invcm[i] = 1.0 / s->cm[i];
   s->atol = s->rtol = (d->tol > 0) ? d->tol : tol_def[s->type];
   s->hmin = (d->hmin > 0) ? d->hmin : hmin_def[s->type];
   return s;
@@ -1141,6 +1170,7 @@ void orc_destroy(orc_sys *s) {
   free(s->ede); free(s->vnew); free(s->dammy);
   free(s->stim_comp); free(s->stim_amp); free(s->stim_t0); free(s->stim_t1);
   free(s->gap_pre); free(s->gap_post); free(s->gap_cur); free(s->gap_g);
+  free(s->invcm); free(s->scratch);
   free(s);
 }
 
@@ -1149,6 +1179,19 @@ void orc_destroy(orc_sys *s) {
 /* ------------------------------------------------------------------ */
 /* dydt (solve_rkc.cu:178-196) */
 static void dydt(orc_sys *s, const double *y, double *dy) {
+  if (s->canon) {
+    /* diagonal entries contribute val * (y_i - y_i) = 0 and are skipped */
+    for (int i = 0; i < s->nc; i++) {
+      double d = (-(s->b[i]));
+      const double yi = y[i];
+      for (int j = s->row[i]; j < s->row[i + 1]; j++) {
+        if (s->col[j] == i) continue;
+        d = fma(s->val[j], y[s->col[j]] - yi, d);
+      }
+      dy[i] = d * s->invcm[i];
+    }
+    return;
+  }
   for (int i = 0; i < s->nc; i++) {
     double d = (-(s->b[i]));
     const double yi = y[i];
@@ -1161,6 +1204,13 @@ static double dot(const double *a, const double *b, int n) {
   double r = 0.0;
   for (int i = 0; i < n; i++) r += a[i] * b[i];
   return r;
+}
+
+/* sum of squares: sequential (reference mode) or the canonical tree */
+static double sumsq(orc_sys *s, const double *a, int n) {
+  if (!s->canon) return dot(a, a, n);
+  for (int i = 0; i < n; i++) s->scratch[i] = a[i] * a[i];
+  return tree_sum(s->scratch, n);
 }
 
 static double fmax_ori(double a, double b) { return (a > b) ? a : b; }
@@ -1178,17 +1228,19 @@ static void rkcrho(orc_sys *s) {
   const double uround = UROUND, sqrtu = sqrt(UROUND), small = 1.0 / 0.125;
   double *yn = VEC(s, LYN), *fn = VEC(s, LFN), *v1 = VEC(s, LV1), *v2 = VEC(s, LV2);
   double *ede = s->ede, *dam = s->dammy;
-  double ynrm = sqrt(dot(yn, yn, nc));
-  double vnrm = sqrt(dot(ede, ede, nc));
+  double ynrm = sqrt(sumsq(s, yn, nc));
+  double vnrm = sqrt(sumsq(s, ede, nc));
   double dynrm, sigma, sigmal, dfnrm;
   s->n_rho++;
   if (ynrm != 0.0 && vnrm != 0.0) {
     dynrm = ynrm * sqrtu;
     double al = dynrm / vnrm;
-    for (int i = 0; i < nc; i++) v1[i] = al * ede[i] + yn[i];
+    if (s->canon) for (int i = 0; i < nc; i++) v1[i] = fma(al, ede[i], yn[i]);
+    else for (int i = 0; i < nc; i++) v1[i] = al * ede[i] + yn[i];
   } else if (ynrm != 0.0) {
     dynrm = ynrm * sqrtu;
-    for (int i = 0; i < nc; i++) v1[i] = sqrtu * yn[i] + yn[i];
+    if (s->canon) for (int i = 0; i < nc; i++) v1[i] = fma(sqrtu, yn[i], yn[i]);
+    else for (int i = 0; i < nc; i++) v1[i] = sqrtu * yn[i] + yn[i];
   } else if (vnrm != 0.0) {
     dynrm = uround;
     double al = dynrm / vnrm;
@@ -1199,9 +1251,10 @@ static void rkcrho(orc_sys *s) {
   }
   sigma = 0.0;
   for (int iter = 0; iter < itmax; iter++) {
+    s->n_rho_iter++;
     dydt(s, v1, v2);
     for (int i = 0; i < nc; i++) dam[i] = -1.0 * fn[i] + v2[i];
-    dfnrm = sqrt(dot(dam, dam, nc));
+    dfnrm = sqrt(sumsq(s, dam, nc));
     sigmal = sigma;
     sigma = dfnrm / dynrm;
     sprad_old[0] = sprad_old[1];
@@ -1221,8 +1274,12 @@ static void rkcrho(orc_sys *s) {
     }
     if (dfnrm != 0.0) {
       double al = dynrm / dfnrm;
-      for (int i = 0; i < nc; i++) v1[i] = -1.0 * v2[i] + fn[i];
-      for (int i = 0; i < nc; i++) v1[i] = al * v1[i] + yn[i];
+      if (s->canon) {
+        for (int i = 0; i < nc; i++) v1[i] = fma(al, fn[i] - v2[i], yn[i]);
+      } else {
+        for (int i = 0; i < nc; i++) v1[i] = -1.0 * v2[i] + fn[i];
+        for (int i = 0; i < nc; i++) v1[i] = al * v1[i] + yn[i];
+      }
     } else {
       int idx = iter % nc;
       v1[idx] = 2.0 * yn[idx] - v1[idx];
@@ -1234,6 +1291,7 @@ static void rkcrho(orc_sys *s) {
 /* set_initial_vec + rkcrho + set_initial_absh (solve_rkc.cu:438-560, 757-791) */
 int orc_init(orc_sys *s) {
   int nc = s->nc;
+  g_canon = s->canon;
   orc_update_b(s, s->v);
   for (int i = 0; i < nc; i++) {
     s->vnew[i] = s->v[i]; VEC(s, LY)[i] = s->v[i]; VEC(s, LYN)[i] = s->v[i];
@@ -1257,15 +1315,16 @@ int orc_init(orc_sys *s) {
   double absh = H_MAX;
   if (s->sprad * absh > 1.0) absh = 1.0 / s->sprad;
   absh = fmax_ori(absh, s->hw[6]);
-  for (int i = 0; i < nc; i++) v1[i] = yn[i] + absh * fn[i];
+  if (s->canon) for (int i = 0; i < nc; i++) v1[i] = fma(absh, fn[i], yn[i]);
+  else for (int i = 0; i < nc; i++) v1[i] = yn[i] + absh * fn[i];
   dydt(s, v1, v2);
   for (int i = 0; i < nc; i++) {
-    double wt = s->atol + s->rtol * fabs(yn[i]);
+    double wt = s->canon ? fma(s->rtol, fabs(yn[i]), s->atol) : s->atol + s->rtol * fabs(yn[i]);
     if (wt == 0.0) { s->idid = 3.0; return 3; }
     s->dammy[i] = 1.0 / wt;
   }
   for (int i = 0; i < nc; i++) s->dammy[i] = (v2[i] - fn[i]) * s->dammy[i];
-  double est = dot(s->dammy, s->dammy, nc);
+  double est = sumsq(s, s->dammy, nc);
   est = absh * sqrt(est / nc);
   if (0.1 * absh < H_MAX * sqrt(est)) absh = fmax_ori(0.1 * absh / sqrt(est), s->hw[6]);
   else absh = H_MAX;
@@ -1297,7 +1356,8 @@ static void step(orc_sys *s, double h, int m) {
     double *yn = VEC(s, LYN), *fn = VEC(s, LFN), *v1 = VEC(s, LV1), *v2 = VEC(s, LV2);
     memcpy(v2, yn, sizeof(double) * nc);
     double hm = h * mus;
-    for (int i = 0; i < nc; i++) v1[i] = hm * fn[i] + yn[i];
+    if (s->canon) for (int i = 0; i < nc; i++) v1[i] = fma(hm, fn[i], yn[i]);
+    else for (int i = 0; i < nc; i++) v1[i] = hm * fn[i] + yn[i];
   }
   zjm1 = w0; zjm2 = 1.0; dzjm1 = 1.0; dzjm2 = 0.0; d2zjm1 = 0.0; d2zjm2 = 0.0;
   for (int j = 1; j < m; j++) {
@@ -1312,8 +1372,18 @@ static void step(orc_sys *s, double h, int m) {
     double *y = VEC(s, LY), *yn = VEC(s, LYN), *fn = VEC(s, LFN), *v1 = VEC(s, LV1), *v2 = VEC(s, LV2);
     dydt(s, v1, y);
     double omn = (1.0 - mu - nu), hm = h * mus;
-    for (int i = 0; i < nc; i++)
-      y[i] = mu * v1[i] + nu * v2[i] + omn * yn[i] + hm * (y[i] - ajm1 * fn[i]);
+    if (s->canon) {
+      for (int i = 0; i < nc; i++) {
+        double t = mu * v1[i];
+        t = fma(nu, v2[i], t);
+        t = fma(omn, yn[i], t);
+        double u = fma(-ajm1, fn[i], y[i]);
+        y[i] = fma(hm, u, t);
+      }
+    } else {
+      for (int i = 0; i < nc; i++)
+        y[i] = mu * v1[i] + nu * v2[i] + omn * yn[i] + hm * (y[i] - ajm1 * fn[i]);
+    }
     /* rotate v2 <- v1 <- y <- v2 (solve_rkc.cu:879-883) */
     int t = s->map[LV2];
     s->map[LV2] = s->map[LV1]; s->map[LV1] = s->map[LY]; s->map[LY] = t;
@@ -1349,15 +1419,25 @@ static void rkclow(orc_sys *s) {
     double *y = VEC(s, LY), *yn = VEC(s, LYN), *fn = VEC(s, LFN), *v1 = VEC(s, LV1);
     dydt(s, y, v1);
     err = 0.0;
-    for (int i = 0; i < nc; i++) {
-      double wt = s->atol + s->rtol * fmax_ori(fabs(y[i]), fabs(yn[i]));
-      double est = 0.8 * (yn[i] - y[i]) + 0.4 * h * (fn[i] + v1[i]);
-      err += (est / wt) * (est / wt);
+    if (s->canon) {
+      for (int i = 0; i < nc; i++) {
+        double wt = fma(s->rtol, fmax_ori(fabs(y[i]), fabs(yn[i])), s->atol);
+        double est = fma(0.4 * h, fn[i] + v1[i], 0.8 * (yn[i] - y[i]));
+        double q = est / wt;
+        s->scratch[i] = q * q;
+      }
+      err = tree_sum(s->scratch, nc);
+    } else {
+      for (int i = 0; i < nc; i++) {
+        double wt = s->atol + s->rtol * fmax_ori(fabs(y[i]), fabs(yn[i]));
+        double est = 0.8 * (yn[i] - y[i]) + 0.4 * h * (fn[i] + v1[i]);
+        err += (est / wt) * (est / wt);
+      }
     }
     if (s->idid == 3.0) return;
     err = sqrt(err / (double)nc);
     if (err > 1.0) {
-      s->absh = 0.8 * s->absh / (pow(err, 1.0 / 3.0));
+      s->absh = 0.8 * s->absh / (POW(err, 1.0 / 3.0));
       s->n_rej++;
       if (s->absh < hmin) {
         s->idid = 4;
@@ -1384,11 +1464,11 @@ static void rkclow(orc_sys *s) {
     }
     fac = 10.0;
     if (s->naccpt == 1) {
-      temp2 = pow(err, 1.0 / 3.0);
+      temp2 = POW(err, 1.0 / 3.0);
       if (0.8 < fac * temp2) fac = 0.8 / temp2;
     } else {
-      temp1 = 0.8 * s->absh * pow(s->errold, 1.0 / 3.0);
-      temp2 = fabs(s->hold) * pow(err, 2.0 / 3.0);
+      temp1 = 0.8 * s->absh * POW(s->errold, 1.0 / 3.0);
+      temp2 = fabs(s->hold) * POW(err, 2.0 / 3.0);
       if (temp1 < fac * temp2) fac = temp1 / temp2;
     }
     s->absh = fmax_ori(0.1, fac) * s->absh;
@@ -1410,7 +1490,11 @@ static void rkcint(orc_sys *s) {
   double b1 = hlast * sv * (sv - 1.0) * (sv - 1.0);
   double b2 = hlast * (sv - 1.0) * sv * sv;
   double *v1 = VEC(s, LV1), *v2 = VEC(s, LV2), *yn = VEC(s, LYN), *fn = VEC(s, LFN);
-  for (int i = 0; i < s->nc; i++) s->vnew[i] = a1 * v1[i] + a2 * yn[i] + b1 * v2[i] + b2 * fn[i];
+  if (s->canon)
+    for (int i = 0; i < s->nc; i++)
+      s->vnew[i] = fma(b2, fn[i], fma(b1, v2[i], fma(a2, yn[i], a1 * v1[i])));
+  else
+    for (int i = 0; i < s->nc; i++) s->vnew[i] = a1 * v1[i] + a2 * yn[i] + b1 * v2[i] + b2 * fn[i];
 }
 
 /* per-cell step current, evaluated at the start of each interval
@@ -1427,6 +1511,7 @@ static void set_current(orc_sys *s, double t) {
 
 /* *_solve_by_rkc (solve_rkc.cu:1122-1362) for one 0.125 ms interval */
 int orc_advance(orc_sys *s, double t) {
+  g_canon = s->canon;
   set_current(s, t);
   /* GR and IO compare with '>', GO and PKJ with '>=' (solve_rkc.cu:1148,1212,1284,1347) */
   const int ge = (s->type == ORC_GO || s->type == ORC_PKJ);
@@ -1479,6 +1564,7 @@ void orc_ctl(const orc_sys *s, double *o) {
 
 void orc_stats(const orc_sys *s, long long *o) {
   o[0] = s->n_steps; o[1] = s->n_rej; o[2] = s->n_stage; o[3] = s->n_rho; o[4] = s->n_ion;
+  o[5] = s->n_rho_iter;
 }
 
 void orc_draw_jitter(int type, int n, double *out) {

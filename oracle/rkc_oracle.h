@@ -50,6 +50,8 @@ typedef struct {
   double hmin;         /* <= 0: reference per-type default */
   int io_gap;          /* IO: 1 = build the nonlinear gap network (reference: n > 1) */
   int go_gj, pkj_gj;   /* 1 = add the linear GJ entries to the CSR (reference: n > 1) */
+  int canon;           /* 1 = canonical arithmetic (canon_math.h), bit-comparable with
+                          the GPU plain-FP64 path; 0 = the reference's literal expressions */
 } orc_desc;
 
 orc_sys *orc_create(const orc_desc *d);
@@ -71,8 +73,9 @@ const double *orc_ion(const orc_sys *s, int k);
 const double *orc_ca(const orc_sys *s);
 /* controller scalars: absh sprad naccpt errold hold lt tend sum_dt */
 void orc_ctl(const orc_sys *s, double *out8);
-/* counters: steps, rejects, stage evals (sum of m), rho evals, ion updates */
-void orc_stats(const orc_sys *s, long long *out5);
+/* counters: steps, rejects, stage evals (sum of m), rho calls, ion updates,
+ * power-iteration RHS evaluations */
+void orc_stats(const orc_sys *s, long long *out6);
 
 /* static setup, for the setup pins: Cm, area, cond k, shell, CSR */
 const double *orc_cm(const orc_sys *s);
