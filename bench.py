@@ -1,0 +1,392 @@
+"""Benchmark: compartment-updates/s of the RKC hot path on one GB300.
+
+Default workload (BASELINE config "mixed-type batch"): 4096 reduced granule
+cells, 1024 Golgi cells, 256 Purkinje cells and one 16x16 inferior-olive
+gap-junction network, FP32 gating with FP64 voltage, advanced together.
+A step advances every system by --step-ms of simulated time (default 5 ms =
+40 output intervals) in one device-resident launch per cell type.
+
+Unit: one compartment-update = one RKC right-hand-side (stage) evaluation of
+one compartment: sum over step attempts of (m + 1) x compartments, accepted
+and rejected steps counted, power iterations excluded.
+
+  python bench.py [--gpus N --steps K --warmup W] [--precision fp64|mixed]
+                  [--config mixed|pkj3x3] [--impl reference]
+
+Multi-GPU: independent replicas of the workload (each rank its own), no
+collective on the data path; value = units of all ranks / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cerebellum-neuron-model-simulation-using-rkc_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+for p in (PKG, ORACLE):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+H_MAX = 0.125
+ALG_BYTES = {"mixed": 56, "fp64": 68}   # algorithmic bytes per compartment-update
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ workloads
+def workload(name):
+    import configs
+    if name == "mixed":
+        return configs.mixed_batch(), "mixed-type batch: 4096 GrC x4 + 1024 GoC x131 + 256 PC x1600 + IO 16x16 net x3"
+    if name == "pkj3x3":
+        return configs.pkj_grid(3, 3), "Purkinje 3x3 grid, one RKC system, x-neighbour gap junctions, 0.5 nA"
+    raise SystemExit(f"unknown config {name}")
+
+
+# ------------------------------------------------------------ CPU side
+def _oracle_worker(args):
+    """Run a slice of a sampled workload in the oracle (reference arithmetic)."""
+    cfg, fraction, idx, t_begin, n_iv, warm_iv = args
+    sys.path.insert(0, PKG)
+    sys.path.insert(0, ORACLE)
+    import configs
+    import oracle_py as O
+    specs = configs.scaled_mixed_batch(fraction) if cfg == "mixed" else configs.pkj_grid(3, 3)
+    systems = [(specs[i], configs.add_to_oracle(O, specs[i], canon=False)) for i in idx]
+    t = 0.0
+    for _ in range(warm_iv):
+        for sp, s in systems:
+            s.advance(t)
+        t += H_MAX
+    before = sum((s.stats()["stages"] + s.stats()["steps"]) * sp.nc for sp, s in systems)
+    t0 = time.perf_counter()
+    for _ in range(n_iv):
+        for sp, s in systems:
+            if s.advance(t) != 0:
+                raise RuntimeError("oracle step failed")
+        t += H_MAX
+    dt = time.perf_counter() - t0
+    after = sum((s.stats()["stages"] + s.stats()["steps"]) * sp.nc for sp, s in systems)
+    return after - before, dt
+
+
+def cpu_sample(cfg, fraction, n_iv, warm_iv, workers):
+    """Time the oracle on a bounded, proportional sample of the workload."""
+    import configs
+    specs = configs.scaled_mixed_batch(fraction) if cfg == "mixed" else configs.pkj_grid(3, 3)
+    order = sorted(range(len(specs)), key=lambda i: -specs[i].nc)
+    slices = [order[k::workers] for k in range(workers)]
+    jobs = [(cfg, fraction, sl, 0.0, n_iv, warm_iv) for sl in slices if sl]
+    if workers == 1:
+        res = [_oracle_worker(j) for j in jobs]
+    else:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(len(jobs)) as pool:
+            res = pool.map(_oracle_worker, jobs)
+    units = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    counts = configs.type_counts(specs)
+    desc = ", ".join(f"{v[0]} {k}" for k, v in counts.items())
+    return units, wall, f"{desc}; {n_iv} intervals ({n_iv * H_MAX:g} ms) after {warm_iv} warm-up intervals"
+
+
+def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's RKC path (the
+    reference's own CUDA code cannot travel: its sources are not part of this
+    repository), on all host cores, over a bounded sample of the workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    cfg = args.config
+    fraction = 1.0 / 16 if cfg == "mixed" else 1.0
+    n_iv = 8 if cfg == "mixed" else 4
+    vals = []
+    for k in range(args.warmup + args.steps):
+        units, wall, sample = cpu_sample(cfg, fraction, n_iv, 0, cores)
+        if k >= args.warmup:
+            vals.append((units, wall))
+    units = sum(u for u, _ in vals)
+    wall = sum(w for _, w in vals)
+    v = units / wall
+    _, wl = workload(cfg)
+    out = {"impl": "reference", "metric": "compartment-updates/s", "value": v, "unit": "compartment-updates/s",
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * wall / max(1, len(vals)), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded morphologies and stimuli)",
+           "config": {"workload": wl, "precision": "fp64 (reference arithmetic)"},
+           "cpu_baseline": {"value": v, "unit": "compartment-updates/s", "cores": cores, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": "compartment-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ------------------------------------------------------------ GPU side
+def dist_init(n):
+    if n <= 1 and "RANK" not in os.environ:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, dist
+
+
+def barrier_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier_sum(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gbrkc", choices=["gbrkc", "reference"])
+    ap.add_argument("--config", default="mixed", choices=["mixed", "pkj3x3"])
+    ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
+    ap.add_argument("--step-ms", type=float, default=5.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    precision = args.precision or ("mixed" if args.config == "mixed" else "fp64")
+    rank, world, dist = dist_init(args.gpus)
+    import torch
+    import gbrkc as G
+    import configs
+    specs, wl = workload(args.config)
+    eng = G.Engine(G.MIXED if precision == "mixed" else G.FP64)
+    configs.add_to(eng, specs)
+    t_setup = time.perf_counter()
+    eng.build()
+    setup_s = time.perf_counter() - t_setup
+    n_iv = int(round(args.step_ms / H_MAX))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+    t = 0.0
+    for _ in range(args.warmup):
+        eng.advance(t, n_iv, tolerate_retire=True)
+        t += n_iv * H_MAX
+    torch.cuda.synchronize()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    dev_ms, kern_ms = 0.0, {k: 0.0 for k in range(4)}
+    units0 = eng.compartment_updates(-1)
+    units_t0 = {k: eng.compartment_updates(k) for k in range(4)}
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        eng.advance(t, n_iv, tolerate_retire=True)
+        t += n_iv * H_MAX
+        dev_ms += eng.last_advance_ms()
+        for k in range(4):
+            kern_ms[k] += eng.last_kernel_ms(k)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    units = eng.compartment_updates(-1) - units0
+    units_t = {k: eng.compartment_updates(k) - units_t0[k] for k in range(4)}
+    t_max_ms = barrier_max(dist, dev_ms)
+    units_all = barrier_sum(dist, units)
+    value = units_all / (t_max_ms * 1e-3)
+    launches = args.steps * sum(1 for k in range(4) if eng.type_cells(k) > 0)
+
+    # roofline of the dominant kernel
+    dom = max(range(4), key=lambda k: kern_ms[k])
+    names = {0: "gr", 1: "go", 2: "pkj", 3: "io"}
+    peak, peak_kind = peaks()
+    bpu = ALG_BYTES[precision]
+    per_launch_bytes = bpu * units_t[dom] / args.steps
+    per_launch_ms = kern_ms[dom] / args.steps
+    achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", f"traffic_{args.config}_{precision}.json")
+    if os.path.exists(tfile):
+        try:
+            tr = json.load(open(tfile))
+            traffic = tr.get(names[dom])
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "kernel": f"k_advance<{names[dom]}>",
+                "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_update": bpu,
+                "kernel_ms_per_step": {names[k]: kern_ms[k] / args.steps for k in range(4)}}
+
+    # end to end through the C ABI with host buffers: per step, upload every
+    # cell's stimulus table (pinned host -> device) and read back every cell's
+    # soma voltage at every interval (device -> pinned host)
+    e2e = None
+    if not args.no_e2e:
+        ncell = {k: eng.type_cells(k) for k in range(4)}
+        eng.record_soma(n_iv)
+        bufs = {}
+        rng = np.random.default_rng(7)
+        cell_specs = {k: [] for k in range(4)}
+        for s in specs:
+            cell_specs[s.cell_type].append(s)
+        for k in range(4):
+            if ncell[k] == 0:
+                continue
+            comp = torch.empty(ncell[k], dtype=torch.int32, pin_memory=True)
+            amp, t0v, t1v = (torch.empty(ncell[k], dtype=torch.float64, pin_memory=True) for _ in range(3))
+            cs = []
+            for s in cell_specs[k]:
+                c = np.broadcast_to(np.asarray(s.stim[0]), s.n)
+                cs.append(c)
+            comp.numpy()[:] = np.concatenate(cs)
+            soma = torch.empty((n_iv, ncell[k]), dtype=torch.float64, pin_memory=True)
+            bufs[k] = (comp, amp, t0v, t1v, soma)
+        h2d = sum(b[0].numel() * 4 + 3 * b[1].numel() * 8 for b in bufs.values())
+        d2h = sum(b[4].numel() * 8 for b in bufs.values())
+        e_units0 = eng.compartment_updates(-1)
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            for k, (comp, amp, t0v, t1v, soma) in bufs.items():
+                amp.numpy()[:] = rng.uniform(0, configs.AMP_MAX[k], ncell[k])
+                t0v.numpy()[:] = t
+                t1v.numpy()[:] = 1e9
+                eng.set_stim_type(k, comp.numpy(), amp.numpy(), t0v.numpy(), t1v.numpy())
+            eng.rewind_soma()
+            eng.advance(t, n_iv, tolerate_retire=True)
+            t += n_iv * H_MAX
+            for k, (comp, amp, t0v, t1v, soma) in bufs.items():
+                eng.read_soma_type(k, n_iv, soma.numpy())
+        torch.cuda.synchronize()
+        e_wall = time.perf_counter() - w0
+        e_units = eng.compartment_updates(-1) - e_units0
+        e_wall = barrier_max(dist, e_wall)
+        e_units = barrier_sum(dist, e_units)
+        e2e = {"value": e_units / e_wall, "unit": "compartment-updates/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "timing": "host wall clock incl. pinned copies"}
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        # bounded single-thread sample of the same workload in the oracle
+        frac = 1.0 / 256 if args.config == "mixed" else 1.0
+        probe_units, probe_wall, _ = cpu_sample(args.config, frac, 2, 0, 1)
+        per_iv = max(probe_wall / 2, 1e-3)
+        n_cpu = int(max(4, min(4000, args.cpu_seconds / per_iv)))
+        units_c, wall_c, sample = cpu_sample(args.config, frac, n_cpu, 0, 1)
+        cpu = {"value": units_c / wall_c, "unit": "compartment-updates/s", "cores": 1, "kind": "port",
+               "sample": sample + " (oracle, reference arithmetic, FP64, one thread)"}
+
+    if rank == 0:
+        counts = configs.type_counts(specs)
+        out = {"metric": "compartment-updates/s", "value": value, "unit": "compartment-updates/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": t_max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64 state+stages, f32 gating" if precision == "mixed" else "f64",
+               "data": "synthetic (seeded morphologies, jitter and step currents)",
+               "config": {"workload": wl, "precision": precision, "step_sim_ms": args.step_ms,
+                          "cells": {k: v[0] for k, v in counts.items()},
+                          "compartments": eng.total_compartments(),
+                          "l2": "flushed (256 MB write) between timed steps",
+                          "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                          "setup_s": round(setup_s, 2), "wall_s": round(wall, 3),
+                          "retired_systems": eng.retired(),
+                          "sim_ms_per_wall_s": args.steps * args.step_ms / (t_max_ms * 1e-3)},
+               "roofline": roofline, "gpu_launches": launches, "clocks": clk}
+        if e2e:
+            out["e2e"] = e2e
+        if cpu:
+            out["cpu_baseline"] = cpu
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -388,6 +388,7 @@ struct PoolHost {
   Ctl *d_ctl = nullptr;
   double *d_soma = nullptr;
   int soma_cap = 0;
+  std::vector<char> retired;
 };
 
 }  // namespace gbrkc
@@ -411,9 +412,18 @@ struct gbrkc_engine {
   int coef_mmax = 0;
   int soma_cap = 0;
   int soma_iv = 0;   // intervals recorded so far
+  int n_retired = 0;
+  cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_k0[NTYPES] = {}, ev_k1[NTYPES] = {};
+  float last_ms = 0.0f, last_kernel_ms[NTYPES] = {};
   ~gbrkc_engine() {
     for (auto &s : streams)
       if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t e : {ev_start, ev_end})
+      if (e) cudaEventDestroy(e);
+    for (int t = 0; t < NTYPES; t++) {
+      if (ev_k0[t]) cudaEventDestroy(ev_k0[t]);
+      if (ev_k1[t]) cudaEventDestroy(ev_k1[t]);
+    }
   }
 };
 
@@ -427,6 +437,12 @@ extern "C" int gbrkc_engine_create(int precision, gbrkc_engine **out) {
   std::unique_ptr<gbrkc_engine> E(new gbrkc_engine());
   E->precision = precision;
   for (auto &s : E->streams) CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreate(&E->ev_start));
+  CUDA_TRY(cudaEventCreate(&E->ev_end));
+  for (int t = 0; t < NTYPES; t++) {
+    CUDA_TRY(cudaEventCreate(&E->ev_k0[t]));
+    CUDA_TRY(cudaEventCreate(&E->ev_k1[t]));
+  }
   *out = E.release();
   return 0;
 }
@@ -480,6 +496,28 @@ extern "C" int gbrkc_add_system(gbrkc_engine *E, const gbrkc_system_desc *d, int
       E->csrs.push_back(std::move(C));
       S.csr = (int)E->csrs.size() - 1;
     }
+  }
+  if (S.n > 1 && S.csr < 0) {
+    // multi-cell system without linear junctions: replicate the template into
+    // a system CSR so the stage loop needs no cell arithmetic
+    const Template &T = E->templates[S.tmpl];
+    SysCsr C;
+    const int nz = (int)T.val.size();
+    C.row.assign(S.nc + 1, 0);
+    C.col.resize((size_t)nz * S.n);
+    C.val.resize((size_t)nz * S.n);
+    for (int ci = 0; ci < S.n; ci++) {
+      for (int j = 0; j < nz; j++) {
+        C.col[j + (size_t)nz * ci] = T.col[j] + S.ncomp * ci;
+        C.val[j + (size_t)nz * ci] = T.val[j];
+      }
+      for (int j = 0; j < S.ncomp; j++) C.row[j + S.ncomp * ci] = T.row[j] + nz * ci;
+    }
+    C.row[S.nc] = nz * S.n;
+    C.invcm.resize(S.nc);
+    for (int i = 0; i < S.nc; i++) C.invcm[i] = T.invcm[i % S.ncomp];
+    E->csrs.push_back(std::move(C));
+    S.csr = (int)E->csrs.size() - 1;
   }
   E->systems.push_back(std::move(S));
   if (sys_id) *sys_id = (int)E->systems.size() - 1;
@@ -601,7 +639,10 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
   P.ws_total = ws;
   // launch configuration: team shape by system size, workspace in shared
   // memory when it fits
-  if (P.max_nc <= 8) { P.team = TEAM_TILE4; P.block = 128; }
+  // tiny cells: one lane per compartment, 16 cells per 64-thread block (more
+  // warps per SM to hide the serial controller's latency)
+  if (P.max_nc <= 4) { P.team = TEAM_TILE4; P.block = 64; }
+  else if (P.max_nc <= 8) { P.team = TEAM_TILE4; P.block = 128; }
   else if (P.max_nc <= 320) { P.team = TEAM_WARP; P.block = 128; }
   else { P.team = TEAM_BLOCK; P.block = 256; }
   const int teams = (P.team == TEAM_BLOCK) ? 1 : P.block / P.team;
@@ -686,18 +727,33 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
   return prepare_pool_kernel<R>(P.type, P.team, P.smem) ? fail(GBRKC_ECUDA, "cudaFuncSetAttribute failed") : 0;
 }
 
+// Launch every pool's kernel on its own stream (the pools run concurrently)
+// and time the whole advance and each kernel with CUDA events recorded on the
+// launching streams.
 int launch_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
+  CUDA_TRY(cudaEventRecord(E->ev_start, E->streams[0]));
+  for (int t = 1; t < NTYPES; t++) CUDA_TRY(cudaStreamWaitEvent(E->streams[t], E->ev_start, 0));
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
     if (P.systems.empty()) continue;
     int rc;
+    CUDA_TRY(cudaEventRecord(E->ev_k0[t], E->streams[t]));
     if (E->precision == GBRKC_FP64)
       rc = launch_pool<double>(t, P.vd, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
     else
       rc = launch_pool<float>(t, P.vf, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
     if (rc) return fail(GBRKC_ECUDA, "launch (type %d): %s", t, cudaGetErrorString((cudaError_t)rc));
+    CUDA_TRY(cudaEventRecord(E->ev_k1[t], E->streams[t]));
+    if (t != 0) CUDA_TRY(cudaStreamWaitEvent(E->streams[0], E->ev_k1[t], 0));
   }
+  CUDA_TRY(cudaEventRecord(E->ev_end, E->streams[0]));
+  CUDA_TRY(cudaEventSynchronize(E->ev_end));
   for (int t = 0; t < NTYPES; t++) CUDA_TRY(cudaStreamSynchronize(E->streams[t]));
+  CUDA_TRY(cudaEventElapsedTime(&E->last_ms, E->ev_start, E->ev_end));
+  for (int t = 0; t < NTYPES; t++) {
+    E->last_kernel_ms[t] = 0.0f;
+    if (!E->pools[t].systems.empty()) CUDA_TRY(cudaEventElapsedTime(&E->last_kernel_ms[t], E->ev_k0[t], E->ev_k1[t]));
+  }
   return 0;
 }
 
@@ -752,17 +808,30 @@ extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
   int rc = launch_all(E, t0, n_iv, iv0, 0);
   if (rc) return rc;
   if (E->soma_cap > 0) E->soma_iv += n_iv;
-  // a stopped system is reported (its state stays readable)
+  // A system that stops (non-finite step, loop bound) is retired: it keeps
+  // its last state, the kernels skip it from now on, and every other system
+  // goes on.  The call reports systems that stopped during it.
+  int newly = 0, first_id = -1, first_status = 0;
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
     if (P.systems.empty()) continue;
     std::vector<Ctl> c(P.systems.size());
     CUDA_TRY(cudaMemcpy(c.data(), P.d_ctl, c.size() * sizeof(Ctl), cudaMemcpyDeviceToHost));
+    if (P.retired.size() != c.size()) P.retired.assign(c.size(), 0);
     for (size_t i = 0; i < c.size(); i++)
-      if (c[i].status) return fail(GBRKC_ESOLVER, "system %d (type %d) stopped with status %d", P.systems[i], t, c[i].status);
+      if (c[i].status && !P.retired[i]) {
+        P.retired[i] = 1;
+        E->n_retired++;
+        if (!newly++) { first_id = P.systems[i]; first_status = c[i].status; }
+      }
   }
+  if (newly)
+    return fail(GBRKC_ESOLVER, "%d system(s) stopped (first: system %d, status %d); the others advanced", newly,
+                first_id, first_status);
   return 0;
 }
+
+extern "C" int gbrkc_retired_systems(gbrkc_engine *E) { return E ? E->n_retired : 0; }
 
 extern "C" int gbrkc_read(gbrkc_engine *E, int id, int field, int k, double *host, long n) {
   PoolHost *P;
@@ -820,6 +889,107 @@ extern "C" int gbrkc_system_ctl(gbrkc_engine *E, int id, double *ctl8, long long
   }
   if (status) *status = c.status;
   return 0;
+}
+
+extern "C" int gbrkc_set_stim(gbrkc_engine *E, int id, const int *comp, const double *amp,
+                              const double *t0, const double *t1) {
+  PoolHost *P;
+  HostSystem *S;
+  int rc = system_loc(E, id, &P, &S);
+  if (rc) return rc;
+  if (!comp || !amp || !t0 || !t1) return fail(GBRKC_EINVAL, "null stimulus");
+  for (int c = 0; c < S->n; c++)
+    if (comp[c] >= S->ncomp) return fail(GBRKC_EINVAL, "stimulus compartment out of range");
+  const int c0 = P->sys_cell0[S->pool_index];
+  const bool f64 = E->precision == GBRKC_FP64;
+  int *dc = const_cast<int *>(f64 ? P->vd.stim_comp : P->vf.stim_comp);
+  double *da = const_cast<double *>(f64 ? P->vd.stim_amp : P->vf.stim_amp);
+  double *d0 = const_cast<double *>(f64 ? P->vd.stim_t0 : P->vf.stim_t0);
+  double *d1 = const_cast<double *>(f64 ? P->vd.stim_t1 : P->vf.stim_t1);
+  cudaStream_t st = E->streams[S->type];
+  CUDA_TRY(cudaMemcpyAsync(dc + c0, comp, S->n * sizeof(int), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(da + c0, amp, S->n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d0 + c0, t0, S->n * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d1 + c0, t1, S->n * sizeof(double), cudaMemcpyHostToDevice, st));
+  P->vd.stim_on = 1;
+  P->vf.stim_on = 1;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return 0;
+}
+
+extern "C" int gbrkc_type_cells(gbrkc_engine *E, int type) {
+  if (!E || type < 0 || type >= NTYPES) return fail(GBRKC_EINVAL, "bad type");
+  int n = 0;
+  for (auto &s : E->systems)
+    if (s.type == type) n += s.n;
+  return n;
+}
+
+extern "C" int gbrkc_set_stim_type(gbrkc_engine *E, int type, const int *comp, const double *amp,
+                                   const double *t0, const double *t1) {
+  if (!E || type < 0 || type >= NTYPES || !comp || !amp || !t0 || !t1) return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  PoolHost &P = E->pools[type];
+  if (P.systems.empty()) return 0;
+  // validate against each cell's own compartment count
+  int cell = 0;
+  for (int id : P.systems) {
+    const HostSystem &S = E->systems[id];
+    for (int c = 0; c < S.n; c++, cell++)
+      if (comp[cell] >= S.ncomp) return fail(GBRKC_EINVAL, "stimulus compartment out of range");
+  }
+  const bool f64 = E->precision == GBRKC_FP64;
+  int *dc = const_cast<int *>(f64 ? P.vd.stim_comp : P.vf.stim_comp);
+  double *da = const_cast<double *>(f64 ? P.vd.stim_amp : P.vf.stim_amp);
+  double *d0 = const_cast<double *>(f64 ? P.vd.stim_t0 : P.vf.stim_t0);
+  double *d1 = const_cast<double *>(f64 ? P.vd.stim_t1 : P.vf.stim_t1);
+  cudaStream_t st = E->streams[type];
+  CUDA_TRY(cudaMemcpyAsync(dc, comp, P.ncell * sizeof(int), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(da, amp, P.ncell * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d0, t0, P.ncell * sizeof(double), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(d1, t1, P.ncell * sizeof(double), cudaMemcpyHostToDevice, st));
+  P.vd.stim_on = 1;
+  P.vf.stim_on = 1;
+  return 0;
+}
+
+extern "C" int gbrkc_read_soma_type(gbrkc_engine *E, int type, int n_iv, double *host) {
+  if (!E || type < 0 || type >= NTYPES || !host) return fail(GBRKC_EINVAL, "bad arguments");
+  PoolHost &P = E->pools[type];
+  if (P.systems.empty()) return 0;
+  if (!P.d_soma || n_iv > E->soma_iv) return fail(GBRKC_EINVAL, "no such recording");
+  CUDA_TRY(cudaMemcpyAsync(host, P.d_soma, (size_t)n_iv * P.ncell * sizeof(double), cudaMemcpyDeviceToHost,
+                           E->streams[type]));
+  CUDA_TRY(cudaStreamSynchronize(E->streams[type]));
+  return 0;
+}
+
+extern "C" int gbrkc_rewind_soma(gbrkc_engine *E) {
+  if (!E) return fail(GBRKC_EINVAL, "null engine");
+  E->soma_iv = 0;
+  return 0;
+}
+
+// sum over systems of (stage evaluations + step attempts) x compartments:
+// the compartment-update count of the benchmark metric
+extern "C" long long gbrkc_compartment_updates(gbrkc_engine *E, int type) {
+  if (!E || !E->built) return (long long)fail(GBRKC_ESTATE, "engine not built");
+  long long total = 0;
+  for (int t = 0; t < NTYPES; t++) {
+    if (type >= 0 && t != type) continue;
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty()) continue;
+    std::vector<Ctl> c(P.systems.size());
+    if (cudaMemcpy(c.data(), P.d_ctl, c.size() * sizeof(Ctl), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return (long long)fail(GBRKC_ECUDA, "reading counters failed");
+    for (size_t i = 0; i < c.size(); i++) total += (c[i].n_stage + c[i].n_steps) * (long long)P.sys_nc[i];
+  }
+  return total;
+}
+
+extern "C" float gbrkc_last_advance_ms(gbrkc_engine *E) { return E ? E->last_ms : 0.0f; }
+extern "C" float gbrkc_last_kernel_ms(gbrkc_engine *E, int type) {
+  return (E && type >= 0 && type < NTYPES) ? E->last_kernel_ms[type] : 0.0f;
 }
 
 extern "C" int gbrkc_system_nc(gbrkc_engine *E, int id) {

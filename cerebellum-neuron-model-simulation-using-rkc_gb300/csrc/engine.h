@@ -39,6 +39,7 @@ enum Status : int {
 struct Ctl {
   double absh, sprad, naccpt, errold, hold, lt, tend, gt, gt_old, idid, mmax, hw0, hw1;
   double sum_dt, integ, hmin, tol;
+  double cbrt_errold;  // errold^(1/3), carried from the last accepted step
   int map[5];          // logical {y, yn, fn, vtemp1, vtemp2} -> physical buffer
   int newspc, jacatt, last, status;
   long long n_steps, n_rej, n_stage, n_rho, n_rho_iter, n_ion;
@@ -89,9 +90,9 @@ struct PoolView {
   long ws_tile_doubles;               // shared-memory workspace per team
 };
 
-// Team shapes the kernels are instantiated for: 4 or 32 lanes per system, or
-// a whole block per system.
-enum TeamKind { TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0 };
+// Team shapes the kernels are instantiated for: one thread (tiny cells, 32
+// systems per warp), 4 or 32 lanes per system, or a whole block per system.
+enum TeamKind { TEAM_THREAD = 1, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0 };
 
 // Launch the advance / initialise kernel of one pool (kernels.cu).
 template <typename R>

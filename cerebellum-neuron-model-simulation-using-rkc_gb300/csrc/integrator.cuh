@@ -32,7 +32,9 @@ struct TileTeam {
   int r;
   __device__ __forceinline__ int rank() const { return r; }
   __device__ __forceinline__ int size() const { return T; }
-  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+  __device__ __forceinline__ void sync() const {
+    if (T > 1) __syncwarp(mask);
+  }
 };
 
 // logical vectors of the reference (param.h:21)
@@ -100,7 +102,7 @@ struct Sys {
   }
 
   // pairwise tree over a[0..n): stride doubling, identical to the oracle
-  __device__ double tree_sum(double *a, int n) const {
+  __device__ __forceinline__ double tree_sum(double *a, int n) const {
     tm.sync();
     for (int stride = 1; stride < n; stride *= 2) {
       const int step = 2 * stride;
@@ -112,14 +114,14 @@ struct Sys {
     return r;
   }
 
-  __device__ double sumsq(const double *a) const {
+  __device__ __forceinline__ double sumsq(const double *a) const {
     double *sc = scratch();
     for (int i = tm.rank(); i < nc; i += tm.size()) sc[i] = a[i] * a[i];
     return tree_sum(sc, nc);
   }
 
   // ---------------------------------------------------------------- rkcrho
-  __device__ void rkcrho() {
+  __device__ __forceinline__ void rkcrho() {
     const double uround = UROUND, sqrtu = sqrt(UROUND), small = 1.0 / 0.125;
     double *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
     double *ede = P.ede + off, *sc = scratch();
@@ -187,7 +189,7 @@ struct Sys {
   }
 
   // ----------------------------------------------------------------- step
-  __device__ bool step(double h, int m) {
+  __device__ __forceinline__ bool step(double h, int m) {
     if (m > P.coef_mmax) {
       c.status |= ST_COEF_TABLE;
       return false;
@@ -230,7 +232,7 @@ struct Sys {
   }
 
   // --------------------------------------------------------------- rkclow
-  __device__ void rkclow() {
+  __device__ __forceinline__ void rkclow() {
     const double hmax = H_MAX, hmin = c.hmin;
     for (int loop = 1; loop <= RKCLOW_LOOP_CAP; loop++) {
       if (c.newspc) {
@@ -302,15 +304,18 @@ struct Sys {
         c.map[LYN] = c.map[LY];
         c.map[LY] = tmp;
       }
+      // err^(1/3) once; err^(2/3) as its square; errold^(1/3) carried over
       double fac = 10.0, temp1, temp2;
+      const double cr = cm_pow(err, 1.0 / 3.0);
       if (c.naccpt == 1) {
-        temp2 = cm_pow(err, 1.0 / 3.0);
+        temp2 = cr;
         if (0.8 < fac * temp2) fac = 0.8 / temp2;
       } else {
-        temp1 = 0.8 * c.absh * cm_pow(c.errold, 1.0 / 3.0);
-        temp2 = fabs(c.hold) * cm_pow(err, 2.0 / 3.0);
+        temp1 = 0.8 * c.absh * c.cbrt_errold;
+        temp2 = fabs(c.hold) * (cr * cr);
         if (temp1 < fac * temp2) fac = temp1 / temp2;
       }
+      c.cbrt_errold = cr;
       c.absh = ((0.1 > fac) ? 0.1 : fac) * c.absh;
       {
         const double mn = fmin(hmax, c.absh);
@@ -326,7 +331,7 @@ struct Sys {
   }
 
   // ------------------------------------------ ion update + current vector b
-  __device__ void ion_and_b(double sum_dt, bool update_ion, bool with_gap = true) {
+  __device__ __forceinline__ void ion_and_b(double sum_dt, bool update_ion, bool with_gap = true) {
     const double *vy = vec(LY);
     double *b = bvec();
     const Slots<R> sl0{P.ion, P.cond, P.stride, 0};
@@ -393,7 +398,7 @@ struct Sys {
 
   // ----------------------------------------------------- initialisation
   // RKC_vec_initialize: b from the initial V, vectors, rho, first step
-  __device__ void initialize() {
+  __device__ __forceinline__ void initialize() {
     double *y = vec(LY), *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
     double *ede = P.ede + off;
     for (int i = tm.rank(); i < nc; i += tm.size()) {
@@ -449,7 +454,7 @@ struct Sys {
 
   // ---------------------------------------------------- one output interval
   // *_set_current at t, then *_solve_by_rkc (solve_rkc.cu:1122-1362)
-  __device__ bool interval(double t) {
+  __device__ __forceinline__ bool interval(double t) {
     if (P.stim_on) {
       for (int cc = tm.rank(); cc < ncell; cc += tm.size()) {
         const int pc = cell0 + cc;
@@ -518,7 +523,7 @@ __device__ void ws_copy(const Team &tm, double *dst, const double *src, long n) 
 
 // Advance one system by n_iv intervals starting at t0 (or initialise it).
 template <int CT, typename R, class Team>
-__device__ void run_system(const PoolView<R> &P, const Team &tm, int s, double *smem_ws, double t0,
+__device__ __forceinline__ void run_system(const PoolView<R> &P, const Team &tm, int s, double *smem_ws, double t0,
                            int n_iv, int iv0_global, bool init) {
   const long wsn = (long)WS_VECS * (long)((P.sys_nc[s] + 1) & ~1);
   double *gws = P.ws + P.sys_ws[s];

@@ -12,7 +12,8 @@
 namespace gbrkc {
 
 template <int CT, typename R, int TS>
-__global__ void __launch_bounds__(256) k_advance(PoolView<R> P, double t0, int n_iv, int iv0, int init) {
+__global__ void __launch_bounds__(256, 1) k_advance(const __grid_constant__ PoolView<R> P, double t0, int n_iv,
+                                                 int iv0, int init) {
   extern __shared__ __align__(16) double smem[];
   if (TS == TEAM_BLOCK) {
     BlockTeam tm;
@@ -26,6 +27,8 @@ __global__ void __launch_bounds__(256) k_advance(PoolView<R> P, double t0, int n
     TileTeam<TS> tm;
     tm.r = threadIdx.x % T;
     tm.mask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << ((threadIdx.x & 31) / T * T));
+    // thread teams need no warp-level synchronisation at all
+    if (T == 1) tm.mask = 1u << (threadIdx.x & 31);
     double *my = smem + (long)tile * P.ws_tile_doubles;
     for (int s = blockIdx.x * tiles + tile; s < P.nsys; s += gridDim.x * tiles)
       run_system<CT, R, TileTeam<TS>>(P, tm, s, my, t0, n_iv, iv0, init != 0);
@@ -35,6 +38,7 @@ __global__ void __launch_bounds__(256) k_advance(PoolView<R> P, double t0, int n
 template <int CT, typename R>
 static const void *kernel_for(int team) {
   switch (team) {
+    case TEAM_THREAD: return (const void *)k_advance<CT, R, TEAM_THREAD>;
     case TEAM_TILE4: return (const void *)k_advance<CT, R, TEAM_TILE4>;
     case TEAM_WARP: return (const void *)k_advance<CT, R, TEAM_WARP>;
     default: return (const void *)k_advance<CT, R, TEAM_BLOCK>;

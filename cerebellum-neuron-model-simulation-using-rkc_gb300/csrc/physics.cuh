@@ -317,6 +317,11 @@ __device__ bool small_solve(R (&A)[N][N], R (&b)[N]) {
       R t = b[i]; b[i] = b[piv]; b[piv] = t;
     }
     for (int j = i + 1; j < N; j++) {
+      // A row whose entry in the pivot column is exactly zero has multiplier
+      // zero and would be left unchanged (x - y * 0 = x): skip it.  The
+      // kinetic matrices are banded, so this removes most of the work while
+      // producing the same values as the dense elimination.
+      if (A[j][i] == R(0.0)) continue;
       R w = A[j][i] / A[i][i];
       A[j][i] = R(0.0);
       for (int k = i + 1; k < N; k++) A[j][k] = A[j][k] - A[i][k] * w;

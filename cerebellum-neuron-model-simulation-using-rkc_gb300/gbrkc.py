@@ -57,6 +57,20 @@ def lib() -> C.CDLL:
         L.gbrkc_total_compartments.argtypes = [P]
         L.gbrkc_total_compartments.restype = C.c_long
         L.gbrkc_last_error.restype = C.c_char_p
+        L.gbrkc_set_stim.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.gbrkc_last_advance_ms.argtypes = [P]
+        L.gbrkc_last_advance_ms.restype = C.c_float
+        L.gbrkc_last_kernel_ms.argtypes = [P, C.c_int]
+        L.gbrkc_last_kernel_ms.restype = C.c_float
+        L.gbrkc_type_cells.argtypes = [P, C.c_int]
+        L.gbrkc_set_stim_type.argtypes = [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.gbrkc_read_soma_type.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.gbrkc_rewind_soma.argtypes = [P]
+        L.gbrkc_retired_systems.argtypes = [P]
+        L.gbrkc_compartment_updates.argtypes = [P, C.c_int]
+        L.gbrkc_compartment_updates.restype = C.c_longlong
         _LIB = L
     return _LIB
 
@@ -135,8 +149,16 @@ class Engine:
         _check(lib().gbrkc_build(self.h))
         self._keep = []
 
-    def advance(self, t0: float, n_intervals: int):
-        _check(lib().gbrkc_advance(self.h, t0, n_intervals))
+    def advance(self, t0: float, n_intervals: int, tolerate_retire: bool = False):
+        """Advance every system.  A system whose step goes non-finite is
+        retired (the others continue); that raises unless tolerate_retire."""
+        rc = lib().gbrkc_advance(self.h, t0, n_intervals)
+        if rc == -5 and tolerate_retire:
+            return
+        _check(rc)
+
+    def retired(self) -> int:
+        return lib().gbrkc_retired_systems(self.h)
 
     def nc(self, sid: int) -> int:
         return lib().gbrkc_system_nc(self.h, sid)
@@ -171,3 +193,38 @@ class Engine:
 
     def total_compartments(self) -> int:
         return lib().gbrkc_total_compartments(self.h)
+
+    def set_stim(self, sid, comp, amp, t0, t1):
+        _, n, _ = self.ncomp[sid]
+        comp = np.ascontiguousarray(np.broadcast_to(comp, n), dtype=np.int32)
+        amp, t0, t1 = (np.ascontiguousarray(np.broadcast_to(a, n), dtype=np.float64) for a in (amp, t0, t1))
+        _check(lib().gbrkc_set_stim(self.h, sid, _ip(comp), _dp(amp), _dp(t0), _dp(t1)))
+
+    def type_cells(self, cell_type: int) -> int:
+        n = lib().gbrkc_type_cells(self.h, cell_type)
+        if n < 0:
+            _check(n)
+        return n
+
+    def set_stim_type(self, cell_type, comp, amp, t0, t1):
+        """Bulk stimulus upload from host buffers (np arrays of type_cells entries)."""
+        _check(lib().gbrkc_set_stim_type(self.h, cell_type, _ip(comp), _dp(amp), _dp(t0), _dp(t1)))
+
+    def read_soma_type(self, cell_type: int, n_intervals: int, out: np.ndarray):
+        _check(lib().gbrkc_read_soma_type(self.h, cell_type, n_intervals, _dp(out)))
+        return out
+
+    def rewind_soma(self):
+        _check(lib().gbrkc_rewind_soma(self.h))
+
+    def compartment_updates(self, cell_type: int = -1) -> int:
+        n = lib().gbrkc_compartment_updates(self.h, cell_type)
+        if n < 0:
+            _check(int(n))
+        return int(n)
+
+    def last_advance_ms(self) -> float:
+        return float(lib().gbrkc_last_advance_ms(self.h))
+
+    def last_kernel_ms(self, cell_type: int) -> float:
+        return float(lib().gbrkc_last_kernel_ms(self.h, cell_type))

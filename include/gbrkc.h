@@ -79,8 +79,13 @@ int gbrkc_build(gbrkc_engine *e);
 /* Advance every system by n_intervals output intervals of 0.125 ms, the
  * first one starting at time t0 (ms), in one device-resident launch per cell
  * type.  Equivalent to the reference's main loop calling *_set_current and
- * *_solve_update_v once per interval (main.cu:182-311). */
+ * *_solve_update_v once per interval (main.cu:182-311).  A system whose step
+ * becomes non-finite stops (the reference exits, main.cu:202); here it is
+ * retired -- kept readable, skipped afterwards -- and GBRKC_ESOLVER reports
+ * the systems that stopped during this call while all others advanced. */
 int gbrkc_advance(gbrkc_engine *e, double t0, int n_intervals);
+/* Number of retired systems so far. */
+int gbrkc_retired_systems(gbrkc_engine *e);
 
 /* Copy n values of a per-compartment field of one system to host memory. */
 int gbrkc_read(gbrkc_engine *e, int sys_id, int field, int k, double *host, long n);
@@ -96,7 +101,32 @@ int gbrkc_system_nc(gbrkc_engine *e, int sys_id);
 int gbrkc_record_soma(gbrkc_engine *e, int n_intervals_max);
 int gbrkc_read_soma(gbrkc_engine *e, int sys_id, int n_intervals, double *host);
 
-/* Total compartments, and the CUDA stream pools launch on (one per type). */
+/* Replace the step-current table of one system (host buffers, nx*ny each);
+ * takes effect from the next interval. */
+int gbrkc_set_stim(gbrkc_engine *e, int sys_id, const int *comp, const double *amp,
+                   const double *t0, const double *t1);
+
+/* The same for every cell of one type at once: arrays of gbrkc_type_cells()
+ * entries, cells in system order (bulk host-to-device copies). */
+int gbrkc_type_cells(gbrkc_engine *e, int cell_type);
+int gbrkc_set_stim_type(gbrkc_engine *e, int cell_type, const int *comp, const double *amp,
+                        const double *t0, const double *t1);
+/* Soma recording of every cell of one type, [interval][cell] (one copy), and
+ * restart of the recording window without reallocating. */
+int gbrkc_read_soma_type(gbrkc_engine *e, int cell_type, int n_intervals, double *host);
+int gbrkc_rewind_soma(gbrkc_engine *e);
+
+/* Device time of the last gbrkc_advance (CUDA events on the launching
+ * streams): whole advance, and the kernel of one cell type. */
+float gbrkc_last_advance_ms(gbrkc_engine *e);
+float gbrkc_last_kernel_ms(gbrkc_engine *e, int cell_type);
+
+/* Compartment updates so far (sum over systems of (stage evaluations + step
+ * attempts) x compartments; power iterations excluded), for one cell type
+ * or, with cell_type = -1, all.  Negative on error. */
+long long gbrkc_compartment_updates(gbrkc_engine *e, int cell_type);
+
+/* Total compartments over all systems. */
 long gbrkc_total_compartments(gbrkc_engine *e);
 const char *gbrkc_last_error(void);
 

@@ -18,6 +18,10 @@
  *        plus e ln2 with the same two-part ln2.
  *   pow: exp(y log x) for x >= 0.
  *
+ * The canonical step-size controller evaluates err^(1/3) once per step with
+ * cm_pow, takes err^(2/3) as its square and reuses the cube root of the
+ * previous error (the reference calls pow three times, solve_rkc.cu:1038-1051).
+ *
  * Accuracy against the correctly rounded result is within a few ulp
  * (tests/test_canon_math.py).  The CUDA product carries its own copy of the
  * same algorithm (csrc/canon_math.cuh); a GPU test checks the two agree bit

@@ -119,6 +119,7 @@ struct orc_sys {
   /* controller (param.h:22, h_work/h_others/h_bool of solve_rkc.cu) */
   double mmax, absh, sprad, naccpt, atol, rtol, idid, gt, gt_old, lt, tend, errold,
       hold, nstsig;
+  double cbrt_errold; /* canonical mode: errold^(1/3) kept from the last accepted step */
   double hw[8];
   int last, newspc, jacatt;
   double sum_dt, integ;
@@ -1300,6 +1301,7 @@ int orc_init(orc_sys *s) {
   memset(s->hw, 0, sizeof s->hw);
   s->mmax = s->absh = s->sprad = s->naccpt = s->idid = s->gt = s->gt_old = s->lt = 0.0;
   s->errold = s->hold = s->nstsig = 0.0;
+  s->cbrt_errold = 0.0;
   s->hw[2] = nc; s->hw[3] = UROUND; s->hw[4] = sqrt(UROUND); s->hw[5] = H_MAX; s->hw[6] = s->hmin;
   s->tend = H_MAX;
   s->last = 1; s->newspc = 1; s->jacatt = 0;
@@ -1463,7 +1465,20 @@ static void rkclow(orc_sys *s) {
       s->map[LYN] = s->map[LY]; s->map[LY] = tmp;
     }
     fac = 10.0;
-    if (s->naccpt == 1) {
+    if (s->canon) {
+      /* canonical: err^(1/3) once; err^(2/3) as its square; errold^(1/3)
+       * carried over from the previous accepted step */
+      const double cr = cm_pow(err, 1.0 / 3.0);
+      if (s->naccpt == 1) {
+        temp2 = cr;
+        if (0.8 < fac * temp2) fac = 0.8 / temp2;
+      } else {
+        temp1 = 0.8 * s->absh * s->cbrt_errold;
+        temp2 = fabs(s->hold) * (cr * cr);
+        if (temp1 < fac * temp2) fac = temp1 / temp2;
+      }
+      s->cbrt_errold = cr;
+    } else if (s->naccpt == 1) {
       temp2 = POW(err, 1.0 / 3.0);
       if (0.8 < fac * temp2) fac = 0.8 / temp2;
     } else {
