@@ -4,7 +4,8 @@ Default workload (BASELINE config "mixed-type batch"): 4096 reduced granule
 cells, 1024 Golgi cells, 256 Purkinje cells and one 16x16 inferior-olive
 gap-junction network, FP32 gating with FP64 voltage, advanced together.
 A step advances every system by --step-ms of simulated time (default 5 ms =
-40 output intervals) in one device-resident launch per cell type.
+40 output intervals) in one persistent launch: every CTA takes a cell-type
+role and pulls systems from that role's work queue.
 
 Unit: one compartment-update = one RKC right-hand-side (stage) evaluation of
 one compartment: sum over step attempts of (m + 1) x compartments, accepted
@@ -281,28 +282,45 @@ def main():
     t_max_ms = barrier_max(dist, dev_ms)
     units_all = barrier_sum(dist, units)
     value = units_all / (t_max_ms * 1e-3)
-    launches = args.steps * sum(1 for k in range(4) if eng.type_cells(k) > 0)
+    persistent, role_ctas = eng.launch_layout()
+    if persistent:
+        launches = args.steps
+    else:
+        launches = args.steps * sum(1 for k in range(4) if eng.type_cells(k) > 0)
 
-    # roofline of the dominant kernel
-    dom = max(range(4), key=lambda k: kern_ms[k])
+    # roofline of the dominant kernel: the one persistent launch, or the
+    # longest per-type launch
     names = {0: "gr", 1: "go", 2: "pkj", 3: "io"}
     peak, peak_kind = peaks()
     bpu = ALG_BYTES[precision]
-    per_launch_bytes = bpu * units_t[dom] / args.steps
-    per_launch_ms = kern_ms[dom] / args.steps
+    if persistent:
+        kname, key = "k_mega", "mega"
+        per_launch_units = units / args.steps
+        per_launch_ms = dev_ms / args.steps
+    else:
+        dom = max(range(4), key=lambda k: kern_ms[k])
+        kname, key = f"k_advance<{names[dom]}>", names[dom]
+        per_launch_units = units_t[dom] / args.steps
+        per_launch_ms = kern_ms[dom] / args.steps
+    per_launch_bytes = bpu * per_launch_units
     achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
     traffic = None
     tfile = os.path.join(ROOT, "profiles", f"traffic_{args.config}_{precision}.json")
     if os.path.exists(tfile):
         try:
             tr = json.load(open(tfile))
-            traffic = tr.get(names[dom])
+            # bytes per compartment-update from one capture, scaled to this launch
+            if key in tr:
+                traffic = tr[key] * per_launch_units
         except Exception:
             traffic = None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "kernel": f"k_advance<{names[dom]}>",
+                "frac": achieved / peak, "traffic": traffic, "kernel": kname,
                 "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_update": bpu,
-                "kernel_ms_per_step": {names[k]: kern_ms[k] / args.steps for k in range(4)}}
+                "role_ms_per_step" if persistent else "kernel_ms_per_step":
+                    {names[k]: kern_ms[k] / args.steps for k in range(4)}}
+    if persistent:
+        roofline["role_ctas"] = {names[k]: role_ctas[k] for k in range(4)}
 
     # end to end through the C ABI with host buffers: per step, upload every
     # cell's stimulus table (pinned host -> device) and read back every cell's

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -374,7 +375,7 @@ struct PoolHost {
   std::vector<int> stim_comp, cell_soma;
   std::vector<double> stim_amp, stim_t0, stim_t1;
   long ws_total = 0;
-  int max_nc = 0;
+  int max_nc = 0, min_nc = 1 << 30;
   // launch configuration
   int team = TEAM_BLOCK, block = 256, grid = 1;
   size_t smem = 0;
@@ -415,6 +416,14 @@ struct gbrkc_engine {
   int n_retired = 0;
   cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_k0[NTYPES] = {}, ev_k1[NTYPES] = {};
   float last_ms = 0.0f, last_kernel_ms[NTYPES] = {};
+  // persistent mixed-type launch
+  bool mega = false;
+  int mega_grid = 0;
+  size_t mega_smem = 0;
+  int role_ctas[NTYPES] = {};
+  int role_cap[NTYPES] = {};
+  int *d_queue = nullptr;
+  unsigned long long *d_tstart = nullptr, *d_tend = nullptr;
   ~gbrkc_engine() {
     for (auto &s : streams)
       if (s) cudaStreamDestroy(s);
@@ -552,6 +561,7 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
     P.sys_ncomp.push_back(S.ncomp);
     P.sys_cell0.push_back(cell0);
     P.max_nc = std::max(P.max_nc, S.nc);
+    P.min_nc = std::min(P.min_nc, S.nc);
     // template (pool-local)
     auto tl = P.tmpl_local.find(S.tmpl);
     if (tl == P.tmpl_local.end()) {
@@ -639,19 +649,33 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
   P.ws_total = ws;
   // launch configuration: team shape by system size, workspace in shared
   // memory when it fits
-  // tiny cells: one lane per compartment, 16 cells per 64-thread block (more
-  // warps per SM to hide the serial controller's latency)
-  if (P.max_nc <= 4) { P.team = TEAM_TILE4; P.block = 64; }
-  else if (P.max_nc <= 8) { P.team = TEAM_TILE4; P.block = 128; }
+  // tiny cells: one system per thread, the block's first warps spread over
+  // the SMs (a warp's FP64 instructions cost the same for 1 or 32 lanes, so
+  // 32 systems side by side beat one system over 4 lanes)
+  const int nsys = (int)P.systems.size();
+  if (P.max_nc <= LANE_MAX_NC) {
+    P.team = (P.type == GR && P.min_nc == 4 && P.max_nc == 4) ? TEAM_LANE4 : TEAM_THREAD;
+    P.block = MEGA_BLOCK;
+  }
   else if (P.max_nc <= 320) { P.team = TEAM_WARP; P.block = 128; }
   else { P.team = TEAM_BLOCK; P.block = 256; }
-  const int teams = (P.team == TEAM_BLOCK) ? 1 : P.block / P.team;
+  const bool lanes = (P.team == TEAM_THREAD || P.team == TEAM_LANE4);
+  // single-lane workspaces interleave across all MEGA_BLOCK threads of the
+  // block, whichever of them hold a system
+  const int teams = (P.team == TEAM_BLOCK) ? 1 : lanes ? MEGA_BLOCK : P.block / P.team;
   P.ws_tile = (long)WS_VECS * ((P.max_nc + 1) & ~1);
   const size_t need = (size_t)teams * P.ws_tile * sizeof(double);
   P.ws_in_smem = need <= 200 * 1024;
+  if (lanes && !P.ws_in_smem) return fail(GBRKC_EINVAL, "single-lane pool workspace does not fit shared memory");
   P.smem = P.ws_in_smem ? need : 0;
-  const int nsys = (int)P.systems.size();
-  P.grid = (nsys + teams - 1) / teams;
+  if (P.team == TEAM_THREAD || P.team == TEAM_LANE4) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    P.grid = std::max(1, std::min((nsys + 31) / 32, sms));
+  } else {
+    P.grid = (nsys + teams - 1) / teams;
+  }
   return 0;
 }
 
@@ -730,13 +754,76 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
 // Launch every pool's kernel on its own stream (the pools run concurrently)
 // and time the whole advance and each kernel with CUDA events recorded on the
 // launching streams.
+void rebalance_roles(gbrkc_engine *E, const double *role_ms);
+
+template <typename R> PoolView<R> &pool_view(PoolHost &P);
+template <> PoolView<double> &pool_view<double>(PoolHost &P) { return P.vd; }
+template <> PoolView<float> &pool_view<float>(PoolHost &P) { return P.vf; }
+
+template <typename R>
+int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
+  MegaView<R> M{};
+  int end = 0;
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    M.pool[t] = P.systems.empty() ? PoolView<R>{} : pool_view<R>(P);
+    end += E->role_ctas[t];
+    M.role_end[t] = end;
+  }
+  M.lane_warps = 8;
+  M.gr_nc4 = E->pools[GR].team == TEAM_LANE4;
+  if (E->role_ctas[GR] > 0) {
+    const int nsys = (int)E->pools[GR].systems.size();
+    const int per_cta = (nsys + E->role_ctas[GR] - 1) / E->role_ctas[GR];
+    M.lane_warps = std::min(MEGA_BLOCK / 32, std::max(1, (per_cta + 31) / 32));
+  }
+  if (E->role_ctas[GR] > 0 &&
+      (!E->pools[GR].ws_in_smem ||
+       E->mega_smem < (size_t)MEGA_BLOCK * (size_t)E->pools[GR].ws_tile * sizeof(double)))
+    return fail(GBRKC_ESTATE, "persistent launch: granule workspaces do not fit its shared memory");
+  M.queue = E->d_queue;
+  M.t_start = E->d_tstart;
+  M.t_end = E->d_tend;
+  cudaStream_t st = E->streams[0];
+  CUDA_TRY(cudaMemsetAsync(E->d_queue, 0, NTYPES * sizeof(int), st));
+  CUDA_TRY(cudaEventRecord(E->ev_start, st));
+  int rc = launch_mega<R>(M, end, E->mega_smem, st, t0, n_iv, iv0, init);
+  if (rc) return fail(GBRKC_ECUDA, "persistent launch: %s", cudaGetErrorString((cudaError_t)rc));
+  CUDA_TRY(cudaEventRecord(E->ev_end, st));
+  CUDA_TRY(cudaEventSynchronize(E->ev_end));
+  CUDA_TRY(cudaEventElapsedTime(&E->last_ms, E->ev_start, E->ev_end));
+  // per-role makespans from the CTAs' device timestamps
+  std::vector<unsigned long long> ts(end), te(end);
+  CUDA_TRY(cudaMemcpy(ts.data(), E->d_tstart, end * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(te.data(), E->d_tend, end * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  unsigned long long t_first = ~0ull;
+  for (int b = 0; b < end; b++) t_first = std::min(t_first, ts[b]);
+  double role_ms[NTYPES] = {};
+  int b = 0;
+  for (int t = 0; t < NTYPES; t++) {
+    unsigned long long last = t_first;
+    for (int k = 0; k < E->role_ctas[t]; k++, b++) last = std::max(last, te[b]);
+    role_ms[t] = E->role_ctas[t] ? (double)(last - t_first) * 1e-6 : 0.0;
+    E->last_kernel_ms[t] = (float)role_ms[t];
+  }
+  if (!init && n_iv > 0) rebalance_roles(E, role_ms);
+  return 0;
+}
+
 int launch_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
+  if (E->mega)
+    return (E->precision == GBRKC_FP64) ? launch_mega_all<double>(E, t0, n_iv, iv0, init)
+                                        : launch_mega_all<float>(E, t0, n_iv, iv0, init);
   CUDA_TRY(cudaEventRecord(E->ev_start, E->streams[0]));
   for (int t = 1; t < NTYPES; t++) CUDA_TRY(cudaStreamWaitEvent(E->streams[t], E->ev_start, 0));
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
     if (P.systems.empty()) continue;
     int rc;
+    if ((P.team == TEAM_THREAD || P.team == TEAM_LANE4) &&
+        (P.block != MEGA_BLOCK || !P.ws_in_smem ||
+         P.smem < (size_t)MEGA_BLOCK * (size_t)P.ws_tile * sizeof(double)))
+      return fail(GBRKC_ESTATE, "single-lane pool %d: launch shape does not cover its workspaces", t);
     CUDA_TRY(cudaEventRecord(E->ev_k0[t], E->streams[t]));
     if (E->precision == GBRKC_FP64)
       rc = launch_pool<double>(t, P.vd, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
@@ -767,6 +854,97 @@ int system_loc(gbrkc_engine *E, int id, PoolHost **P, HostSystem **S) {
 
 }  // namespace
 
+namespace {
+
+// Re-split the persistent launch's CTAs between roles so that they finish
+// together: each role's work is estimated as (its CTAs x its makespan) from
+// the last launch, and CTAs are handed out in proportion, within each role's
+// cap (a role cannot use more CTAs than it has teams of work).
+void rebalance_roles(gbrkc_engine *E, const double *role_ms) {
+  double work[NTYPES] = {}, total = 0.0;
+  for (int t = 0; t < NTYPES; t++)
+    if (E->role_ctas[t] > 0) { work[t] = std::max(role_ms[t], 1e-3) * E->role_ctas[t]; total += work[t]; }
+  if (total <= 0.0) return;
+  int want[NTYPES] = {}, used = 0;
+  for (int t = 0; t < NTYPES; t++) {
+    if (E->role_ctas[t] == 0) continue;
+    double share = E->mega_grid * work[t] / total;
+    int n = (int)std::lround(0.5 * E->role_ctas[t] + 0.5 * share);
+    want[t] = std::max(1, std::min(E->role_cap[t], n));
+    used += want[t];
+  }
+  // fix the total by moving CTAs to / from the role with the largest work per CTA
+  while (used != E->mega_grid) {
+    int best = -1;
+    double bv = used < E->mega_grid ? -1.0 : 1e300;
+    for (int t = 0; t < NTYPES; t++) {
+      if (want[t] == 0) continue;
+      double v = work[t] / want[t];
+      if (used < E->mega_grid && want[t] < E->role_cap[t] && v > bv) { bv = v; best = t; }
+      if (used > E->mega_grid && want[t] > 1 && v < bv) { bv = v; best = t; }
+    }
+    if (best < 0) break;
+    want[best] += used < E->mega_grid ? 1 : -1;
+    used += used < E->mega_grid ? 1 : -1;
+  }
+  for (int t = 0; t < NTYPES; t++) E->role_ctas[t] = want[t];
+}
+
+// Decide whether all pools fit the persistent launch's team shapes and size
+// its shared memory; sets each pool's team / workspace placement.
+int setup_mega(gbrkc_engine *E) {
+  const char *no = getenv("GBRKC_NO_MEGA");
+  if (no && no[0] == '1') return 0;
+  const PoolHost &G = E->pools[GR], &O = E->pools[GO];
+  if (!G.systems.empty() && G.max_nc > LANE_MAX_NC) return 0;
+  if (!O.systems.empty() && O.max_nc > 320) return 0;
+  // granule CTAs run up to MEGA_BLOCK single-lane systems (capped below at one
+  // warp per CTA); Golgi 8 warps; Purkinje / olive one system per CTA
+  const int teams[NTYPES] = {32, MEGA_BLOCK / TEAM_WARP, 1, 1};
+  const int team_kind[NTYPES] = {(G.min_nc == 4 && G.max_nc == 4) ? TEAM_LANE4 : TEAM_THREAD, TEAM_WARP,
+                                 TEAM_BLOCK, TEAM_BLOCK};
+  size_t smem = 0;
+  int nonempty = 0;
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty()) continue;
+    nonempty++;
+    P.team = team_kind[t];
+    P.block = MEGA_BLOCK;
+    P.ws_tile = (long)WS_VECS * ((P.max_nc + 1) & ~1);
+    const size_t need = (size_t)(t == GR ? MEGA_BLOCK : teams[t]) * P.ws_tile * sizeof(double);
+    P.ws_in_smem = need <= 200 * 1024;
+    if (t == GR && !P.ws_in_smem) return 0;
+    if (P.ws_in_smem) smem = std::max(smem, need);
+    const int nsys = (int)P.systems.size();
+    E->role_cap[t] = (nsys + teams[t] - 1) / teams[t];
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int bps = 0;
+  int rc = (E->precision == GBRKC_FP64) ? prepare_mega_kernel<double>(smem, &bps) : prepare_mega_kernel<float>(smem, &bps);
+  if (rc || bps <= 0) return 0;
+  E->mega_grid = sms * bps;
+  if (E->mega_grid < nonempty) return 0;
+  E->mega_smem = smem;
+  E->mega = true;
+  // first split: by compartment count with per-type weights (granule cells
+  // take ~20x more steps per compartment); refined after every launch
+  const double w[NTYPES] = {30.0, 1.0, 0.35, 3.0};
+  double ms[NTYPES];
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    E->role_ctas[t] = P.systems.empty() ? 0 : 1;
+    ms[t] = P.systems.empty() ? 0.0 : w[t] * (double)P.nc;
+  }
+  rebalance_roles(E, ms);
+  for (int i = 0; i < 3; i++) rebalance_roles(E, ms);
+  return 0;
+}
+
+}  // namespace
+
 extern "C" int gbrkc_build(gbrkc_engine *E) {
   if (!E) return fail(GBRKC_EINVAL, "null engine");
   if (E->built) return fail(GBRKC_ESTATE, "already built");
@@ -786,7 +964,23 @@ extern "C" int gbrkc_build(gbrkc_engine *E) {
     if (P.systems.empty()) continue;
     int rc = assemble_pool(E, P);
     if (rc) return rc;
-    rc = (E->precision == GBRKC_FP64) ? upload_pool<double>(E, P, P.vd) : upload_pool<float>(E, P, P.vf);
+  }
+  {
+    int rc = setup_mega(E);
+    if (rc) return rc;
+  }
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty()) continue;
+    int rc = (E->precision == GBRKC_FP64) ? upload_pool<double>(E, P, P.vd) : upload_pool<float>(E, P, P.vf);
+    if (rc) return rc;
+  }
+  if (E->mega) {
+    std::vector<int> q(NTYPES, 0);
+    std::vector<unsigned long long> z(E->mega_grid, 0ull);
+    int rc = E->mem.upload(q, &E->d_queue);
+    if (!rc) rc = E->mem.upload(z, &E->d_tstart);
+    if (!rc) rc = E->mem.upload(z, &E->d_tend);
     if (rc) return rc;
   }
   E->built = true;
@@ -988,6 +1182,12 @@ extern "C" long long gbrkc_compartment_updates(gbrkc_engine *E, int type) {
 }
 
 extern "C" float gbrkc_last_advance_ms(gbrkc_engine *E) { return E ? E->last_ms : 0.0f; }
+
+extern "C" int gbrkc_launch_layout(gbrkc_engine *E, int *ctas_per_type) {
+  if (!E || !E->built) return fail(GBRKC_ESTATE, "engine not built");
+  for (int t = 0; t < NTYPES; t++) ctas_per_type[t] = E->mega ? E->role_ctas[t] : -1;
+  return E->mega ? 1 : 0;
+}
 extern "C" float gbrkc_last_kernel_ms(gbrkc_engine *E, int type) {
   return (E && type >= 0 && type < NTYPES) ? E->last_kernel_ms[type] : 0.0f;
 }

@@ -91,8 +91,35 @@ struct PoolView {
 };
 
 // Team shapes the kernels are instantiated for: one thread (tiny cells, 32
-// systems per warp), 4 or 32 lanes per system, or a whole block per system.
-enum TeamKind { TEAM_THREAD = 1, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0 };
+// systems per warp, blocks of MEGA_BLOCK threads with interleaved shared
+// workspaces), 4 or 32 lanes per system, or a whole block per system.
+// TEAM_LANE4: one thread per system for pools whose systems all have exactly
+// 4 compartments (loops unrolled at compile time).
+enum TeamKind { TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0 };
+
+// All pools in one persistent launch: CTA b < role_end[0] integrates granule
+// systems (one per lane, on the CTA's first lane_warps warps), then Golgi
+// (32-lane warps), Purkinje and olive (whole blocks).  Each role pulls
+// systems from its own atomic queue.
+template <typename R>
+struct MegaView {
+  PoolView<R> pool[NTYPES];
+  int role_end[NTYPES];
+  int lane_warps;             // active warps per granule CTA
+  int gr_nc4;                 // every granule system has 4 compartments
+  int *queue;                 // [NTYPES] next-system counters, zeroed per launch
+  unsigned long long *t_start; // [grid] globaltimer at each CTA's start
+  unsigned long long *t_end;   // [grid] globaltimer at each CTA's finish
+};
+
+constexpr int MEGA_BLOCK = 256;
+constexpr int LANE_MAX_NC = 8;   // largest system integrated by a single lane
+
+template <typename R>
+int launch_mega(const MegaView<R> &M, int grid, size_t smem, void *stream, double t0, int n_iv, int iv0,
+                int init);
+template <typename R>
+int prepare_mega_kernel(size_t smem, int *blocks_per_sm);
 
 // Launch the advance / initialise kernel of one pool (kernels.cu).
 template <typename R>

@@ -6,21 +6,42 @@
 // per-interval driver with its ion-update clock (*_solve_by_rkc, 1122-1362).
 //
 // One "team" of threads integrates one system; the same code runs with a
-// tile of 1..32 lanes (small cells, many per block) or a whole block (large
-// cells / networks).  Every scalar of the controller is computed redundantly
-// and identically by all team members, so control flow stays uniform within
-// a team and needs no broadcast.  Every sum is the pairwise tree over
-// compartment indices, the FP64 vector updates use the same explicit fused
-// multiply-adds as the oracle's canonical mode, and the translation unit is
-// built with -fmad=false: the plain-FP64 path reproduces the oracle bit for
-// bit.
+// tile of 4 or 32 lanes, a whole block (large cells / networks), or a single
+// lane (tiny cells: every thread its own system, the warp advancing 32
+// systems side by side).  Every scalar of the controller is computed
+// redundantly and identically by all team members, so control flow stays
+// uniform within a team and needs no broadcast.  Every sum is the pairwise
+// tree over compartment indices, the FP64 vector updates use the same
+// explicit fused multiply-adds as the oracle's canonical mode, and the
+// translation unit is built with -fmad=false: the plain-FP64 path reproduces
+// the oracle bit for bit.
+//
+// The driver is flat: one call of tick() is one step attempt (rkclow's loop
+// body) plus the bookkeeping after an accepted step, so independent systems
+// sharing a warp move through their own attempt sequences without waiting
+// for each other to accept.  A due ion update is returned to the caller
+// (TICK_ION) instead of being run inside tick(): single-lane systems park
+// until most of the warp's lanes have one due and then run them in one pass.
+// On GB300 an FP64 warp instruction costs the same whatever its active-lane
+// count, and the ion update is by far the longest path, so running it for 4
+// lanes at a time would cost nearly as much as for 32.
 #pragma once
 #include "engine.h"
 #include "physics.cuh"
 
 namespace gbrkc {
 
+// A workspace vector: element i at p[i * LS] (LS = 1, or the block width for
+// single-lane teams, whose workspaces interleave element by element so that a
+// warp's 32 systems hit 32 consecutive shared-memory words).
+template <int LS>
+struct WVec {
+  double *p;
+  __device__ __forceinline__ double &operator[](int i) const { return p[(long)i * LS]; }
+};
+
 struct BlockTeam {
+  static constexpr int LS = 1, NCF = 0;
   __device__ __forceinline__ int rank() const { return threadIdx.x; }
   __device__ __forceinline__ int size() const { return blockDim.x; }
   __device__ __forceinline__ void sync() const { __syncthreads(); }
@@ -28,6 +49,7 @@ struct BlockTeam {
 
 template <int T>
 struct TileTeam {
+  static constexpr int LS = 1, NCF = 0;
   unsigned mask;
   int r;
   __device__ __forceinline__ int rank() const { return r; }
@@ -37,15 +59,43 @@ struct TileTeam {
   }
 };
 
+// One thread, one system; workspaces interleaved across the block.  With
+// NCF > 0 every system of the pool has exactly NCF compartments: the
+// compartment loops unroll, values are computed into registers before they
+// are stored (the rotating buffers are not known to be distinct, so stores
+// would otherwise serialise the loop) and the pairwise sums run in registers.
+template <int BLOCK, int NCF_ = 0>
+struct LaneTeam {
+  static constexpr int LS = BLOCK, NCF = NCF_;
+  __device__ __forceinline__ int rank() const { return 0; }
+  __device__ __forceinline__ int size() const { return 1; }
+  __device__ __forceinline__ void sync() const {}
+};
+
+// pairwise tree over a[0..N) in registers, the same order as Sys::tree_sum
+template <int N>
+__device__ __forceinline__ double tree_regs(double (&a)[N]) {
+#pragma unroll
+  for (int stride = 1; stride < N; stride *= 2)
+#pragma unroll
+    for (int i = 0; i + stride < N; i += 2 * stride) a[i] = a[i] + a[i + stride];
+  return a[0];
+}
+
 // logical vectors of the reference (param.h:21)
 enum { LY = 0, LYN = 1, LFN = 2, LV1 = 3, LV2 = 4 };
 
 constexpr int RKCLOW_LOOP_CAP = 1000;        // solve_rkc.cu:939
 constexpr long STEPS_PER_INTERVAL_CAP = 200000;   // step attempts per 0.125 ms interval
 constexpr int RHO_ITMAX = 1000;              // solve_rkc.cu:572
+enum Tick { TICK_DONE = 0, TICK_MORE = 1, TICK_ION = 2 };
+constexpr int ION_WAIT_MAX = 12;             // warp iterations a due ion update may wait
 
 template <int CT, typename R, class Team>
 struct Sys {
+  static constexpr int LS = Team::LS, NCF = Team::NCF;
+  static constexpr int NR = NCF > 0 ? NCF : 1;   // register staging width
+  typedef WVec<LS> V;
   const PoolView<R> &P;
   const Team &tm;
   int s, nc, ncp, ncell, ncomp, off, cell0;
@@ -54,8 +104,17 @@ struct Sys {
   const double *g, *invcm;
   double *W;
   Ctl c;
+  // flat driver state
+  double t0;
+  int k_iv, n_iv, iv0, rej_run;
+  long long attempts0;
 
-  __device__ Sys(const PoolView<R> &P_, const Team &tm_, int s_, double *W_) : P(P_), tm(tm_), s(s_), W(W_) {
+  __device__ Sys(const PoolView<R> &P_, const Team &tm_) : P(P_), tm(tm_) {}
+  __device__ Sys(const PoolView<R> &P_, const Team &tm_, int s_, double *W_) : P(P_), tm(tm_) { bind(s_, W_); }
+
+  __device__ __forceinline__ void bind(int s_, double *W_) {
+    s = s_;
+    W = W_;
     nc = P.sys_nc[s];
     ncp = (nc + 1) & ~1;
     ncell = P.sys_ncell[s];
@@ -78,12 +137,12 @@ struct Sys {
     }
   }
 
-  __device__ __forceinline__ double *vec(int logical) const { return W + (long)c.map[logical] * ncp; }
-  __device__ __forceinline__ double *bvec() const { return W + (long)WS_B * ncp; }
-  __device__ __forceinline__ double *scratch() const { return W + (long)WS_SCRATCH * ncp; }
+  __device__ __forceinline__ V vec(int logical) const { return V{W + (long)c.map[logical] * ncp * LS}; }
+  __device__ __forceinline__ V bvec() const { return V{W + (long)WS_B * ncp * LS}; }
+  __device__ __forceinline__ V scratch() const { return V{W + (long)WS_SCRATCH * ncp * LS}; }
 
   // dydt at compartment i (solve_rkc.cu:178-196): (-b + sum g (y_j - y_i)) / Cm
-  __device__ __forceinline__ double rhs(const double *__restrict__ y, int i) const {
+  __device__ __forceinline__ double rhs(const V y, int i) const {
     double d = -(bvec()[i]);
     const double yi = y[i];
     int r0, r1, base, j;
@@ -102,7 +161,7 @@ struct Sys {
   }
 
   // pairwise tree over a[0..n): stride doubling, identical to the oracle
-  __device__ __forceinline__ double tree_sum(double *a, int n) const {
+  __device__ __forceinline__ double tree_sum(const V a, int n) const {
     tm.sync();
     for (int stride = 1; stride < n; stride *= 2) {
       const int step = 2 * stride;
@@ -114,8 +173,15 @@ struct Sys {
     return r;
   }
 
-  __device__ __forceinline__ double sumsq(const double *a) const {
-    double *sc = scratch();
+  template <class A>
+  __device__ __forceinline__ double sumsq(const A a) const {
+    if constexpr (NCF > 0) {
+      double q[NR];
+#pragma unroll
+      for (int i = 0; i < NCF; i++) q[i] = a[i] * a[i];
+      return tree_regs<NR>(q);
+    }
+    V sc = scratch();
     for (int i = tm.rank(); i < nc; i += tm.size()) sc[i] = a[i] * a[i];
     return tree_sum(sc, nc);
   }
@@ -123,8 +189,8 @@ struct Sys {
   // ---------------------------------------------------------------- rkcrho
   __device__ __forceinline__ void rkcrho() {
     const double uround = UROUND, sqrtu = sqrt(UROUND), small = 1.0 / 0.125;
-    double *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
-    double *ede = P.ede + off, *sc = scratch();
+    V yn = vec(LYN), fn = vec(LFN), v1 = vec(LV1), v2 = vec(LV2), sc = scratch();
+    double *ede = P.ede + off;
     double sprad_old[3] = {0.0, 0.0, 0.0};
     c.n_rho++;
     const double ynrm = sqrt(sumsq(yn));
@@ -150,13 +216,28 @@ struct Sys {
     for (int iter = 0; iter < RHO_ITMAX; iter++) {
       c.n_rho_iter++;
       // v2 = F(v1); dam = v2 - fn; squares into the scratch
-      for (int i = tm.rank(); i < nc; i += tm.size()) {
-        const double f = rhs(v1, i);
-        v2[i] = f;
-        const double dm = -1.0 * fn[i] + f;
-        sc[i] = dm * dm;
+      double dfsq;
+      if constexpr (NCF > 0) {
+        double f[NR], q[NR];
+#pragma unroll
+        for (int i = 0; i < NCF; i++) {
+          f[i] = rhs(v1, i);
+          const double dm = -1.0 * fn[i] + f[i];
+          q[i] = dm * dm;
+        }
+#pragma unroll
+        for (int i = 0; i < NCF; i++) v2[i] = f[i];
+        dfsq = tree_regs<NR>(q);
+      } else {
+        for (int i = tm.rank(); i < nc; i += tm.size()) {
+          const double f = rhs(v1, i);
+          v2[i] = f;
+          const double dm = -1.0 * fn[i] + f;
+          sc[i] = dm * dm;
+        }
+        dfsq = tree_sum(sc, nc);
       }
-      const double dfnrm = sqrt(tree_sum(sc, nc));
+      const double dfnrm = sqrt(dfsq);
       sigmal = sigma;
       sigma = dfnrm / dynrm;
       sprad_old[0] = sprad_old[1];
@@ -178,7 +259,15 @@ struct Sys {
       }
       if (dfnrm != 0.0) {
         const double al = dynrm / dfnrm;
-        for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = fma(al, fn[i] - v2[i], yn[i]);
+        if constexpr (NCF > 0) {
+          double w[NR];
+#pragma unroll
+          for (int i = 0; i < NCF; i++) w[i] = fma(al, fn[i] - v2[i], yn[i]);
+#pragma unroll
+          for (int i = 0; i < NCF; i++) v1[i] = w[i];
+        } else {
+          for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = fma(al, fn[i] - v2[i], yn[i]);
+        }
       } else {
         const int idx = iter % nc;
         if (tm.rank() == 0) v1[idx] = 2.0 * yn[idx] - v1[idx];
@@ -196,11 +285,25 @@ struct Sys {
     }
     const double *T = P.coef + P.coef_off[m];
     {
-      double *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
+      V yn = vec(LYN), fn = vec(LFN), v1 = vec(LV1), v2 = vec(LV2);
       const double hm = h * __ldg(T);
-      for (int i = tm.rank(); i < nc; i += tm.size()) {
-        v2[i] = yn[i];
-        v1[i] = fma(hm, fn[i], yn[i]);
+      if constexpr (NCF > 0) {
+        double a[NR], b[NR];
+#pragma unroll
+        for (int i = 0; i < NCF; i++) {
+          a[i] = yn[i];
+          b[i] = fma(hm, fn[i], a[i]);
+        }
+#pragma unroll
+        for (int i = 0; i < NCF; i++) {
+          v2[i] = a[i];
+          v1[i] = b[i];
+        }
+      } else {
+        for (int i = tm.rank(); i < nc; i += tm.size()) {
+          v2[i] = yn[i];
+          v1[i] = fma(hm, fn[i], yn[i]);
+        }
       }
     }
     tm.sync();
@@ -208,14 +311,29 @@ struct Sys {
       const double *q = T + 1 + 5 * (j - 1);
       const double mu = __ldg(q), nu = __ldg(q + 1), omn = __ldg(q + 2), mus = __ldg(q + 3), ajm1 = __ldg(q + 4);
       const double hm = h * mus;
-      double *y = vec(LY), *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
-      for (int i = tm.rank(); i < nc; i += tm.size()) {
-        const double f = rhs(v1, i);
-        double t = mu * v1[i];
-        t = fma(nu, v2[i], t);
-        t = fma(omn, yn[i], t);
-        const double u = fma(-ajm1, fn[i], f);
-        y[i] = fma(hm, u, t);
+      V y = vec(LY), yn = vec(LYN), fn = vec(LFN), v1 = vec(LV1), v2 = vec(LV2);
+      if constexpr (NCF > 0) {
+        double out[NR];
+#pragma unroll
+        for (int i = 0; i < NCF; i++) {
+          const double f = rhs(v1, i);
+          double t = mu * v1[i];
+          t = fma(nu, v2[i], t);
+          t = fma(omn, yn[i], t);
+          const double u = fma(-ajm1, fn[i], f);
+          out[i] = fma(hm, u, t);
+        }
+#pragma unroll
+        for (int i = 0; i < NCF; i++) y[i] = out[i];
+      } else {
+        for (int i = tm.rank(); i < nc; i += tm.size()) {
+          const double f = rhs(v1, i);
+          double t = mu * v1[i];
+          t = fma(nu, v2[i], t);
+          t = fma(omn, yn[i], t);
+          const double u = fma(-ajm1, fn[i], f);
+          y[i] = fma(hm, u, t);
+        }
       }
       const int t2 = c.map[LV2];
       c.map[LV2] = c.map[LV1];
@@ -231,38 +349,59 @@ struct Sys {
     return true;
   }
 
-  // --------------------------------------------------------------- rkclow
-  __device__ __forceinline__ void rkclow() {
+  // ------------------------------------------------------ rkclow, flat
+  // One pass of rkclow's loop body (solve_rkc.cu:939-1096): returns
+  // ATT_ACCEPT (the step was taken, c.idid = 1 or 2), ATT_REJECT (absh was
+  // reduced; call again) or ATT_FAIL (c.status set).  rej_run counts the
+  // attempts of the current rkclow call, bounded like the reference's loop.
+  enum { ATT_FAIL = -1, ATT_REJECT = 0, ATT_ACCEPT = 1 };
+
+  __device__ __forceinline__ int attempt() {
     const double hmax = H_MAX, hmin = c.hmin;
-    for (int loop = 1; loop <= RKCLOW_LOOP_CAP; loop++) {
-      if (c.newspc) {
-        rkcrho();
-        c.jacatt = 1;
-      }
+    if (c.newspc) {
+      rkcrho();
+      c.jacatt = 1;
+    }
+    c.last = 0;
+    if (1.1 * c.absh >= fabs(c.tend - c.lt)) {
+      c.absh = fabs(c.tend - c.lt);
+      c.last = 1;
+    }
+    const double marg = sqrt(1.54 * c.absh * c.sprad + 1.0);
+    if (!(marg < 1.0e9)) {
+      c.status |= ST_NAN;
+      return ATT_FAIL;
+    }
+    int m = 1 + (int)(marg);
+    if (m > c.mmax) {
+      m = (int)c.mmax;
+      c.absh = (m * m - 1) / (1.54 * c.sprad);
       c.last = 0;
-      if (1.1 * c.absh >= fabs(c.tend - c.lt)) {
-        c.absh = fabs(c.tend - c.lt);
-        c.last = 1;
-      }
-      const double marg = sqrt(1.54 * c.absh * c.sprad + 1.0);
-      if (!(marg < 1.0e9)) {
-        c.status |= ST_NAN;
-        return;
-      }
-      int m = 1 + (int)(marg);
-      if (m > c.mmax) {
-        m = (int)c.mmax;
-        c.absh = (m * m - 1) / (1.54 * c.sprad);
-        c.last = 0;
-      }
-      double h = 1.0 * c.absh;
-      if (h <= hmin) h = hmin;
-      if (!step(h, m)) return;
-      c.n_steps++;
-      // F(y) into vtemp1 and the error terms, fused
-      {
-        double *y = vec(LY), *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *sc = scratch();
-        const double h04 = 0.4 * h;
+    }
+    double h = 1.0 * c.absh;
+    if (h <= hmin) h = hmin;
+    if (!step(h, m)) return ATT_FAIL;
+    c.n_steps++;
+    // F(y) into vtemp1 and the error terms, fused
+    double err;
+    {
+      V y = vec(LY), yn = vec(LYN), fn = vec(LFN), v1 = vec(LV1), sc = scratch();
+      const double h04 = 0.4 * h;
+      if constexpr (NCF > 0) {
+        double f[NR], q[NR];
+#pragma unroll
+        for (int i = 0; i < NCF; i++) {
+          f[i] = rhs(y, i);
+          const double ay = fabs(y[i]), ayn = fabs(yn[i]);
+          const double wt = fma(c.tol, (ay > ayn) ? ay : ayn, c.tol);
+          const double est = fma(h04, fn[i] + f[i], 0.8 * (yn[i] - y[i]));
+          const double qv = est / wt;
+          q[i] = qv * qv;
+        }
+#pragma unroll
+        for (int i = 0; i < NCF; i++) v1[i] = f[i];
+        err = tree_regs<NR>(q);
+      } else {
         for (int i = tm.rank(); i < nc; i += tm.size()) {
           const double f = rhs(y, i);
           v1[i] = f;
@@ -272,68 +411,74 @@ struct Sys {
           const double qv = est / wt;
           sc[i] = qv * qv;
         }
+        err = tree_sum(sc, nc);
       }
-      double err = tree_sum(scratch(), nc);
-      err = sqrt(err / (double)nc);
-      if (!(err == err)) {
-        c.status |= ST_NAN;
-        return;
-      }
-      if (err > 1.0) {
-        c.absh = 0.8 * c.absh / (cm_pow(err, 1.0 / 3.0));
-        c.n_rej++;
-        if (c.absh < hmin) {
-          c.idid = 4;
-        } else {
-          c.newspc = !c.jacatt;
-          continue;
-        }
-      }
-      c.naccpt += 1;
-      c.lt += h;
-      c.gt = c.lt;
-      c.jacatt = 0;
-      c.newspc = 0;  // nstsig never advances (solve_rkc.cu:1024-1026)
-      c.hw0 = h;
-      c.hw1 = c.lt;
-      {
-        const int tmp = c.map[LV2];
-        c.map[LV2] = c.map[LFN];
-        c.map[LFN] = c.map[LV1];
-        c.map[LV1] = c.map[LYN];
-        c.map[LYN] = c.map[LY];
-        c.map[LY] = tmp;
-      }
-      // err^(1/3) once; err^(2/3) as its square; errold^(1/3) carried over
-      double fac = 10.0, temp1, temp2;
-      const double cr = cm_pow(err, 1.0 / 3.0);
-      if (c.naccpt == 1) {
-        temp2 = cr;
-        if (0.8 < fac * temp2) fac = 0.8 / temp2;
-      } else {
-        temp1 = 0.8 * c.absh * c.cbrt_errold;
-        temp2 = fabs(c.hold) * (cr * cr);
-        if (temp1 < fac * temp2) fac = temp1 / temp2;
-      }
-      c.cbrt_errold = cr;
-      c.absh = ((0.1 > fac) ? 0.1 : fac) * c.absh;
-      {
-        const double mn = fmin(hmax, c.absh);
-        c.absh = (hmin > mn) ? hmin : mn;
-      }
-      c.errold = err;
-      c.hold = h;
-      c.idid = c.last ? 1 : 2;
-      tm.sync();
-      return;
     }
-    c.status |= ST_LOOP_CAP;
+    err = sqrt(err / (double)nc);
+    if (!(err == err)) {
+      c.status |= ST_NAN;
+      return ATT_FAIL;
+    }
+    // err^(1/3), shared by the reject and accept paths (one evaluation per
+    // attempt whichever way the lanes of a warp go)
+    const double cr = cm_pow(err, 1.0 / 3.0);
+    if (err > 1.0) {
+      c.absh = 0.8 * c.absh / cr;
+      c.n_rej++;
+      if (c.absh < hmin) {
+        c.idid = 4;
+      } else {
+        c.newspc = !c.jacatt;
+        if (++rej_run >= RKCLOW_LOOP_CAP) {
+          c.status |= ST_LOOP_CAP;
+          return ATT_FAIL;
+        }
+        return ATT_REJECT;
+      }
+    }
+    rej_run = 0;
+    c.naccpt += 1;
+    c.lt += h;
+    c.gt = c.lt;
+    c.jacatt = 0;
+    c.newspc = 0;  // nstsig never advances (solve_rkc.cu:1024-1026)
+    c.hw0 = h;
+    c.hw1 = c.lt;
+    {
+      const int tmp = c.map[LV2];
+      c.map[LV2] = c.map[LFN];
+      c.map[LFN] = c.map[LV1];
+      c.map[LV1] = c.map[LYN];
+      c.map[LYN] = c.map[LY];
+      c.map[LY] = tmp;
+    }
+    // err^(2/3) as the square of err^(1/3); errold^(1/3) carried over
+    double fac = 10.0, temp1, temp2;
+    if (c.naccpt == 1) {
+      temp2 = cr;
+      if (0.8 < fac * temp2) fac = 0.8 / temp2;
+    } else {
+      temp1 = 0.8 * c.absh * c.cbrt_errold;
+      temp2 = fabs(c.hold) * (cr * cr);
+      if (temp1 < fac * temp2) fac = temp1 / temp2;
+    }
+    c.cbrt_errold = cr;
+    c.absh = ((0.1 > fac) ? 0.1 : fac) * c.absh;
+    {
+      const double mn = fmin(hmax, c.absh);
+      c.absh = (hmin > mn) ? hmin : mn;
+    }
+    c.errold = err;
+    c.hold = h;
+    c.idid = c.last ? 1 : 2;
+    tm.sync();
+    return ATT_ACCEPT;
   }
 
   // ------------------------------------------ ion update + current vector b
   __device__ __forceinline__ void ion_and_b(double sum_dt, bool update_ion, bool with_gap = true) {
-    const double *vy = vec(LY);
-    double *b = bvec();
+    const V vy = vec(LY);
+    const V b = bvec();
     const Slots<R> sl0{P.ion, P.cond, P.stride, 0};
     for (int i = tm.rank(); i < nc; i += tm.size()) {
       const long gi = off + i;
@@ -399,7 +544,7 @@ struct Sys {
   // ----------------------------------------------------- initialisation
   // RKC_vec_initialize: b from the initial V, vectors, rho, first step
   __device__ __forceinline__ void initialize() {
-    double *y = vec(LY), *yn = vec(LYN), *fn = vec(LFN), *v1 = vec(LV1), *v2 = vec(LV2);
+    V y = vec(LY), yn = vec(LYN), fn = vec(LFN), v1 = vec(LV1), v2 = vec(LV2);
     double *ede = P.ede + off;
     for (int i = tm.rank(); i < nc; i += tm.size()) {
       const double v0 = P.v[off + i];
@@ -426,7 +571,7 @@ struct Sys {
     absh = (absh > c.hmin) ? absh : c.hmin;
     for (int i = tm.rank(); i < nc; i += tm.size()) v1[i] = fma(absh, fn[i], yn[i]);
     tm.sync();
-    double *sc = scratch();
+    V sc = scratch();
     int bad = 0;
     for (int i = tm.rank(); i < nc; i += tm.size()) {
       const double f = rhs(v1, i);
@@ -452,9 +597,11 @@ struct Sys {
     }
   }
 
-  // ---------------------------------------------------- one output interval
-  // *_set_current at t, then *_solve_by_rkc (solve_rkc.cu:1122-1362)
-  __device__ __forceinline__ bool interval(double t) {
+  // ------------------------------------------------------- flat driver
+  // *_set_current at t, then the start of *_solve_by_rkc
+  // (solve_rkc.cu:1122-1150); TICK_ION if the ion update left pending by
+  // the previous interval is due before the first attempt.
+  __device__ __forceinline__ int begin_interval(double t) {
     if (P.stim_on) {
       for (int cc = tm.rank(); cc < ncell; cc += tm.size()) {
         const int pc = cell0 + cc;
@@ -467,86 +614,180 @@ struct Sys {
       }
       tm.sync();
     }
-    const bool ge = (CT == GO || CT == PKJ);
-    if (c.sum_dt != 0.0) {
-      ion_and_b(c.sum_dt, true);
-      c.sum_dt = 0.0;
-    }
-    const long attempts0 = c.n_steps;
-    for (;;) {
-      rkclow();
-      if (c.status) return false;
-      if (c.n_steps - attempts0 > STEPS_PER_INTERVAL_CAP) {
-        c.status |= ST_LOOP_CAP;
-        return false;
-      }
-      c.sum_dt += c.gt - c.gt_old;
-      c.gt_old = c.gt;
-      const bool trig = ge ? (c.sum_dt >= c.integ) : (c.sum_dt > c.integ);
-      if (trig && c.idid == 2.0) {
-        ion_and_b(c.sum_dt, true);
-        c.sum_dt = 0.0;
-      }
-      if (c.idid == 2.0) {
-        continue;
-      } else if (c.idid == 1.0) {
-        break;
-      } else {
-        c.status |= ST_IDID;
-        return false;
-      }
-    }
-    // rkcint
-    {
-      const double hlast = c.hw0, tlast = c.hw1 - hlast;
-      const double sv = (c.gt_old - tlast) / hlast;
-      const double a1 = (1.0 + 2.0 * sv) * (sv - 1.0) * (sv - 1.0);
-      const double a2 = (3.0 - 2.0 * sv) * sv * sv;
-      const double b1 = hlast * sv * (sv - 1.0) * (sv - 1.0);
-      const double b2 = hlast * (sv - 1.0) * sv * sv;
-      const double *v1 = vec(LV1), *v2 = vec(LV2), *yn = vec(LYN), *fn = vec(LFN);
-      for (int i = tm.rank(); i < nc; i += tm.size())
-        P.vnew[off + i] = fma(b2, fn[i], fma(b1, v2[i], fma(a2, yn[i], a1 * v1[i])));
-    }
+    attempts0 = c.n_steps;
+    rej_run = 0;
+    return (c.sum_dt != 0.0) ? TICK_ION : TICK_MORE;
+  }
+
+  // the ion update and new current vector a TICK_ION asked for
+  __device__ __forceinline__ void ion_due() {
+    ion_and_b(c.sum_dt, true);
+    c.sum_dt = 0.0;
+  }
+
+  // rkcint at the interval's end (solve_rkc.cu:795-813) and the soma record
+  __device__ __forceinline__ void end_interval() {
+    const double hlast = c.hw0, tlast = c.hw1 - hlast;
+    const double sv = (c.gt_old - tlast) / hlast;
+    const double a1 = (1.0 + 2.0 * sv) * (sv - 1.0) * (sv - 1.0);
+    const double a2 = (3.0 - 2.0 * sv) * sv * sv;
+    const double b1 = hlast * sv * (sv - 1.0) * (sv - 1.0);
+    const double b2 = hlast * (sv - 1.0) * sv * sv;
+    const V v1 = vec(LV1), v2 = vec(LV2), yn = vec(LYN), fn = vec(LFN);
+    for (int i = tm.rank(); i < nc; i += tm.size())
+      P.vnew[off + i] = fma(b2, fn[i], fma(b1, v2[i], fma(a2, yn[i], a1 * v1[i])));
     c.tend += H_MAX;
     tm.sync();
-    return true;
+    if (P.soma_out) {
+      for (int cc = tm.rank(); cc < ncell; cc += tm.size()) {
+        const int pc = cell0 + cc;
+        P.soma_out[(long)(iv0 + k_iv) * P.ncell_pool + pc] = P.vnew[P.cell_soma[pc]];
+      }
+    }
+  }
+
+  // Start advancing by n intervals from t: TICK_DONE if there is nothing to
+  // do, else what begin_interval returns.
+  __device__ __forceinline__ int start(double t, int n, int iv0_global) {
+    t0 = t;
+    n_iv = n;
+    iv0 = iv0_global;
+    k_iv = 0;
+    if (c.status != 0 || n <= 0) return TICK_DONE;
+    return begin_interval(t0);
+  }
+
+  // One step attempt and what follows it (the loop of *_solve_by_rkc,
+  // solve_rkc.cu:1150-1362): TICK_MORE (attempt again), TICK_ION (run
+  // ion_due() first) or TICK_DONE (intervals finished, or c.status set).
+  __device__ __forceinline__ int tick() {
+    const int a = attempt();
+    if (a == ATT_REJECT) return TICK_MORE;
+    if (a == ATT_FAIL) return TICK_DONE;
+    if (c.n_steps - attempts0 > STEPS_PER_INTERVAL_CAP) {
+      c.status |= ST_LOOP_CAP;
+      return TICK_DONE;
+    }
+    c.sum_dt += c.gt - c.gt_old;
+    c.gt_old = c.gt;
+    const bool ge = (CT == GO || CT == PKJ);
+    const bool trig = ge ? (c.sum_dt >= c.integ) : (c.sum_dt > c.integ);
+    if (c.idid == 2.0) return trig ? TICK_ION : TICK_MORE;
+    if (c.idid != 1.0) {
+      c.status |= ST_IDID;
+      return TICK_DONE;
+    }
+    end_interval();
+    if (++k_iv >= n_iv) return TICK_DONE;
+    return begin_interval(t0 + k_iv * H_MAX);
   }
 };
 
-// Stage a system's workspace between HBM and shared memory.
+// Stage a system's workspace between HBM (contiguous) and shared memory
+// (element stride LS).
 template <class Team>
-__device__ void ws_copy(const Team &tm, double *dst, const double *src, long n) {
-  for (long i = tm.rank(); i < n; i += tm.size()) dst[i] = src[i];
+__device__ __forceinline__ void ws_in(const Team &tm, double *dst, const double *src, long n) {
+  for (long i = tm.rank(); i < n; i += tm.size()) dst[i * Team::LS] = src[i];
+  tm.sync();
+}
+template <class Team>
+__device__ __forceinline__ void ws_out(const Team &tm, double *dst, const double *src, long n) {
+  for (long i = tm.rank(); i < n; i += tm.size()) dst[i] = src[i * Team::LS];
   tm.sync();
 }
 
 // Advance one system by n_iv intervals starting at t0 (or initialise it).
 template <int CT, typename R, class Team>
 __device__ __forceinline__ void run_system(const PoolView<R> &P, const Team &tm, int s, double *smem_ws, double t0,
-                           int n_iv, int iv0_global, bool init) {
+                                           int n_iv, int iv0_global, bool init) {
   const long wsn = (long)WS_VECS * (long)((P.sys_nc[s] + 1) & ~1);
   double *gws = P.ws + P.sys_ws[s];
   double *W = P.ws_in_smem ? smem_ws : gws;
-  if (P.ws_in_smem) ws_copy(tm, W, gws, wsn);
+  if (P.ws_in_smem) ws_in(tm, W, gws, wsn);
   Sys<CT, R, Team> S(P, tm, s, W);
   S.c = P.ctl[s];
   if (init) {
     S.initialize();
-  } else if (S.c.status == 0) {
-    for (int k = 0; k < n_iv; k++) {
-      if (!S.interval(t0 + k * H_MAX)) break;
-      if (P.soma_out) {
-        for (int cc = tm.rank(); cc < S.ncell; cc += tm.size()) {
-          const int pc = S.cell0 + cc;
-          P.soma_out[(long)(iv0_global + k) * P.ncell_pool + pc] = P.vnew[P.cell_soma[pc]];
-        }
+  } else {
+    int r = S.start(t0, n_iv, iv0_global);
+    while (r != TICK_DONE) {
+      if (r == TICK_ION) {
+        S.ion_due();
+        r = TICK_MORE;
+      } else {
+        r = S.tick();
       }
     }
   }
   tm.sync();
-  if (P.ws_in_smem) ws_copy(tm, gws, W, wsn);
+  if (P.ws_in_smem) ws_out(tm, gws, W, wsn);
   if (tm.rank() == 0) P.ctl[s] = S.c;
+}
+
+// Single-lane systems: every thread of the first `lanes` threads of the block
+// integrates its own systems, taken from *q (or, with q null, the static
+// sequence first, first + stride, ...).  A lane whose system has finished
+// writes it back and takes the next one at once, so the warp keeps 32
+// systems in flight until the queue runs dry.  A lane whose ion update is due
+// parks; the warp runs the parked lanes' updates together once every live
+// lane is parked or the oldest has waited ION_WAIT_MAX iterations.  Parking
+// only delays a system; its own sequence of operations is unchanged.
+// Workspaces always sit in shared memory, interleaved (Team::LS = BLOCK).
+template <int CT, typename R, int BLOCK, int NCF = 0>
+__device__ __forceinline__ void run_lanes(const PoolView<R> &P, int *q, int first, int stride, double *smem,
+                                          double t0, int n_iv, int iv0_global, bool init) {
+  typedef LaneTeam<BLOCK, NCF> Team;
+  Team tm;
+  double *W = smem + threadIdx.x;
+  Sys<CT, R, Team> S(P, tm);
+  int s = q ? atomicAdd(q, 1) : first;
+  int r = TICK_DONE;
+  // take systems until one needs stepping (or the queue is empty)
+  auto acquire = [&]() {
+    while (s < P.nsys) {
+      S.bind(s, W);
+      S.c = P.ctl[s];
+      if (init) {
+        ws_in(tm, W, P.ws + P.sys_ws[s], (long)WS_VECS * S.ncp);
+        S.initialize();
+        ws_out(tm, P.ws + P.sys_ws[s], W, (long)WS_VECS * S.ncp);
+        P.ctl[s] = S.c;
+      } else if (S.c.status == 0 && n_iv > 0) {
+        ws_in(tm, W, P.ws + P.sys_ws[s], (long)WS_VECS * S.ncp);
+        r = S.start(t0, n_iv, iv0_global);
+        if (r != TICK_DONE) return;
+        ws_out(tm, P.ws + P.sys_ws[s], W, (long)WS_VECS * S.ncp);
+        P.ctl[s] = S.c;
+      }
+      s = q ? atomicAdd(q, 1) : s + stride;
+    }
+    r = TICK_DONE;
+  };
+  acquire();
+  int wait = 0;
+  for (;;) {
+    __syncwarp();
+    const unsigned live = __ballot_sync(0xffffffffu, r != TICK_DONE);
+    if (!live) break;
+    const unsigned parked = __ballot_sync(0xffffffffu, r == TICK_ION);
+    if (parked && (parked == live || ++wait > ION_WAIT_MAX)) {
+      wait = 0;
+      if (r == TICK_ION) {
+        S.ion_due();
+        r = TICK_MORE;
+      }
+      __syncwarp();
+    }
+    if (r == TICK_MORE) {
+      r = S.tick();
+      if (r == TICK_DONE) {
+        ws_out(tm, P.ws + P.sys_ws[s], W, (long)WS_VECS * S.ncp);
+        P.ctl[s] = S.c;
+        s = q ? atomicAdd(q, 1) : s + stride;
+        acquire();
+      }
+    }
+  }
 }
 
 }  // namespace gbrkc

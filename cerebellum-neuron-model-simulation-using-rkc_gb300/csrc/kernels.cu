@@ -1,7 +1,9 @@
-// The advance kernel: one launch advances every system of a pool by n_iv
-// output intervals (or initialises them), entirely on the device.  Teams of
-// 4 or 32 lanes take many small systems per block; a whole block takes one
-// large system at a time and loops over its share of systems (persistent).
+// The advance kernels.  k_advance: one launch advances every system of one
+// pool by n_iv output intervals (or initialises them), entirely on the
+// device.  Single lanes take the tiniest systems (one system per thread),
+// teams of 4 or 32 lanes small ones; a whole block takes one large system at
+// a time and loops over its share of systems.  k_mega: one persistent launch
+// for all pools, every CTA a role pulling systems from its role's queue.
 //
 // Built with -fmad=false (see integrator.cuh).  R selects FP64 or FP32
 // gating; the instantiations live in kernels_fp64.cu / kernels_fp32.cu.
@@ -15,7 +17,13 @@ template <int CT, typename R, int TS>
 __global__ void __launch_bounds__(256, 1) k_advance(const __grid_constant__ PoolView<R> P, double t0, int n_iv,
                                                  int iv0, int init) {
   extern __shared__ __align__(16) double smem[];
-  if (TS == TEAM_BLOCK) {
+  if (TS == TEAM_THREAD || TS == TEAM_LANE4) {
+    // warp w of block b starts at system 32 (w * grid + b) + lane: the first
+    // warps of every block are filled before any block's later warps
+    const int first = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * 32 + ((int)threadIdx.x & 31);
+    run_lanes<CT, R, MEGA_BLOCK, TS == TEAM_LANE4 ? 4 : 0>(P, nullptr, first, gridDim.x * MEGA_BLOCK, smem, t0, n_iv,
+                                                           iv0, init != 0);
+  } else if (TS == TEAM_BLOCK) {
     BlockTeam tm;
     for (int s = blockIdx.x; s < P.nsys; s += gridDim.x) {
       run_system<CT, R, BlockTeam>(P, tm, s, smem, t0, n_iv, iv0, init != 0);
@@ -27,17 +35,104 @@ __global__ void __launch_bounds__(256, 1) k_advance(const __grid_constant__ Pool
     TileTeam<TS> tm;
     tm.r = threadIdx.x % T;
     tm.mask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << ((threadIdx.x & 31) / T * T));
-    // thread teams need no warp-level synchronisation at all
-    if (T == 1) tm.mask = 1u << (threadIdx.x & 31);
     double *my = smem + (long)tile * P.ws_tile_doubles;
     for (int s = blockIdx.x * tiles + tile; s < P.nsys; s += gridDim.x * tiles)
       run_system<CT, R, TileTeam<TS>>(P, tm, s, my, t0, n_iv, iv0, init != 0);
   }
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// a role of tile teams: every tile repeatedly takes the next system
+template <int CT, typename R, int TS>
+__device__ __forceinline__ void role_tiles(const PoolView<R> &P, int *q, double *smem, double t0, int n_iv,
+                                           int iv0, int init) {
+  const int tile = threadIdx.x / TS;
+  TileTeam<TS> tm;
+  tm.r = threadIdx.x % TS;
+  tm.mask = (TS == 32) ? 0xffffffffu : (((1u << TS) - 1u) << ((threadIdx.x & 31) / TS * TS));
+  double *my = smem + (long)tile * P.ws_tile_doubles;
+  for (;;) {
+    int s = 0;
+    if (tm.r == 0) s = atomicAdd(q, 1);
+    s = __shfl_sync(tm.mask, s, 0, TS);
+    if (s >= P.nsys) break;
+    run_system<CT, R, TileTeam<TS>>(P, tm, s, my, t0, n_iv, iv0, init != 0);
+  }
+}
+
+// a role of whole blocks: the block takes the next system
+template <int CT, typename R>
+__device__ __forceinline__ void role_block(const PoolView<R> &P, int *q, double *smem, double t0, int n_iv,
+                                           int iv0, int init) {
+  __shared__ int s_next;
+  BlockTeam tm;
+  for (;;) {
+    if (threadIdx.x == 0) s_next = atomicAdd(q, 1);
+    __syncthreads();
+    const int s = s_next;
+    __syncthreads();
+    if (s >= P.nsys) break;
+    run_system<CT, R, BlockTeam>(P, tm, s, smem, t0, n_iv, iv0, init != 0);
+    __syncthreads();
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(MEGA_BLOCK, 1) k_mega(const __grid_constant__ MegaView<R> M, double t0,
+                                                         int n_iv, int iv0, int init) {
+  extern __shared__ __align__(16) double smem[];
+  if (threadIdx.x == 0) M.t_start[blockIdx.x] = global_ns();
+  int role = 0;
+  while (role < NTYPES - 1 && (int)blockIdx.x >= M.role_end[role]) role++;
+  switch (role) {
+    case GR:
+      // single-lane granule systems on the first lane_warps warps of the CTA
+      if ((int)(threadIdx.x >> 5) < M.lane_warps) {
+        if (M.gr_nc4)
+          run_lanes<GR, R, MEGA_BLOCK, 4>(M.pool[GR], M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
+        else
+          run_lanes<GR, R, MEGA_BLOCK>(M.pool[GR], M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
+      }
+      break;
+    case GO: role_tiles<GO, R, TEAM_WARP>(M.pool[GO], M.queue + GO, smem, t0, n_iv, iv0, init); break;
+    case PKJ: role_block<PKJ, R>(M.pool[PKJ], M.queue + PKJ, smem, t0, n_iv, iv0, init); break;
+    default: role_block<IO, R>(M.pool[IO], M.queue + IO, smem, t0, n_iv, iv0, init); break;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) M.t_end[blockIdx.x] = global_ns();
+}
+
+template <typename R>
+int prepare_mega_kernel(size_t smem, int *blocks_per_sm) {
+  const void *k = (const void *)k_mega<R>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, MEGA_BLOCK, smem);
+  return (int)e;
+}
+
+template <typename R>
+int launch_mega(const MegaView<R> &M, int grid, size_t smem, void *stream, double t0, int n_iv, int iv0,
+                int init) {
+  MegaView<R> Mc = M;
+  void *args[] = {(void *)&Mc, (void *)&t0, (void *)&n_iv, (void *)&iv0, (void *)&init};
+  cudaError_t e = cudaLaunchKernel((const void *)k_mega<R>, dim3(grid), dim3(MEGA_BLOCK), args, smem,
+                                   (cudaStream_t)stream);
+  return (int)e;
+}
+
 template <int CT, typename R>
 static const void *kernel_for(int team) {
   switch (team) {
+    case TEAM_LANE4:
+      // instantiated for granule pools only (the others never have it)
+      if constexpr (CT == GR) return (const void *)k_advance<CT, R, TEAM_LANE4>;
+      return (const void *)k_advance<CT, R, TEAM_THREAD>;
     case TEAM_THREAD: return (const void *)k_advance<CT, R, TEAM_THREAD>;
     case TEAM_TILE4: return (const void *)k_advance<CT, R, TEAM_TILE4>;
     case TEAM_WARP: return (const void *)k_advance<CT, R, TEAM_WARP>;

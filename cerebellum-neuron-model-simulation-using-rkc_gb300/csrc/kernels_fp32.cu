@@ -4,4 +4,6 @@
 namespace gbrkc {
 template int launch_pool<float>(int, const PoolView<float> &, int, int, int, size_t, void *, double, int, int, int);
 template int prepare_pool_kernel<float>(int, int, size_t);
+template int launch_mega<float>(const MegaView<float> &, int, size_t, void *, double, int, int, int);
+template int prepare_mega_kernel<float>(size_t, int *);
 }  // namespace gbrkc

@@ -336,6 +336,124 @@ __device__ bool small_solve(R (&A)[N][N], R (&b)[N]) {
   return true;
 }
 
+// Register-resident elimination for the channels' Crank-Nicolson systems.
+//
+// Both kinetic matrices (GR Na, 12 states; GoC KAHP, 6 states) are
+// -(Q + (2/DT) I), Q a rate generator (non-negative off-diagonals, each column
+// summing to zero): every column's diagonal exceeds the sum of its
+// off-diagonal magnitudes by 2/DT >= 16.  Gaussian elimination preserves
+// strict column diagonal dominance, so the partial pivoting of the reference
+// (gr_ion.cu:141-190, go_ion.cu:152-200) always keeps the diagonal; rounding
+// (relative 1e-7) cannot close a margin that large.  dd_solve therefore runs
+// the same elimination without row swaps, fully unrolled over the compile-time
+// fill-in pattern of the matrix so it stays in registers.  It still checks
+// every pivot and returns DD_PIVOT if a swap would have been taken (the
+// caller then reruns the dense pivoting solver): results are the dense
+// solver's in every case.  Entries outside the pattern are exactly zero; the
+// dense solver's updates with them leave every value unchanged (up to the
+// sign of a zero), so they are skipped.
+enum { DD_OK = 0, DD_SINGULAR = 1, DD_PIVOT = 2 };
+
+template <int N>
+struct Fill {
+  uint32_t r[N];  // bit k of r[i]: entry (i, k) may be nonzero
+};
+
+template <int N>
+constexpr Fill<N> fill_in(const uint32_t (&rows)[N]) {
+  Fill<N> f{};
+  for (int i = 0; i < N; i++) f.r[i] = rows[i] | (1u << i);
+  for (int i = 0; i < N - 1; i++)
+    for (int j = i + 1; j < N; j++)
+      if ((f.r[j] >> i) & 1u) f.r[j] |= f.r[i] & ~((2u << i) - 1u);
+  return f;
+}
+
+template <int N>
+constexpr Fill<N> as_fill(const uint32_t (&rows)[N]) {
+  Fill<N> f{};
+  for (int i = 0; i < N; i++) f.r[i] = rows[i];
+  return f;
+}
+
+#define GB_ROW(...) gb_bits({__VA_ARGS__})
+template <int K>
+constexpr uint32_t gb_bits(const int (&cols)[K]) {
+  uint32_t m = 0;
+  for (int k = 0; k < K; k++) m |= 1u << cols[k];
+  return m;
+}
+
+// nonzero pattern of the GR Na matrix (gr_na_fill)
+struct NaPattern {
+  static constexpr int N = 12;
+  static constexpr uint32_t rows[12] = {
+      GB_ROW(0, 1, 5),      GB_ROW(0, 1, 2, 6),   GB_ROW(1, 2, 3, 7),   GB_ROW(2, 3, 4, 8),
+      GB_ROW(3, 4, 9, 11),  GB_ROW(0, 5, 6),      GB_ROW(1, 5, 6, 7),   GB_ROW(2, 6, 7, 8),
+      GB_ROW(3, 7, 8, 9),   GB_ROW(4, 8, 9, 10),  GB_ROW(9, 10, 11),    GB_ROW(4, 10, 11)};
+  static constexpr Fill<12> fill = fill_in<12>(rows);
+  static constexpr Fill<12> orig = as_fill<12>(rows);
+};
+
+// nonzero pattern of the GoC KAHP matrix (Go::kahp)
+struct KahpPattern {
+  static constexpr int N = 6;
+  static constexpr uint32_t rows[6] = {GB_ROW(0, 1),       GB_ROW(0, 1, 2),    GB_ROW(1, 2, 3, 4),
+                                       GB_ROW(2, 3, 5),    GB_ROW(2, 4),       GB_ROW(3, 5)};
+  static constexpr Fill<6> fill = fill_in<6>(rows);
+  static constexpr Fill<6> orig = as_fill<6>(rows);
+};
+#undef GB_ROW
+
+template <typename R, class PAT>
+__device__ __forceinline__ int dd_solve(R (&A)[PAT::N][PAT::N], R (&b)[PAT::N]) {
+  constexpr int N = PAT::N;
+  constexpr Fill<N> F = PAT::fill;
+#pragma unroll
+  for (int i = 0; i < N - 1; i++) {
+    const R d = mabs(A[i][i]);
+#pragma unroll
+    for (int j = i + 1; j < N; j++)
+      if ((F.r[j] >> i) & 1u)
+        if (mabs(A[j][i]) > d) return DD_PIVOT;
+    if (d < R(1.0e-12)) return DD_SINGULAR;
+#pragma unroll
+    for (int j = i + 1; j < N; j++) {
+      if (!((F.r[j] >> i) & 1u)) continue;
+      if (A[j][i] == R(0.0)) continue;
+      const R w = A[j][i] / A[i][i];
+      A[j][i] = R(0.0);
+#pragma unroll
+      for (int k = i + 1; k < N; k++)
+        if ((F.r[i] >> k) & 1u) A[j][k] = A[j][k] - A[i][k] * w;
+      b[j] = b[j] - b[i] * w;
+    }
+  }
+#pragma unroll
+  for (int i = N - 1; i >= 0; i--) {
+#pragma unroll
+    for (int j = i + 1; j < N; j++)
+      if ((F.r[i] >> j) & 1u) b[i] = b[i] - A[i][j] * b[j];
+    b[i] = b[i] / A[i][i];
+  }
+  return DD_OK;
+}
+
+// rhs = -M x over the pattern (the dense product's zero terms change nothing)
+template <typename R, class PAT>
+__device__ __forceinline__ void dd_neg_matvec(const R (&M)[PAT::N][PAT::N], const R (&x)[PAT::N], R (&y)[PAT::N]) {
+  constexpr int N = PAT::N;
+  constexpr Fill<N> O = PAT::orig;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    R acc = R(0.0);
+#pragma unroll
+    for (int j = 0; j < N; j++)
+      if ((O.r[i] >> j) & 1u) acc -= x[j] * M[i][j];
+    y[i] = acc;
+  }
+}
+
 // GR 12-state Na channel, Crank-Nicolson step (gr_ion.cu:45-207).  The
 // per-compartment-type constants a = (Oon/Con)^0.25, b = (Ooff/Coff)^0.25,
 // a^4, b^4 come precomputed from the host (NaPar).
@@ -395,21 +513,29 @@ __device__ void gr_na(const Slots<R> &s, const NaPar &p, double v_new, double v_
   const int slot[12] = {GR_c1, GR_c2, GR_c3, GR_c4, GR_c5, GR_i1, GR_i2, GR_i3, GR_i4, GR_i5, GR_i6, GR_o_Na};
   const R vs = (R)p.vshift, tdt = R(2.0) / (R)DT;
   R M[12][12], vc[12], vcb[12];
-  R vo = (R)v_old, vn = (R)v_new;
-  R alpha = (R)p.Aa * mexp((vo - vs) / R(10.0));
-  R beta = (R)p.Ab * mexp(-(vo - vs) / R(10.0));
-  gr_na_fill(M, p, alpha, beta, tdt, false);
+  const R vo = (R)v_old, vn = (R)v_new;
+  const R alpha0 = (R)p.Aa * mexp((vo - vs) / R(10.0));
+  const R beta0 = (R)p.Ab * mexp(-(vo - vs) / R(10.0));
+  gr_na_fill(M, p, alpha0, beta0, tdt, false);
 #pragma unroll
   for (int k = 0; k < 12; k++) vc[k] = s.x(slot[k]);
-  for (int i = 0; i < 12; i++) {
-    R acc = R(0.0);
-    for (int j = 0; j < 12; j++) acc -= vc[j] * M[i][j];
-    vcb[i] = acc;
-  }
-  alpha = (R)p.Aa * mexp((vn - vs) / R(10.0));
-  beta = (R)p.Ab * mexp(-(vn - vs) / R(10.0));
+  dd_neg_matvec<R, NaPattern>(M, vc, vcb);
+  const R alpha = (R)p.Aa * mexp((vn - vs) / R(10.0));
+  const R beta = (R)p.Ab * mexp(-(vn - vs) / R(10.0));
   gr_na_fill(M, p, alpha, beta, tdt, true);
-  if (!small_solve<R, 12>(M, vcb)) return;
+  const int rc = dd_solve<R, NaPattern>(M, vcb);
+  if (rc == DD_SINGULAR) return;
+  if (rc == DD_PIVOT) {
+    // never reached for these matrices (see dd_solve); the dense pivoting
+    // elimination on a fresh copy keeps the result exact regardless
+    R A[12][12], rb[12];
+    gr_na_fill(A, p, alpha0, beta0, tdt, false);
+    dd_neg_matvec<R, NaPattern>(A, vc, rb);
+    gr_na_fill(A, p, alpha, beta, tdt, true);
+    if (!small_solve<R, 12>(A, rb)) return;
+#pragma unroll
+    for (int k = 0; k < 12; k++) vcb[k] = rb[k];
+  }
 #pragma unroll
   for (int k = 0; k < 12; k++) s.x(slot[k]) = vcb[k];
 }
@@ -541,11 +667,7 @@ template <typename R> struct Go {
                  {R(0), R(0), d3, -(i3 + b2) + l_dt, R(0), a2},
                  {R(0), R(0), b1, R(0), -a1 + l_dt, R(0)},
                  {R(0), R(0), R(0), b2, R(0), -a2 + l_dt}};
-    for (int i = 0; i < 6; i++) {
-      R acc = R(0.0);
-      for (int j = 0; j < 6; j++) acc -= vc[j] * E[i][j];
-      vcb[i] = acc;
-    }
+    dd_neg_matvec<R, KahpPattern>(E, vc, vcb);
     l_ca = (R)ca_new;
     d1 = R(200) * l_ca / R(3.0); d2 = R(160) * l_ca / R(3.0); d3 = R(80) * l_ca / R(3.0);
     R M[6][6] = {{-d1 - l_dt, i1, R(0), R(0), R(0), R(0)},
@@ -554,7 +676,22 @@ template <typename R> struct Go {
                  {R(0), R(0), d3, -(i3 + b2) - l_dt, R(0), a2},
                  {R(0), R(0), b1, R(0), -a1 - l_dt, R(0)},
                  {R(0), R(0), R(0), b2, R(0), -a2 - l_dt}};
-    if (!small_solve<R, 6>(M, vcb)) return;
+    const int rc = dd_solve<R, KahpPattern>(M, vcb);
+    if (rc == DD_SINGULAR) return;
+    if (rc == DD_PIVOT) {
+      // never reached (see dd_solve); the dense pivoting solver on a fresh copy
+      R A[6][6] = {{-d1 - l_dt, i1, R(0), R(0), R(0), R(0)},
+                   {d1, -d2 - i1 - l_dt, i2, R(0), R(0), R(0)},
+                   {R(0), d2, -(d3 + i2 + b1) - l_dt, i3, a1, R(0)},
+                   {R(0), R(0), d3, -(i3 + b2) - l_dt, R(0), a2},
+                   {R(0), R(0), b1, R(0), -a1 - l_dt, R(0)},
+                   {R(0), R(0), R(0), b2, R(0), -a2 - l_dt}};
+      R rb[6];
+      dd_neg_matvec<R, KahpPattern>(E, vc, rb);
+      if (!small_solve<R, 6>(A, rb)) return;
+#pragma unroll
+      for (int k = 0; k < 6; k++) vcb[k] = rb[k];
+    }
 #pragma unroll
     for (int k = 0; k < 6; k++) s.x(slot[k]) = vcb[k];
   }

@@ -69,6 +69,7 @@ def lib() -> C.CDLL:
         L.gbrkc_read_soma_type.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.gbrkc_rewind_soma.argtypes = [P]
         L.gbrkc_retired_systems.argtypes = [P]
+        L.gbrkc_launch_layout.argtypes = [P, C.POINTER(C.c_int)]
         L.gbrkc_compartment_updates.argtypes = [P, C.c_int]
         L.gbrkc_compartment_updates.restype = C.c_longlong
         _LIB = L
@@ -156,6 +157,14 @@ class Engine:
         if rc == -5 and tolerate_retire:
             return
         _check(rc)
+
+    def launch_layout(self):
+        """(persistent?, CTAs per cell type) of the advance launch."""
+        c = (C.c_int * 4)()
+        rc = lib().gbrkc_launch_layout(self.h, c)
+        if rc < 0:
+            _check(rc)
+        return bool(rc), list(c)
 
     def retired(self) -> int:
         return lib().gbrkc_retired_systems(self.h)

@@ -121,6 +121,11 @@ int gbrkc_rewind_soma(gbrkc_engine *e);
 float gbrkc_last_advance_ms(gbrkc_engine *e);
 float gbrkc_last_kernel_ms(gbrkc_engine *e, int cell_type);
 
+/* Launch layout: returns 1 when all cell types advance in one persistent
+ * launch (CTAs per type written to ctas_per_type[4]), 0 when each type has
+ * its own launch (entries -1), negative on error. */
+int gbrkc_launch_layout(gbrkc_engine *e, int *ctas_per_type);
+
 /* Compartment updates so far (sum over systems of (stage evaluations + step
  * attempts) x compartments; power iterations excluded), for one cell type
  * or, with cell_type = -1, all.  Negative on error. */

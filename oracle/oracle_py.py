@@ -66,6 +66,7 @@ def lib() -> C.CDLL:
             getattr(L, f).argtypes = [P]
         L.orc_ctl.argtypes = [P, C.POINTER(C.c_double)]
         L.orc_stats.argtypes = [P, C.POINTER(C.c_longlong)]
+        L.orc_pivot_swaps.restype = C.c_longlong
         L.orc_ion_update.argtypes = [P, C.POINTER(C.c_double), C.c_double]
         L.orc_update_b.argtypes = [P, C.POINTER(C.c_double)]
         L.orc_set_elem_v.argtypes = [P, C.POINTER(C.c_double)]
@@ -89,6 +90,11 @@ def draw_jitter(cell_type: int, n: int) -> np.ndarray:
     out = np.zeros(n, dtype=np.float64)
     lib().orc_draw_jitter(cell_type, n, _dp(out))
     return out
+
+
+def pivot_swaps() -> int:
+    """Row swaps taken by the Na / KAHP Markov solvers in this process."""
+    return int(lib().orc_pivot_swaps())
 
 
 def libc_srand(seed: int) -> None:

@@ -400,6 +400,12 @@ static double go_hs2_tau(double v) { return (EXP((0.015 * v + 5.3) * 2.3)); }
 /* gr_ion.cu:141-190 and go_ion.cu:152-200.  Returns 0 on a "pivot     */
 /* error" (the reference returns early and leaves the state).          */
 /* ------------------------------------------------------------------ */
+/* Row swaps taken over the process's lifetime: the kinetic matrices are
+ * strictly column diagonally dominant, so this stays zero (the CUDA path
+ * relies on it and the tests check it). */
+static long long g_pivot_swaps = 0;
+long long orc_pivot_swaps(void) { return g_pivot_swaps; }
+
 static int pivot_solve(int n, double *A /* n*n row-major */, double *bvec) {
   for (int i = 0; i < n - 1; i++) {
     int piv = i;
@@ -408,6 +414,7 @@ static int pivot_solve(int n, double *A /* n*n row-major */, double *bvec) {
       if (fabs(A[j * n + i]) > pmax) { piv = j; pmax = fabs(A[j * n + i]); }
     if (fabs(pmax) < 1.0e-12) return 0;
     if (piv != i) {
+      g_pivot_swaps++;
       for (int j = i; j < n; j++) {
         double t = A[i * n + j]; A[i * n + j] = A[piv * n + j]; A[piv * n + j] = t;
       }

@@ -76,6 +76,8 @@ void orc_ctl(const orc_sys *s, double *out8);
 /* counters: steps, rejects, stage evals (sum of m), rho calls, ion updates,
  * power-iteration RHS evaluations */
 void orc_stats(const orc_sys *s, long long *out6);
+/* Row swaps taken by the Na / KAHP Markov solvers so far (process-wide). */
+long long orc_pivot_swaps(void);
 
 /* static setup, for the setup pins: Cm, area, cond k, shell, CSR */
 const double *orc_cm(const orc_sys *s);

@@ -99,3 +99,35 @@ def test_soma_recording(oracle):
         s.advance(t)
         t += G.H_MAX
         np.testing.assert_array_equal(rec[k], s.vnew()[1::3])
+
+
+@pytest.mark.parametrize("precision", [G.FP64, G.MIXED])
+def test_persistent_equals_per_type(monkeypatch, precision):
+    """The one persistent launch (every CTA a cell-type role pulling systems
+    from a queue, with the role split re-tuned after every launch) gives the
+    same bits as one launch per cell type."""
+    import configs
+    specs = configs.scaled_mixed_batch(1.0 / 64)
+    out = {}
+    for mode in ("persistent", "per_type"):
+        if mode == "per_type":
+            monkeypatch.setenv("GBRKC_NO_MEGA", "1")
+        else:
+            monkeypatch.delenv("GBRKC_NO_MEGA", raising=False)
+        eng = G.Engine(precision)
+        ids = configs.add_to(eng, specs)
+        eng.build()
+        persistent, ctas = eng.launch_layout()
+        assert persistent == (mode == "persistent"), ctas
+        if persistent:
+            assert all(c > 0 for c in ctas), ctas
+        t = 0.0
+        for n_iv in (8, 8, 16):
+            eng.advance(t, n_iv, tolerate_retire=True)
+            t += n_iv * G.H_MAX
+        out[mode] = [eng.vnew(i) for i in ids]
+        out[mode + "_units"] = eng.compartment_updates(-1)
+        eng.close()
+    for k, (a, b) in enumerate(zip(out["persistent"], out["per_type"])):
+        np.testing.assert_array_equal(a, b, err_msg=f"system {k}")
+    assert out["persistent_units"] == out["per_type_units"]
