@@ -2,7 +2,10 @@
 host runtime + C ABI) and the gbrkc_main CLI.
 
 Kernel translation units use -fmad=false (the FP64 path reproduces the
-oracle bit for bit; wanted fused multiply-adds are written explicitly);
+oracle bit for bit; wanted fused multiply-adds are written explicitly).  The
+mixed-precision unit (FP32 gating) also takes approximate FP32 division
+(-prec-div=false, within 2 ulp): it is checked against FP64 by tolerance, and
+FP64 arithmetic is unaffected by the flag;
 host code uses -ffp-contract=off so setup arithmetic is identical on x86 and
 aarch64 hosts.  Objects go to _build/ next to this file.
 """
@@ -30,6 +33,7 @@ CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-un
             f"-I{CUDA_HOME}/include", f"-I{os.path.join(ROOT, 'include')}"]
 
 KERNEL_TUS = ["kernels_fp64.cu", "kernels_fp32.cu"]
+TU_FLAGS = {"kernels_fp32.cu": ["-prec-div=false"]}
 HOST_TUS = ["engine.cpp", "host_init.cpp", "compat.cpp"]
 
 
@@ -51,10 +55,10 @@ def build(verbose: bool = False) -> str:
             continue
         obj = os.path.join(BUILD, tu + ".o")
         objs.append(obj)
-        if not _newer(obj, [src] + headers):
+        if not _newer(obj, [src, os.path.abspath(__file__)] + headers):
             continue
         if tu.endswith(".cu"):
-            cmd = [NVCC] + NVFLAGS + ["-c", src, "-o", obj]
+            cmd = [NVCC] + NVFLAGS + TU_FLAGS.get(tu, []) + ["-c", src, "-o", obj]
         else:
             cmd = [CXX] + CXXFLAGS + ["-c", src, "-o", obj]
         if verbose:

@@ -375,7 +375,7 @@ struct PoolHost {
   std::vector<int> stim_comp, cell_soma;
   std::vector<double> stim_amp, stim_t0, stim_t1;
   long ws_total = 0;
-  int max_nc = 0, min_nc = 1 << 30;
+  int max_nc = 0, min_nc = 1 << 30, max_ncell = 0;
   // launch configuration
   int team = TEAM_BLOCK, block = 256, grid = 1;
   size_t smem = 0;
@@ -422,6 +422,8 @@ struct gbrkc_engine {
   size_t mega_smem = 0;
   int role_ctas[NTYPES] = {};
   int role_cap[NTYPES] = {};
+  int gr_warps = 0;             // granule warps in all (32 systems each)
+  double role_work[NTYPES] = {};  // smoothed CTA-ms per role
   int *d_queue = nullptr;
   unsigned long long *d_tstart = nullptr, *d_tend = nullptr;
   ~gbrkc_engine() {
@@ -562,6 +564,7 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
     P.sys_cell0.push_back(cell0);
     P.max_nc = std::max(P.max_nc, S.nc);
     P.min_nc = std::min(P.min_nc, S.nc);
+    P.max_ncell = std::max(P.max_ncell, S.n);
     // template (pool-local)
     auto tl = P.tmpl_local.find(S.tmpl);
     if (tl == P.tmpl_local.end()) {
@@ -654,7 +657,7 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
   // 32 systems side by side beat one system over 4 lanes)
   const int nsys = (int)P.systems.size();
   if (P.max_nc <= LANE_MAX_NC) {
-    P.team = (P.type == GR && P.min_nc == 4 && P.max_nc == 4) ? TEAM_LANE4 : TEAM_THREAD;
+    P.team = (P.type == GR && P.min_nc == 4 && P.max_nc == 4 && P.max_ncell == 1) ? TEAM_LANE4 : TEAM_THREAD;
     P.block = MEGA_BLOCK;
   }
   else if (P.max_nc <= 320) { P.team = TEAM_WARP; P.block = 128; }
@@ -754,7 +757,7 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
 // Launch every pool's kernel on its own stream (the pools run concurrently)
 // and time the whole advance and each kernel with CUDA events recorded on the
 // launching streams.
-void rebalance_roles(gbrkc_engine *E, const double *role_ms);
+void rebalance_roles(gbrkc_engine *E, const double *role_ms, bool tune_gr);
 
 template <typename R> PoolView<R> &pool_view(PoolHost &P);
 template <> PoolView<double> &pool_view<double>(PoolHost &P) { return P.vd; }
@@ -770,12 +773,17 @@ int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
     end += E->role_ctas[t];
     M.role_end[t] = end;
   }
-  M.lane_warps = 8;
   M.gr_nc4 = E->pools[GR].team == TEAM_LANE4;
+  // granule warps spread as evenly as whole warps allow: the first
+  // lane_extra CTAs take lane_warps + 1
+  M.lane_warps = 0;
+  M.lane_extra = 0;
   if (E->role_ctas[GR] > 0) {
-    const int nsys = (int)E->pools[GR].systems.size();
-    const int per_cta = (nsys + E->role_ctas[GR] - 1) / E->role_ctas[GR];
-    M.lane_warps = std::min(MEGA_BLOCK / 32, std::max(1, (per_cta + 31) / 32));
+    M.lane_warps = E->gr_warps / E->role_ctas[GR];
+    M.lane_extra = E->gr_warps % E->role_ctas[GR];
+    if (M.lane_warps + (M.lane_extra > 0) > MEGA_BLOCK / 32)
+      return fail(GBRKC_ESTATE, "persistent launch: %d granule warps do not fit %d CTAs", E->gr_warps,
+                  E->role_ctas[GR]);
   }
   if (E->role_ctas[GR] > 0 &&
       (!E->pools[GR].ws_in_smem ||
@@ -806,7 +814,7 @@ int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
     role_ms[t] = E->role_ctas[t] ? (double)(last - t_first) * 1e-6 : 0.0;
     E->last_kernel_ms[t] = (float)role_ms[t];
   }
-  if (!init && n_iv > 0) rebalance_roles(E, role_ms);
+  if (!init && n_iv > 0) rebalance_roles(E, role_ms, true);
   return 0;
 }
 
@@ -857,37 +865,79 @@ int system_loc(gbrkc_engine *E, int id, PoolHost **P, HostSystem **S) {
 namespace {
 
 // Re-split the persistent launch's CTAs between roles so that they finish
-// together: each role's work is estimated as (its CTAs x its makespan) from
-// the last launch, and CTAs are handed out in proportion, within each role's
-// cap (a role cannot use more CTAs than it has teams of work).
-void rebalance_roles(gbrkc_engine *E, const double *role_ms) {
+// together.  Granule warps are latency-bound (a lone warp runs one dependent
+// FP64 chain per system at ~64 cycles an operation): spreading them over more
+// CTAs shortens their time only through less sharing of each SM's FP64 pipe,
+// modelled as T ~ (warps per CTA)^0.5.  The other roles' time is taken as
+// inversely proportional to the CTAs they get.  The granule CTA count moves
+// halfway to where the two models cross; the other roles then split the
+// remaining CTAs in proportion to their measured work (CTAs x makespan,
+// smoothed over launches), each within its cap (a role cannot use more CTAs
+// than it has teams of work).
+void rebalance_roles(gbrkc_engine *E, const double *role_ms, bool tune_gr) {
+  int avail = E->mega_grid;
+  if (E->role_ctas[GR] > 0) {
+    double others = 0.0;
+    int nother = 0, other_ctas = 0;
+    for (int t = 0; t < NTYPES; t++)
+      if (t != GR && E->role_ctas[t] > 0) {
+        others = std::max(others, role_ms[t]);
+        nother++;
+        other_ctas += E->role_ctas[t];
+      }
+    const int lo = std::max(1, (E->gr_warps + MEGA_BLOCK / 32 - 1) / (MEGA_BLOCK / 32));
+    const int hi = std::max(lo, std::min(E->gr_warps, E->mega_grid - nother));
+    int c = E->role_ctas[GR];
+    if (tune_gr && others > 0.0 && role_ms[GR] > 0.0 && other_ctas > 0) {
+      const double d0 = (double)E->gr_warps / c;
+      int best = c;
+      double bestv = 1e300;
+      for (int x = lo; x <= hi; x++) {
+        const double tg = role_ms[GR] * sqrt(((double)E->gr_warps / x) / d0);
+        const int oc = E->mega_grid - x;
+        if (oc < nother) continue;
+        const double to = others * (double)other_ctas / (double)oc;
+        const double v = std::max(tg, to);
+        if (v < bestv) { bestv = v; best = x; }
+      }
+      c = (c + best + 1) / 2;
+    }
+    E->role_ctas[GR] = std::max(lo, std::min(hi, c));
+    avail -= E->role_ctas[GR];
+  }
+  // work per role (CTA-ms), smoothed over launches
   double work[NTYPES] = {}, total = 0.0;
-  for (int t = 0; t < NTYPES; t++)
-    if (E->role_ctas[t] > 0) { work[t] = std::max(role_ms[t], 1e-3) * E->role_ctas[t]; total += work[t]; }
+  for (int t = 0; t < NTYPES; t++) {
+    if (t == GR || E->role_ctas[t] == 0) continue;
+    const double w = std::max(role_ms[t], 1e-3) * E->role_ctas[t];
+    E->role_work[t] = (E->role_work[t] > 0.0) ? 0.5 * E->role_work[t] + 0.5 * w : w;
+    work[t] = E->role_work[t];
+    total += work[t];
+  }
   if (total <= 0.0) return;
   int want[NTYPES] = {}, used = 0;
   for (int t = 0; t < NTYPES; t++) {
-    if (E->role_ctas[t] == 0) continue;
-    double share = E->mega_grid * work[t] / total;
-    int n = (int)std::lround(0.5 * E->role_ctas[t] + 0.5 * share);
+    if (t == GR || E->role_ctas[t] == 0) continue;
+    const int n = (int)std::lround(avail * work[t] / total);
     want[t] = std::max(1, std::min(E->role_cap[t], n));
     used += want[t];
   }
   // fix the total by moving CTAs to / from the role with the largest work per CTA
-  while (used != E->mega_grid) {
+  while (used != avail) {
     int best = -1;
-    double bv = used < E->mega_grid ? -1.0 : 1e300;
+    double bv = used < avail ? -1.0 : 1e300;
     for (int t = 0; t < NTYPES; t++) {
-      if (want[t] == 0) continue;
-      double v = work[t] / want[t];
-      if (used < E->mega_grid && want[t] < E->role_cap[t] && v > bv) { bv = v; best = t; }
-      if (used > E->mega_grid && want[t] > 1 && v < bv) { bv = v; best = t; }
+      if (t == GR || want[t] == 0) continue;
+      const double v = work[t] / want[t];
+      if (used < avail && want[t] < E->role_cap[t] && v > bv) { bv = v; best = t; }
+      if (used > avail && want[t] > 1 && v < bv) { bv = v; best = t; }
     }
     if (best < 0) break;
-    want[best] += used < E->mega_grid ? 1 : -1;
-    used += used < E->mega_grid ? 1 : -1;
+    want[best] += used < avail ? 1 : -1;
+    used += used < avail ? 1 : -1;
   }
-  for (int t = 0; t < NTYPES; t++) E->role_ctas[t] = want[t];
+  for (int t = 0; t < NTYPES; t++)
+    if (t != GR) E->role_ctas[t] = want[t];
 }
 
 // Decide whether all pools fit the persistent launch's team shapes and size
@@ -901,7 +951,7 @@ int setup_mega(gbrkc_engine *E) {
   // granule CTAs run up to MEGA_BLOCK single-lane systems (capped below at one
   // warp per CTA); Golgi 8 warps; Purkinje / olive one system per CTA
   const int teams[NTYPES] = {32, MEGA_BLOCK / TEAM_WARP, 1, 1};
-  const int team_kind[NTYPES] = {(G.min_nc == 4 && G.max_nc == 4) ? TEAM_LANE4 : TEAM_THREAD, TEAM_WARP,
+  const int team_kind[NTYPES] = {(G.min_nc == 4 && G.max_nc == 4 && G.max_ncell == 1) ? TEAM_LANE4 : TEAM_THREAD, TEAM_WARP,
                                  TEAM_BLOCK, TEAM_BLOCK};
   size_t smem = 0;
   int nonempty = 0;
@@ -929,17 +979,26 @@ int setup_mega(gbrkc_engine *E) {
   if (E->mega_grid < nonempty) return 0;
   E->mega_smem = smem;
   E->mega = true;
-  // first split: by compartment count with per-type weights (granule cells
-  // take ~20x more steps per compartment); refined after every launch
-  const double w[NTYPES] = {30.0, 1.0, 0.35, 3.0};
+  // first split: granule warps two to a CTA (or spread over every CTA when
+  // granules are alone); the rest by compartment count with per-type weights;
+  // refined after every launch
+  E->gr_warps = (int)((E->pools[GR].systems.size() + 31) / 32);
+  const double w[NTYPES] = {0.0, 1.0, 0.35, 3.0};
   double ms[NTYPES];
+  int others = 0;
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
     E->role_ctas[t] = P.systems.empty() ? 0 : 1;
     ms[t] = P.systems.empty() ? 0.0 : w[t] * (double)P.nc;
+    others += (t != GR && !P.systems.empty());
   }
-  rebalance_roles(E, ms);
-  for (int i = 0; i < 3; i++) rebalance_roles(E, ms);
+  if (E->role_ctas[GR] > 0) {
+    // two granule warps to a CTA beside other roles, else spread over all
+    E->role_ctas[GR] = others ? (E->gr_warps + 1) / 2 : std::min(E->gr_warps, E->mega_grid);
+    E->role_ctas[GR] = std::max(1, std::min(E->role_ctas[GR], E->mega_grid - others));
+  }
+  rebalance_roles(E, ms, false);
+  for (int t = 0; t < NTYPES; t++) E->role_work[t] = 0.0;
   return 0;
 }
 

@@ -98,14 +98,14 @@ struct PoolView {
 enum TeamKind { TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0 };
 
 // All pools in one persistent launch: CTA b < role_end[0] integrates granule
-// systems (one per lane, on the CTA's first lane_warps warps), then Golgi
+// systems (one per lane, on the CTA's first warps), then Golgi
 // (32-lane warps), Purkinje and olive (whole blocks).  Each role pulls
 // systems from its own atomic queue.
 template <typename R>
 struct MegaView {
   PoolView<R> pool[NTYPES];
   int role_end[NTYPES];
-  int lane_warps;             // active warps per granule CTA
+  int lane_warps, lane_extra;  // granule CTA b runs lane_warps (+1 if b < lane_extra) warps
   int gr_nc4;                 // every granule system has 4 compartments
   int *queue;                 // [NTYPES] next-system counters, zeroed per launch
   unsigned long long *t_start; // [grid] globaltimer at each CTA's start

@@ -91,6 +91,47 @@ constexpr int RHO_ITMAX = 1000;              // solve_rkc.cu:572
 enum Tick { TICK_DONE = 0, TICK_MORE = 1, TICK_ION = 2 };
 constexpr int ION_WAIT_MAX = 12;             // warp iterations a due ion update may wait
 
+// One compartment's ion update (when update_ion) and its current term b
+// (*_update_ion* and *_update_matrix of the reference), at pool compartment gi
+// with stage voltage vyi.
+template <int CT, typename R>
+__device__ __forceinline__ double comp_ion_b(const PoolView<R> &P, long gi, double vyi, double sum_dt,
+                                            bool update_ion) {
+  const Slots<R> sl{P.ion, P.cond, P.stride, gi};
+  if (CT == PKJ) {
+    if (update_ion) {
+      double ve = P.v[gi], ca = P.ca[gi], rv = P.rev[gi];
+      Pkj<R>::ion(sl, ve, ca, rv, P.shell[gi], (P.flags[gi] & 1) != 0, vyi, sum_dt);
+      P.v[gi] = ve; P.ca[gi] = ca; P.rev[gi] = rv;
+    }
+    return (double)Pkj<R>::b(sl, vyi, P.iext[gi], P.rev[gi]);
+  } else if (CT == IO) {
+    if (update_ion) {
+      double ve = P.v[gi], ca = P.ca[gi];
+      Io<R>::ion(sl, ve, ca, P.ctype[gi], vyi, sum_dt);
+      P.v[gi] = ve; P.ca[gi] = ca;
+    }
+    return (double)Io<R>::b(sl, vyi, P.iext[gi]);
+  } else if (CT == GR) {
+    if (update_ion) {
+      const int t = P.ctype[gi];
+      double ve = P.v[gi];
+      if (t >= 5) gr_na<R>(sl, P.na[t], vyi, ve, sum_dt);
+      Gr<R>::ion(sl, ve, P.ca[gi], vyi, sum_dt);
+      P.v[gi] = ve;
+    }
+    return (double)Gr<R>::b(sl, vyi, P.iext[gi]);
+  } else {  // GO
+    if (update_ion) {
+      double ve = P.v[gi], ca = P.ca[gi], ca2 = P.ca2[gi], rv = P.rev[gi], cao = P.ca_old[gi];
+      Go<R>::ion(sl, ve, ca, ca2, rv, P.area[gi], vyi, sum_dt);
+      Go<R>::kahp(sl, ca, cao, sum_dt);
+      P.v[gi] = ve; P.ca[gi] = ca; P.ca2[gi] = ca2; P.rev[gi] = rv; P.ca_old[gi] = cao;
+    }
+    return (double)Go<R>::b(sl, vyi, P.iext[gi], P.rev[gi]);
+  }
+}
+
 template <int CT, typename R, class Team>
 struct Sys {
   static constexpr int LS = Team::LS, NCF = Team::NCF;
@@ -414,7 +455,12 @@ struct Sys {
         err = tree_sum(sc, nc);
       }
     }
-    err = sqrt(err / (double)nc);
+    // division by a power of two is exact scaling: multiply instead (the
+    // same correctly rounded value, without the long FP64 divide)
+    if ((nc & (nc - 1)) == 0)
+      err = sqrt(err * __longlong_as_double((long long)(1023 - (__ffs(nc) - 1)) << 52));  // 2^-log2(nc)
+    else
+      err = sqrt(err / (double)nc);
     if (!(err == err)) {
       c.status |= ST_NAN;
       return ATT_FAIL;
@@ -479,47 +525,7 @@ struct Sys {
   __device__ __forceinline__ void ion_and_b(double sum_dt, bool update_ion, bool with_gap = true) {
     const V vy = vec(LY);
     const V b = bvec();
-    const Slots<R> sl0{P.ion, P.cond, P.stride, 0};
-    for (int i = tm.rank(); i < nc; i += tm.size()) {
-      const long gi = off + i;
-      Slots<R> sl = sl0;
-      sl.i = gi;
-      const double vyi = vy[i];
-      double bi;
-      if (CT == PKJ) {
-        if (update_ion) {
-          double ve = P.v[gi], ca = P.ca[gi], rv = P.rev[gi];
-          Pkj<R>::ion(sl, ve, ca, rv, P.shell[gi], (P.flags[gi] & 1) != 0, vyi, sum_dt);
-          P.v[gi] = ve; P.ca[gi] = ca; P.rev[gi] = rv;
-        }
-        bi = (double)Pkj<R>::b(sl, vyi, P.iext[gi], P.rev[gi]);
-      } else if (CT == IO) {
-        if (update_ion) {
-          double ve = P.v[gi], ca = P.ca[gi];
-          Io<R>::ion(sl, ve, ca, P.ctype[gi], vyi, sum_dt);
-          P.v[gi] = ve; P.ca[gi] = ca;
-        }
-        bi = (double)Io<R>::b(sl, vyi, P.iext[gi]);
-      } else if (CT == GR) {
-        if (update_ion) {
-          const int t = P.ctype[gi];
-          double ve = P.v[gi];
-          if (t >= 5) gr_na<R>(sl, P.na[t], vyi, ve, sum_dt);
-          Gr<R>::ion(sl, ve, P.ca[gi], vyi, sum_dt);
-          P.v[gi] = ve;
-        }
-        bi = (double)Gr<R>::b(sl, vyi, P.iext[gi]);
-      } else {  // GO
-        if (update_ion) {
-          double ve = P.v[gi], ca = P.ca[gi], ca2 = P.ca2[gi], rv = P.rev[gi], cao = P.ca_old[gi];
-          Go<R>::ion(sl, ve, ca, ca2, rv, P.area[gi], vyi, sum_dt);
-          Go<R>::kahp(sl, ca, cao, sum_dt);
-          P.v[gi] = ve; P.ca[gi] = ca; P.ca2[gi] = ca2; P.rev[gi] = rv; P.ca_old[gi] = cao;
-        }
-        bi = (double)Go<R>::b(sl, vyi, P.iext[gi], P.rev[gi]);
-      }
-      b[i] = bi;
-    }
+    for (int i = tm.rank(); i < nc; i += tm.size()) b[i] = comp_ion_b<CT, R>(P, off + i, vy[i], sum_dt, update_ion);
     if (CT == IO && with_gap && P.sys_ngap[s] > 0) {
       // io_gap_update + add_io_gap_val: per receiving dendrite, its four
       // edges in order (the reference adds them with atomics)

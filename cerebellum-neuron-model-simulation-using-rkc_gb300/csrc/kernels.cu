@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "integrator.cuh"
+#include "lane_sys.cuh"
 
 namespace gbrkc {
 
@@ -21,8 +22,10 @@ __global__ void __launch_bounds__(256, 1) k_advance(const __grid_constant__ Pool
     // warp w of block b starts at system 32 (w * grid + b) + lane: the first
     // warps of every block are filled before any block's later warps
     const int first = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * 32 + ((int)threadIdx.x & 31);
-    run_lanes<CT, R, MEGA_BLOCK, TS == TEAM_LANE4 ? 4 : 0>(P, nullptr, first, gridDim.x * MEGA_BLOCK, smem, t0, n_iv,
-                                                           iv0, init != 0);
+    if (TS == TEAM_LANE4)
+      run_lanes_regs<CT, R, MEGA_BLOCK, 4>(P, nullptr, first, gridDim.x * MEGA_BLOCK, smem, t0, n_iv, iv0, init != 0);
+    else
+      run_lanes<CT, R, MEGA_BLOCK>(P, nullptr, first, gridDim.x * MEGA_BLOCK, smem, t0, n_iv, iv0, init != 0);
   } else if (TS == TEAM_BLOCK) {
     BlockTeam tm;
     for (int s = blockIdx.x; s < P.nsys; s += gridDim.x) {
@@ -91,10 +94,10 @@ __global__ void __launch_bounds__(MEGA_BLOCK, 1) k_mega(const __grid_constant__ 
   while (role < NTYPES - 1 && (int)blockIdx.x >= M.role_end[role]) role++;
   switch (role) {
     case GR:
-      // single-lane granule systems on the first lane_warps warps of the CTA
-      if ((int)(threadIdx.x >> 5) < M.lane_warps) {
+      // single-lane granule systems on the CTA's first warps
+      if ((int)(threadIdx.x >> 5) < M.lane_warps + ((int)blockIdx.x < M.lane_extra ? 1 : 0)) {
         if (M.gr_nc4)
-          run_lanes<GR, R, MEGA_BLOCK, 4>(M.pool[GR], M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
+          run_lanes_regs<GR, R, MEGA_BLOCK, 4>(M.pool[GR], M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
         else
           run_lanes<GR, R, MEGA_BLOCK>(M.pool[GR], M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
       }
