@@ -32,9 +32,9 @@ CXX = os.environ.get("CXX", "g++")
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
             f"-I{CUDA_HOME}/include", f"-I{os.path.join(ROOT, 'include')}"]
 
-KERNEL_TUS = ["kernels_fp64.cu", "kernels_fp32.cu"]
+KERNEL_TUS = ["kernels_fp64.cu", "kernels_fp32.cu", "compat.cu"]
 TU_FLAGS = {"kernels_fp32.cu": ["-prec-div=false"]}
-HOST_TUS = ["engine.cpp", "host_init.cpp", "compat.cpp"]
+HOST_TUS = ["engine.cpp", "host_init.cpp"]
 
 
 def _newer(target: str, deps) -> bool:
@@ -78,7 +78,8 @@ def build(verbose: bool = False) -> str:
         subprocess.run(cmd, check=True)
     cli_src = os.path.join(CSRC, "cli.cpp")
     if os.path.exists(cli_src) and _newer(CLI, [cli_src, LIB]):
-        cmd = [CXX] + CXXFLAGS + [cli_src, "-o", CLI, f"-L{HERE}", "-lgbrkc", f"-Wl,-rpath,{HERE}"]
+        cmd = [CXX] + CXXFLAGS + [cli_src, "-o", CLI, f"-L{HERE}", "-lgbrkc", f"-Wl,-rpath,{HERE}",
+                                  f"-L{CUDA_HOME}/lib64", "-lcudart"]
         subprocess.run(cmd, check=True)
     return LIB
 

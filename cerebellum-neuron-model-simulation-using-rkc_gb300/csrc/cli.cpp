@@ -1,0 +1,134 @@
+// gbrkc_main: the reference's command line over gbrkc_compat.h.
+//
+//   gbrkc_main S_gr gx gy S_go ox oy S_pkj px py S_io ix iy [TS_ms]
+//
+// S is the solver name per type, matched on its first three letters as the
+// reference does (main.cu:60-102); only RKC is provided.  A type with
+// nx * ny == 0 is skipped.  Each 0.125 ms interval: the type's stimulus
+// protocol, one advance, the voltages copied back, one CSV row written; the
+// files are the reference's: <type>_v_by_RKC.csv, <type>_raster_by_RKC.csv,
+// comptime.csv (appended) and an empty debug_file.csv.  The jitter stream is
+// seeded with srand(0) first, as main.cu:38 does.  TS_ms (default 1500, the
+// reference's TS) is this tool's addition.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "../../include/gbrkc_compat.h"
+
+namespace {
+
+struct TypeRun {
+  const char *name;
+  neuron_t *(*init)(int, int, const char *, neuron_t *);
+  neuron_solve_t *(*solve_init)(neuron_solve_t *, const char *, neuron_t *, neuron_t *);
+  void (*stim)(neuron_t *, double);
+  void (*out)(neuron_t *, double *, double *, double, FILE *, FILE *);
+  void (*fin)(neuron_t *, neuron_t *, FILE *, FILE *);
+  void (*solve_fin)(int, neuron_solve_t *, neuron_solve_t *);
+  char solver[GBRKC_MAX_BUF];
+  neuron_t *p = nullptr, *d = nullptr;
+  neuron_solve_t *ps = nullptr, *ds = nullptr;
+  FILE *fv = nullptr, *fr = nullptr;
+  double *vh = nullptr, *raster = nullptr;
+};
+
+void gr_update(TypeRun &r) { gr_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr, nullptr); }
+void go_update(TypeRun &r) { go_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr); }
+void pkj_update(TypeRun &r) { pkj_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr, nullptr); }
+void io_update(TypeRun &r) { io_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr); }
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  if (argc < 13) {
+    printf("usage: %s S_gr gx gy S_go ox oy S_pkj px py S_io ix iy [TS_ms]\n", argv[0]);
+    return 1;
+  }
+  const double ts = (argc > 13) ? atof(argv[13]) : 1500.0;
+  srand(0);  // the initial-voltage jitter stream, seeded as main.cu:38 does
+  TypeRun runs[4] = {
+      {"gr", gr_initialize, gr_solve_initialize, gr_set_current_launch, gr_output_file, gr_finalize, gr_solve_finalize},
+      {"go", go_initialize, go_solve_initialize, go_set_current_launch, go_output_file, go_finalize, go_solve_finalize},
+      {"pkj", pkj_initialize, pkj_solve_initialize, pkj_set_current_launch, pkj_output_file, pkj_finalize,
+       pkj_solve_finalize},
+      {"io", io_initialize, io_solve_initialize, io_set_current_launch, io_output_file, io_finalize, io_solve_finalize}};
+  void (*update[4])(TypeRun &) = {gr_update, go_update, pkj_update, io_update};
+  int nx[4], ny[4];
+  for (int k = 0; k < 4; k++) {
+    strncpy(runs[k].solver, argv[1 + 3 * k], GBRKC_MAX_BUF - 1);
+    runs[k].solver[GBRKC_MAX_BUF - 1] = 0;
+    nx[k] = atoi(argv[2 + 3 * k]);
+    ny[k] = atoi(argv[3 + 3 * k]);
+    if (strncmp(runs[k].solver, "RKC", 3) != 0) {
+      printf("Error!! -> set solver name in argv [ %d ] (only RKC is provided)\n", 1 + 3 * k);
+      return 0;
+    }
+    char name[64];
+    snprintf(name, sizeof name, "%s_v_by_RKC.csv", runs[k].name);
+    runs[k].fv = fopen(name, "w");
+    snprintf(name, sizeof name, "%s_raster_by_RKC.csv", runs[k].name);
+    runs[k].fr = fopen(name, "w");
+    if (!runs[k].fv || !runs[k].fr) {
+      printf("cannot open the output files of %s\n", runs[k].name);
+      return 1;
+    }
+  }
+  for (int k = 0; k < 4; k++) {
+    TypeRun &r = runs[k];
+    r.p = (neuron_t *)malloc(sizeof(neuron_t));
+    r.ps = (neuron_solve_t *)malloc(sizeof(neuron_solve_t));
+    r.d = r.init(nx[k], ny[k], r.solver, r.p);
+    r.ds = r.solve_init(r.ps, r.solver, r.p, r.d);
+    r.vh = (double *)malloc((r.p->nc > 0 ? r.p->nc : 1) * sizeof(double));
+    r.raster = (double *)malloc((r.p->n > 0 ? r.p->n : 1) * sizeof(double));
+    for (int j = 0; j < r.p->n; j++) r.raster[j] = 100.0;
+  }
+  gap_t *io_gap = io_gap_create(nx[3], ny[3]);
+  FILE *dbg = fopen("debug_file.csv", "w");
+  if (dbg) fclose(dbg);
+
+  double t = 0.0;
+  const clock_t start = clock();
+  clock_t half = start;
+  while (t < ts - 0.0001) {
+    for (int k = 0; k < 4; k++) {
+      TypeRun &r = runs[k];
+      if (r.p->n <= 0) continue;
+      r.stim(r.d, t);
+      update[k](r);
+      if (cudaMemcpy(r.vh, r.ps->vec[v_new], r.p->nc * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        printf("copy of %s voltages failed\n", r.name);
+        return 1;
+      }
+      if (isnan(r.vh[1])) {
+        printf("isnan in %s, time=%f\n", r.name, t);
+        return 1;
+      }
+      r.out(r.p, r.vh, r.raster, t + H_MAX, r.fv, r.fr);
+    }
+    t += H_MAX;
+    if (t >= 500.0 && 500.0 + H_MAX > t) half = clock();
+  }
+  const clock_t end = clock();
+  const double comp = (double)(end - start) / CLOCKS_PER_SEC;
+  printf("time:%f \ncomputational time = %.2f \n", t, comp);
+  const int n[4] = {runs[0].p->n, runs[1].p->n, runs[2].p->n, runs[3].p->n};
+  if (ts <= 500.0)
+    output_time(n[0], runs[0].solver, n[1], runs[1].solver, n[2], runs[2].solver, n[3], runs[3].solver, comp, (int)ts);
+  else
+    output_time2(n[0], runs[0].solver, n[1], runs[1].solver, n[2], runs[2].solver, n[3], runs[3].solver, comp,
+                 (double)(end - half) / CLOCKS_PER_SEC, (int)ts);
+  io_gap_finalize(io_gap);
+  for (int k = 0; k < 4; k++) {
+    TypeRun &r = runs[k];
+    free(r.vh);
+    free(r.raster);
+    r.fin(r.p, r.d, r.fv, r.fr);
+    r.solve_fin(n[k], r.ds, r.ps);
+  }
+  return 0;
+}

@@ -1125,6 +1125,26 @@ extern "C" int gbrkc_read(gbrkc_engine *E, int id, int field, int k, double *hos
   return 0;
 }
 
+extern "C" int gbrkc_field_device_ptr(gbrkc_engine *E, int id, int field, double **ptr) {
+  PoolHost *P;
+  HostSystem *S;
+  int rc = system_loc(E, id, &P, &S);
+  if (rc) return rc;
+  if (!ptr) return fail(GBRKC_EINVAL, "null output");
+  const long off = P->sys_off[S->pool_index];
+  double *base = nullptr;
+  switch (field) {
+    case GBRKC_F_VNEW: base = P->d_vnew; break;
+    case GBRKC_F_V: base = P->d_v; break;
+    case GBRKC_F_CA: base = P->d_ca; break;
+    case GBRKC_F_REV: base = P->d_rev; break;
+    case GBRKC_F_IEXT: base = (E->precision == GBRKC_FP64) ? P->vd.iext : P->vf.iext; break;
+    default: return fail(GBRKC_EINVAL, "field %d has no per-compartment device array", field);
+  }
+  *ptr = base ? base + off : nullptr;
+  return 0;
+}
+
 extern "C" int gbrkc_system_ctl(gbrkc_engine *E, int id, double *ctl8, long long *stats6, int *status) {
   PoolHost *P;
   HostSystem *S;

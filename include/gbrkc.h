@@ -40,7 +40,8 @@ enum {
   GBRKC_F_B = 3,       /* frozen current vector b */
   GBRKC_F_ION = 4,     /* gating slot k (as FP64) */
   GBRKC_F_REV = 5,     /* Ca reversal potential (GO, PKJ) */
-  GBRKC_F_YN = 6       /* RKC solution vector yn */
+  GBRKC_F_YN = 6,      /* RKC solution vector yn */
+  GBRKC_F_IEXT = 7     /* elem[i_ext]: injected current (device pointer only) */
 };
 
 typedef struct gbrkc_system_desc {
@@ -125,6 +126,14 @@ float gbrkc_last_kernel_ms(gbrkc_engine *e, int cell_type);
  * launch (CTAs per type written to ctas_per_type[4]), 0 when each type has
  * its own launch (entries -1), negative on error. */
 int gbrkc_launch_layout(gbrkc_engine *e, int *ctas_per_type);
+
+/* Device address of one system's per-compartment array (GBRKC_F_VNEW, _V,
+ * _CA, _REV or _IEXT; nc doubles, the system's compartments in order).  Valid
+ * until the engine is destroyed; the array is written by gbrkc_advance and may
+ * be read (or, for _IEXT, written) by the caller's own kernels between
+ * advances.  Replaces the device pointers the reference exposes through
+ * neuron_t::elem and neuron_solve_t::vec (param.h:27-46). */
+int gbrkc_field_device_ptr(gbrkc_engine *e, int system_id, int field, double **device_ptr);
 
 /* Compartment updates so far (sum over systems of (stage evaluations + step
  * attempts) x compartments; power iterations excluded), for one cell type

@@ -1,0 +1,50 @@
+"""The C-ABI library loads and exports every function include/*.h declares
+(no device calls: this runs without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+PKG = os.path.join(ROOT, "cerebellum-neuron-model-simulation-using-rkc_gb300")
+LIB = os.path.join(PKG, "libgbrkc.so")
+
+DECL = re.compile(r"^(?:__global__\s+)?[A-Za-z_][\w\s\*]*?\b([a-z_][a-z0-9_]*)\s*\(", re.M)
+
+
+def declared(header):
+    text = open(os.path.join(INCLUDE, header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = set()
+    for m in DECL.finditer(text):
+        line = text[m.start():text.find("\n", m.start())]
+        if line.lstrip().startswith(("#", "typedef", "return")):
+            continue
+        names.add(m.group(1))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(LIB):
+        import build as B
+        B.build()
+    return ctypes.CDLL(LIB)
+
+
+@pytest.mark.parametrize("header", ["gbrkc.h", "gbrkc_compat.h"])
+def test_every_declared_symbol_is_exported(lib, header):
+    names = declared(header)
+    assert len(names) > 10, names
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, f"{header}: not exported: {missing}"
+
+
+def test_reference_entry_points_present():
+    names = declared("gbrkc_compat.h")
+    for t in ("gr", "go", "pkj", "io"):
+        for f in ("initialize", "solve_initialize", "solve_update_v", "set_current", "output_file", "finalize",
+                  "solve_finalize"):
+            assert f"{t}_{f}" in names

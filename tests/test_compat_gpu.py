@@ -1,0 +1,84 @@
+"""The reference-named drop-in path (include/gbrkc_compat.h) end to end,
+through the gbrkc_main CLI: model files in the reference formats, the
+reference's stimulus kernels, rand() jitter seeded as main.cu:38, and the
+reference's CSV outputs."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import morph as M
+from test_oracle_golden import load_gold
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "cerebellum-neuron-model-simulation-using-rkc_gb300", "gbrkc_main")
+
+
+def run_cli(tmp_path, dims, ts, files):
+    for name, text in files.items():
+        (tmp_path / name).write_text(text)
+    args = [CLI]
+    for nx, ny in dims:
+        args += ["RKC", str(nx), str(ny)]
+    args.append(str(ts))
+    env = dict(os.environ, GBRKC_MODEL_DIR=str(tmp_path))
+    r = subprocess.run(args, cwd=tmp_path, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    return r
+
+
+def read_v(path):
+    rows = []
+    for line in open(path):
+        vals = [float(x) for x in line.strip().rstrip(",").split(",") if x != ""]
+        rows.append(vals)
+    return np.array(rows)
+
+
+def test_io_raster_matches_reference_golden(tmp_path):
+    """io_raster_by_RKC.csv of the reference (8x8 IO, default stimulus)."""
+    run_cli(tmp_path, [(0, 0), (0, 0), (0, 0), (8, 8)], 809.0, {"IO.txt": M.write_rows(M.io_rows(), M.IO)})
+    mine = []
+    for line in open(tmp_path / "io_raster_by_RKC.csv"):
+        t, c = line.strip().split(",")
+        mine.append((float(t), int(c)))
+    gold = {c: t for t, c in load_gold()}
+    assert sorted(c for _, c in mine) == list(range(64)), "every cell spikes exactly once"
+    times = {c: t for t, c in mine}
+    assert all(abs(times[c] - gold[c]) <= 0.125 for c in range(64))
+    exact = sum(times[c] == gold[c] for c in range(64))
+    assert exact >= 62, f"only {exact}/64 spike times identical"
+    v = read_v(tmp_path / "io_v_by_RKC.csv")
+    assert v.shape == (int(809.0 / 0.125), 1 + 3 * 64)
+    assert (tmp_path / "comptime.csv").exists()
+
+
+def test_go_pkj_blocks_match_oracle(tmp_path, oracle):
+    """GoC 2x2 and PC 2x1 blocks (synthetic trees in the reference formats)
+    against the oracle in canonical mode: every written soma voltage equal
+    to the printed precision (%lf, 1e-6 mV)."""
+    go_rows, pkj_rows = M.go_synthetic(3), M.pkj_synthetic(4)
+    gj = "\n".join(f"{a},{b}" for a, b in M.PKJ_GJ_PAIRS) + "\n"
+    ts = 3.0
+    run_cli(tmp_path, [(0, 0), (2, 2), (2, 1), (0, 0)], ts,
+            {"Go_131.txt": M.write_rows(go_rows, M.GO), "Pkj.txt": M.write_rows(pkj_rows, M.PKJ), "Pkj_GJ.csv": gj})
+    O = oracle
+    O.libc_srand(0)
+    jit_go = O.draw_jitter(O.GO, 4)
+    jit_pkj = O.draw_jitter(O.PKJ, 2)
+    cases = [("go", O.System(O.GO, 2, 2, go_rows, jit_go, go_gj=True, canon=True), 30, 131),
+             ("pkj", O.System(O.PKJ, 2, 1, pkj_rows, jit_pkj, gj_pairs=M.PKJ_GJ_PAIRS, pkj_gj=True, canon=True),
+              1599, 1600)]
+    for name, s, soma, ncomp in cases:
+        assert s.init() == 0
+        v = read_v(tmp_path / f"{name}_v_by_RKC.csv")
+        t = 0.0
+        for k in range(int(ts / 0.125)):
+            assert s.advance(t) == 0
+            t += 0.125
+            ref = s.vnew()[soma::ncomp]
+            assert v[k, 0] == pytest.approx(t, abs=1e-9)
+            np.testing.assert_allclose(v[k, 1:], ref, atol=1.5e-6, rtol=0, err_msg=f"{name} interval {k}")
