@@ -114,10 +114,12 @@ void io_solve_update_v(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron
  * (pkj.cu:333); IO: 5.5 uA/cm^2 at the dendrite for 800 <= t < 820
  * (io.cu:247). */
 #ifdef __CUDACC__
-__global__ void gr_set_current(neuron_t *d_gr, const double t);
-__global__ void go_set_current(neuron_t *d_go, const double t);
-__global__ void pkj_set_current(neuron_t *d_pkj, const double t);
-__global__ void io_set_current(neuron_t *d_io, const double t);
+/* default visibility: nvcc hides kernel stubs by default, which would keep a
+ * caller's <<<>>> launch from binding to the library's kernels */
+__attribute__((visibility("default"))) __global__ void gr_set_current(neuron_t *d_gr, const double t);
+__attribute__((visibility("default"))) __global__ void go_set_current(neuron_t *d_go, const double t);
+__attribute__((visibility("default"))) __global__ void pkj_set_current(neuron_t *d_pkj, const double t);
+__attribute__((visibility("default"))) __global__ void io_set_current(neuron_t *d_io, const double t);
 #endif
 void gr_set_current_launch(neuron_t *d_gr, const double t);
 void go_set_current_launch(neuron_t *d_go, const double t);

@@ -17,6 +17,7 @@ DECL = re.compile(r"^(?:__global__\s+)?[A-Za-z_][\w\s\*]*?\b([a-z_][a-z0-9_]*)\s
 def declared(header):
     text = open(os.path.join(INCLUDE, header)).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"__attribute__\(\(\w+(?:\(\"\w+\"\))?\)\)\s*", "", text)
     names = set()
     for m in DECL.finditer(text):
         line = text[m.start():text.find("\n", m.start())]
