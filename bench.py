@@ -100,8 +100,13 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ workloads
-def workload(name):
+def workload(name, scale=1.0):
     import configs
+    if name == "mixed" and scale < 1.0:
+        specs = configs.scaled_mixed_batch(scale)
+        c = configs.type_counts(specs)
+        return specs, (f"mixed-type batch scaled x{scale:g}: {c['gr'][0]} GrC x4 + {c['go'][0]} GoC x131 + "
+                       f"{c['pkj'][0]} PC x1600 + IO 16x16 net x3 (small profiling case)")
     if name == "mixed":
         return configs.mixed_batch(), "mixed-type batch: 4096 GrC x4 + 1024 GoC x131 + 256 PC x1600 + IO 16x16 net x3"
     if name == "pkj3x3":
@@ -231,6 +236,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="population fraction of the mixed batch (small profiling cases; 1 = the benchmark)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -242,7 +249,7 @@ def main():
     import torch
     import gbrkc as G
     import configs
-    specs, wl = workload(args.config)
+    specs, wl = workload(args.config, args.scale)
     eng = G.Engine(G.MIXED if precision == "mixed" else G.FP64)
     configs.add_to(eng, specs)
     t_setup = time.perf_counter()
@@ -411,7 +418,8 @@ def main():
                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                           "setup_s": round(setup_s, 2), "wall_s": round(wall, 3),
                           "retired_systems": eng.retired(),
-                          "sim_ms_per_wall_s": args.steps * args.step_ms / (t_max_ms * 1e-3)},
+                          "sim_ms_per_wall_s": args.steps * args.step_ms / (t_max_ms * 1e-3),
+                          "units_per_step": units / args.steps},
                "roofline": roofline, "gpu_launches": launches, "clocks": clk}
         if e2e:
             out["e2e"] = e2e
