@@ -25,6 +25,7 @@
 #include "engine.h"
 #include "host_init.h"
 #include "model.h"
+#include "noalloc.h"
 
 namespace gbrkc {
 
@@ -1309,5 +1310,116 @@ extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) 
   CUDA_TRY(cudaMemcpy(all.data(), P->d_soma, all.size() * sizeof(double), cudaMemcpyDeviceToHost));
   for (int k = 0; k < n_iv; k++)
     for (int c = 0; c < S->n; c++) host[(size_t)k * S->n + c] = all[(size_t)k * P->ncell + c0 + c];
+  return 0;
+}
+
+// ------------------------------------------------- gbrkc_advance_noalloc
+// gbrkc_advance without any allocation: the persistent launch's work-queue
+// counters and per-CTA timestamps come from the static scratch of
+// noalloc.cu, host-side buffers are fixed-size locals, and the stopped-system
+// check reads the status words with one strided copy per pool chunk.
+namespace {
+
+template <typename R>
+int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, unsigned long long *scratch) {
+  MegaView<R> M{};
+  int end = 0;
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    M.pool[t] = P.systems.empty() ? PoolView<R>{} : pool_view<R>(P);
+    end += E->role_ctas[t];
+    M.role_end[t] = end;
+  }
+  if (end > NOALLOC_MAX_CTAS)
+    return fail(GBRKC_EINVAL, "persistent launch of %d CTAs exceeds the static scratch (%d CTAs)", end,
+                NOALLOC_MAX_CTAS);
+  M.gr_nc4 = E->pools[GR].team == TEAM_LANE4;
+  M.lane_warps = 0;
+  M.lane_extra = 0;
+  if (E->role_ctas[GR] > 0) {
+    M.lane_warps = E->gr_warps / E->role_ctas[GR];
+    M.lane_extra = E->gr_warps % E->role_ctas[GR];
+    if (M.lane_warps + (M.lane_extra > 0) > MEGA_BLOCK / 32)
+      return fail(GBRKC_ESTATE, "persistent launch: %d granule warps do not fit %d CTAs", E->gr_warps,
+                  E->role_ctas[GR]);
+  }
+  if (E->role_ctas[GR] > 0 &&
+      (!E->pools[GR].ws_in_smem ||
+       E->mega_smem < (size_t)MEGA_BLOCK * (size_t)E->pools[GR].ws_tile * sizeof(double)))
+    return fail(GBRKC_ESTATE, "persistent launch: granule workspaces do not fit its shared memory");
+  M.queue = (int *)scratch;
+  M.t_start = scratch + NOALLOC_QUEUE_WORDS;
+  M.t_end = scratch + NOALLOC_QUEUE_WORDS + NOALLOC_MAX_CTAS;
+  cudaStream_t st = E->streams[0];
+  // the counters must start at zero; the stamps are all rewritten
+  CUDA_TRY(cudaMemsetAsync(M.queue, 0, NOALLOC_QUEUE_WORDS * sizeof(unsigned long long), st));
+  CUDA_TRY(cudaEventRecord(E->ev_start, st));
+  int rc = launch_mega<R>(M, end, E->mega_smem, st, t0, n_iv, iv0, 0);
+  if (rc) return fail(GBRKC_ECUDA, "persistent launch: %s", cudaGetErrorString((cudaError_t)rc));
+  CUDA_TRY(cudaEventRecord(E->ev_end, st));
+  CUDA_TRY(cudaEventSynchronize(E->ev_end));
+  CUDA_TRY(cudaEventElapsedTime(&E->last_ms, E->ev_start, E->ev_end));
+  unsigned long long ts[NOALLOC_MAX_CTAS], te[NOALLOC_MAX_CTAS];
+  CUDA_TRY(cudaMemcpy(ts, M.t_start, end * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(te, M.t_end, end * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  unsigned long long t_first = ~0ull;
+  for (int b = 0; b < end; b++) t_first = std::min(t_first, ts[b]);
+  double role_ms[NTYPES] = {};
+  int b = 0;
+  for (int t = 0; t < NTYPES; t++) {
+    unsigned long long last = t_first;
+    for (int k = 0; k < E->role_ctas[t]; k++, b++) last = std::max(last, te[b]);
+    role_ms[t] = E->role_ctas[t] ? (double)(last - t_first) * 1e-6 : 0.0;
+    E->last_kernel_ms[t] = (float)role_ms[t];
+  }
+  if (n_iv > 0) rebalance_roles(E, role_ms, true);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int gbrkc_advance_noalloc(gbrkc_engine *E, double t0, int n_iv) {
+  if (!E || n_iv < 0) return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  const int iv0 = E->soma_iv;
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    double *so = (E->soma_cap > 0 && iv0 + n_iv <= E->soma_cap) ? P.d_soma : nullptr;
+    P.vd.soma_out = so;
+    P.vf.soma_out = so;
+  }
+  int rc;
+  if (E->mega) {
+    unsigned long long *scratch = nullptr;
+    rc = noalloc_scratch(&scratch);
+    if (rc) return fail(GBRKC_ECUDA, "static scratch: %s", cudaGetErrorString((cudaError_t)rc));
+    rc = (E->precision == GBRKC_FP64) ? launch_mega_static<double>(E, t0, n_iv, iv0, scratch)
+                                      : launch_mega_static<float>(E, t0, n_iv, iv0, scratch);
+  } else {
+    // one launch per pool: those kernels use no scratch beyond the engine's state
+    rc = launch_all(E, t0, n_iv, iv0, 0);
+  }
+  if (rc) return rc;
+  if (E->soma_cap > 0) E->soma_iv += n_iv;
+  // stopped systems: their status words, read in chunks with a strided copy
+  int stopped = 0, first_id = -1, first_status = 0;
+  constexpr int CHUNK = 512;
+  int status[CHUNK];
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    const int nsys = (int)P.systems.size();
+    for (int i0 = 0; i0 < nsys; i0 += CHUNK) {
+      const int cnt = std::min(CHUNK, nsys - i0);
+      CUDA_TRY(cudaMemcpy2D(status, sizeof(int), (const char *)(P.d_ctl + i0) + offsetof(Ctl, status), sizeof(Ctl),
+                            sizeof(int), cnt, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < cnt; i++)
+        if (status[i]) {
+          if (!stopped++) { first_id = P.systems[i0 + i]; first_status = status[i]; }
+        }
+    }
+  }
+  if (stopped)
+    return fail(GBRKC_ESOLVER, "%d system(s) are stopped (first: system %d, status %d); the others advanced", stopped,
+                first_id, first_status);
   return 0;
 }

@@ -48,6 +48,7 @@ def lib() -> C.CDLL:
         L.gbrkc_add_system.argtypes = [P, C.POINTER(SystemDesc), C.POINTER(C.c_int)]
         L.gbrkc_build.argtypes = [P]
         L.gbrkc_advance.argtypes = [P, C.c_double, C.c_int]
+        L.gbrkc_advance_noalloc.argtypes = [P, C.c_double, C.c_int]
         L.gbrkc_read.argtypes = [P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_long]
         L.gbrkc_system_ctl.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                        C.POINTER(C.c_int)]
@@ -155,6 +156,15 @@ class Engine:
         retired (the others continue); that raises unless tolerate_retire."""
         rc = lib().gbrkc_advance(self.h, t0, n_intervals)
         if rc == -5 and tolerate_retire:
+            return
+        _check(rc)
+
+    def advance_noalloc(self, t0: float, n_intervals: int, tolerate_stopped: bool = False):
+        """advance() through gbrkc_advance_noalloc: no device or host
+        allocation during the call (launch scratch in static device memory).
+        Raises while any system is stopped, unless tolerate_stopped."""
+        rc = lib().gbrkc_advance_noalloc(self.h, t0, n_intervals)
+        if rc == -5 and tolerate_stopped:
             return
         _check(rc)
 

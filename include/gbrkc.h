@@ -127,6 +127,31 @@ float gbrkc_last_kernel_ms(gbrkc_engine *e, int cell_type);
  * its own launch (entries -1), negative on error. */
 int gbrkc_launch_layout(gbrkc_engine *e, int *ctas_per_type);
 
+/* gbrkc_advance for callers that must not trigger a device allocation
+ * while they step: for example a host already running other GPU work under
+ * its own memory allocator, whose budget or pool a library cudaMalloc would
+ * break into, or a real-time stepping loop that cannot take the device-wide
+ * synchronisation a cudaMalloc / cudaFree may impose.  This call makes no
+ * device allocation of any kind, and on success no host allocation either
+ * (only an error message is stored as a string).  The persistent launch's
+ * scratch -- per-role work-queue counters and per-CTA timestamps -- comes
+ * from one fixed array in the library's static device memory, sized for
+ * launches of at most 1024 CTAs (16.6 KB, held on every GPU that loads the
+ * library until the process exits); a larger launch is rejected with
+ * GBRKC_EINVAL.  Engines advanced one pool per launch need no scratch and
+ * take the same path as gbrkc_advance.
+ *   - The first call on a device looks the array's address up; make that
+ *     first call before any stream capture.
+ *   - Every call shares the one array: calls whose work overlaps on the GPU
+ *     (e.g. two host threads advancing two engines at once) race on it and
+ *     corrupt each other's scheduling.  Serialise them.
+ *   - Results are the same as gbrkc_advance's, bit for bit.  Unlike it, this
+ *     call does not update gbrkc_retired_systems; it returns GBRKC_ESOLVER
+ *     whenever any system of the engine is stopped (the others advance).
+ * The engine itself is still allocated by gbrkc_build.  No counterpart in
+ * the reference (it allocates through cudaMalloc at initialisation only). */
+int gbrkc_advance_noalloc(gbrkc_engine *e, double t0, int n_intervals);
+
 /* Device address of one system's per-compartment array (GBRKC_F_VNEW, _V,
  * _CA, _REV or _IEXT; nc doubles, the system's compartments in order).  Valid
  * until the engine is destroyed; the array is written by gbrkc_advance and may
