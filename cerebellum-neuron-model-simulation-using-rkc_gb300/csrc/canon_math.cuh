@@ -17,10 +17,12 @@
  *        plus e ln2 with the same two-part ln2.
  *   pow: exp(y log x) for x >= 0.
  *
- * Accuracy against the correctly rounded result is within a few ulp.  The
- * oracle carries an independent host copy of the same algorithm; a GPU test
- * checks device and host agree bit for bit.  Every fma here is explicit; the
- * translation units that include this file are built with -fmad=false.
+ * Measured error against the exact result: exp within 0.76 ulp, log within
+ * 1.8 ulp, pow(x, 1/3) within 7 ulp.  The oracle carries an independent host
+ * copy of the same algorithm; the GPU parity tests, bit-exact through whole
+ * trajectories, check that device and host agree.  Every fma here is
+ * explicit; the translation units that include this file are built with
+ * -fmad=false.
  */
 #ifndef GBRKC_CANON_MATH_CUH
 #define GBRKC_CANON_MATH_CUH

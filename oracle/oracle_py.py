@@ -67,6 +67,11 @@ def lib() -> C.CDLL:
         L.orc_ctl.argtypes = [P, C.POINTER(C.c_double)]
         L.orc_stats.argtypes = [P, C.POINTER(C.c_longlong)]
         L.orc_pivot_swaps.restype = C.c_longlong
+        for f in ("orc_cm_exp", "orc_cm_log"):
+            getattr(L, f).restype = C.c_double
+            getattr(L, f).argtypes = [C.c_double]
+        L.orc_cm_pow.restype = C.c_double
+        L.orc_cm_pow.argtypes = [C.c_double, C.c_double]
         L.orc_ion_update.argtypes = [P, C.POINTER(C.c_double), C.c_double]
         L.orc_update_b.argtypes = [P, C.POINTER(C.c_double)]
         L.orc_set_elem_v.argtypes = [P, C.POINTER(C.c_double)]
@@ -90,6 +95,18 @@ def draw_jitter(cell_type: int, n: int) -> np.ndarray:
     out = np.zeros(n, dtype=np.float64)
     lib().orc_draw_jitter(cell_type, n, _dp(out))
     return out
+
+
+def cm_exp(x: float) -> float:
+    return lib().orc_cm_exp(x)
+
+
+def cm_log(x: float) -> float:
+    return lib().orc_cm_log(x)
+
+
+def cm_pow(x: float, y: float) -> float:
+    return lib().orc_cm_pow(x, y)
 
 
 def pivot_swaps() -> int:

@@ -406,6 +406,11 @@ static double go_hs2_tau(double v) { return (EXP((0.015 * v + 5.3) * 2.3)); }
 static long long g_pivot_swaps = 0;
 long long orc_pivot_swaps(void) { return g_pivot_swaps; }
 
+/* the canonical exp / log / pow, exported for tests/test_canon_math.py */
+double orc_cm_exp(double x) { return cm_exp(x); }
+double orc_cm_log(double x) { return cm_log(x); }
+double orc_cm_pow(double x, double y) { return cm_pow(x, y); }
+
 static int pivot_solve(int n, double *A /* n*n row-major */, double *bvec) {
   for (int i = 0; i < n - 1; i++) {
     int piv = i;

@@ -78,6 +78,10 @@ void orc_ctl(const orc_sys *s, double *out8);
 void orc_stats(const orc_sys *s, long long *out6);
 /* Row swaps taken by the Na / KAHP Markov solvers so far (process-wide). */
 long long orc_pivot_swaps(void);
+/* The canonical exp / log / pow of canon_math.h. */
+double orc_cm_exp(double x);
+double orc_cm_log(double x);
+double orc_cm_pow(double x, double y);
 
 /* static setup, for the setup pins: Cm, area, cond k, shell, CSR */
 const double *orc_cm(const orc_sys *s);
