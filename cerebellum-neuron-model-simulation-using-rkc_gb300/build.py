@@ -32,7 +32,7 @@ CXX = os.environ.get("CXX", "g++")
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
             f"-I{CUDA_HOME}/include", f"-I{os.path.join(ROOT, 'include')}"]
 
-KERNEL_TUS = ["kernels_fp64.cu", "kernels_fp32.cu", "compat.cu", "noalloc.cu"]
+KERNEL_TUS = ["kernels_fp64.cu", "kernels_fp32.cu", "compat.cu", "noalloc.cu", "synapse.cu"]
 TU_FLAGS = {"kernels_fp32.cu": ["-prec-div=false"]}
 HOST_TUS = ["engine.cpp", "host_init.cpp"]
 

@@ -427,6 +427,14 @@ struct gbrkc_engine {
   double role_work[NTYPES] = {};  // smoothed CTA-ms per role
   int *d_queue = nullptr;
   unsigned long long *d_tstart = nullptr, *d_tend = nullptr;
+  // chemical synapses (network mode), as added
+  struct {
+    std::vector<int> kind, grp, pre_sys, pre_comp, post_sys, post_comp;
+    std::vector<double> w, grp_rate;
+    std::vector<unsigned long long> grp_seed;
+  } syn;
+  SynView sv{};
+  long long syn_interval = 0;   // intervals advanced in network mode (Poisson counter)
   ~gbrkc_engine() {
     for (auto &s : streams)
       if (s) cudaStreamDestroy(s);
@@ -1005,6 +1013,164 @@ int setup_mega(gbrkc_engine *E) {
 
 }  // namespace
 
+namespace {
+
+// Resolve every synapse to pool compartments, index the synapses of each
+// pool by post compartment in (kind, id) order, and upload the tables.
+int build_synapses(gbrkc_engine *E) {
+  const int n = (int)E->syn.kind.size();
+  if (n == 0) return 0;
+  // reversal potentials, syn.cuh:13,20,31,38 (E_MFGR, E_GRGO, E_GOGR, E_GRPKJ)
+  static const double E_KIND[SYN_KINDS] = {0.0, 0.0, -82.0, 0.0};
+  // decay per state, exp(-RKC_DT / tau): syn.cuh:14-15, 21-23, 32-33, 40
+  static const double TAU[8] = {1.2, 52.0, 1.5, 31.0, 170.0, 7.0, 59.0, 6.0};
+  std::vector<int> pre_type(n, -1), post_type(n);
+  std::vector<long> pre_gi(n, 0), post_gi(n);
+  std::vector<double> e(n), zero(n, 0.0), old_v(n, 1000.0);  // old_v starts at 1000 (syn.cu:176,330,510)
+  for (int i = 0; i < n; i++) {
+    const HostSystem &Q = E->systems[E->syn.post_sys[i]];
+    post_type[i] = Q.type;
+    post_gi[i] = E->pools[Q.type].sys_off[Q.pool_index] + E->syn.post_comp[i];
+    if (E->syn.kind[i] != SYN_MFGR) {
+      const HostSystem &S = E->systems[E->syn.pre_sys[i]];
+      pre_type[i] = S.type;
+      pre_gi[i] = E->pools[S.type].sys_off[S.pool_index] + E->syn.pre_comp[i];
+    }
+    e[i] = E_KIND[E->syn.kind[i]];
+  }
+  DeviceMem &M = E->mem;
+  int rc = 0;
+  double *d_e = nullptr, *d_val = nullptr;
+  SynView &V = E->sv;
+  V.n = n;
+  {
+    int *p;
+    if ((rc = M.upload(E->syn.kind, &p))) return rc;
+    V.kind = p;
+    if ((rc = M.upload(E->syn.grp, &p))) return rc;
+    V.grp = p;
+    if ((rc = M.upload(pre_type, &p))) return rc;
+    V.pre_type = p;
+    long *q;
+    if ((rc = M.upload(pre_gi, &q))) return rc;
+    V.pre_gi = q;
+    double *d;
+    if ((rc = M.upload(E->syn.w, &d))) return rc;
+    V.w = d;
+    if ((rc = M.upload(zero, &V.s0))) return rc;
+    if ((rc = M.upload(zero, &V.s1))) return rc;
+    if ((rc = M.upload(zero, &V.s2))) return rc;
+    if ((rc = M.upload(zero, &d_val))) return rc;
+    V.val = d_val;
+    if ((rc = M.upload(old_v, &V.old_v))) return rc;
+    if ((rc = M.upload(e, &d_e))) return rc;
+    if ((rc = M.upload(E->syn.grp_rate, &d))) return rc;
+    V.grp_rate = d;
+    unsigned long long *u;
+    if ((rc = M.upload(E->syn.grp_seed, &u))) return rc;
+    V.grp_seed = u;
+  }
+  for (int k = 0; k < 8; k++) V.decay[k] = exp(-0.125 / TAU[k]);
+  for (int t = 0; t < NTYPES; t++) V.pre_v[t] = E->pools[t].d_v;
+  // per pool: CSR over post compartments
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty()) continue;
+    std::vector<int> ids;
+    for (int i = 0; i < n; i++)
+      if (post_type[i] == t) ids.push_back(i);
+    if (ids.empty()) continue;
+    std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) {
+      if (post_gi[a] != post_gi[b]) return post_gi[a] < post_gi[b];
+      if (E->syn.kind[a] != E->syn.kind[b]) return E->syn.kind[a] < E->syn.kind[b];
+      return a < b;
+    });
+    std::vector<int> row(P.nc + 1, 0);
+    for (int i : ids) row[post_gi[i] + 1]++;
+    for (long c = 0; c < P.nc; c++) row[c + 1] += row[c];
+    std::vector<double> buf(P.nc, 0.0);
+    int *d_row = nullptr, *d_idx = nullptr;
+    double *d_buf = nullptr;
+    if ((rc = M.upload(row, &d_row))) return rc;
+    if ((rc = M.upload(ids, &d_idx))) return rc;
+    if ((rc = M.upload(buf, &d_buf))) return rc;
+    const int mode = (t == GR) ? SYN_AT_ION : (t == GO) ? SYN_BUFFERED : (t == PKJ) ? SYN_BUFFERED_DECAY : SYN_NONE;
+    if (mode == SYN_NONE) return fail(GBRKC_EINVAL, "synapses onto pool %d are not supported", t);
+    P.vd.syn_mode = P.vf.syn_mode = mode;
+    P.vd.syn_row = P.vf.syn_row = d_row;
+    P.vd.syn_idx = P.vf.syn_idx = d_idx;
+    P.vd.syn_val = P.vf.syn_val = d_val;
+    P.vd.syn_e = P.vf.syn_e = d_e;
+    P.vd.syn_buf = P.vf.syn_buf = d_buf;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int gbrkc_add_synapses(gbrkc_engine *E, const gbrkc_synapse_desc *d, int *first_id) {
+  if (!E || !d) return fail(GBRKC_EINVAL, "null argument");
+  if (E->built) return fail(GBRKC_ESTATE, "synapses must be added before gbrkc_build");
+  if (d->kind < 0 || d->kind >= SYN_KINDS) return fail(GBRKC_EINVAL, "bad synapse kind %d", d->kind);
+  if (d->n < 0) return fail(GBRKC_EINVAL, "bad synapse count");
+  if (d->n > 0 && (!d->post_system || !d->post_comp || !d->weight)) return fail(GBRKC_EINVAL, "missing arrays");
+  const bool poisson = d->kind == SYN_MFGR;
+  if (d->n > 0 && !poisson && (!d->pre_system || !d->pre_comp)) return fail(GBRKC_EINVAL, "missing presynaptic arrays");
+  // expected (pre, post) cell types per kind
+  static const int PRE[SYN_KINDS] = {-1, GR, GO, GR}, POST[SYN_KINDS] = {GR, GO, GR, PKJ};
+  const int nsys = (int)E->systems.size();
+  for (int i = 0; i < d->n; i++) {
+    const int q = d->post_system[i];
+    if (q < 0 || q >= nsys || E->systems[q].type != POST[d->kind] || d->post_comp[i] < 0 ||
+        d->post_comp[i] >= E->systems[q].nc)
+      return fail(GBRKC_EINVAL, "synapse %d: bad postsynaptic system or compartment", i);
+    if (!poisson) {
+      const int p = d->pre_system[i];
+      if (p < 0 || p >= nsys || E->systems[p].type != PRE[d->kind] || d->pre_comp[i] < 0 ||
+          d->pre_comp[i] >= E->systems[p].nc)
+        return fail(GBRKC_EINVAL, "synapse %d: bad presynaptic system or compartment", i);
+    }
+  }
+  const int grp = (int)E->syn.grp_seed.size();
+  if (first_id) *first_id = (int)E->syn.kind.size();
+  for (int i = 0; i < d->n; i++) {
+    E->syn.kind.push_back(d->kind);
+    E->syn.grp.push_back(grp);
+    E->syn.pre_sys.push_back(poisson ? -1 : d->pre_system[i]);
+    E->syn.pre_comp.push_back(poisson ? 0 : d->pre_comp[i]);
+    E->syn.post_sys.push_back(d->post_system[i]);
+    E->syn.post_comp.push_back(d->post_comp[i]);
+    E->syn.w.push_back(d->weight[i]);
+  }
+  // mossy-fibre rates: 5 Hz, 60 Hz for S_Stimuli <= t < E_Stimuli (syn.cu:93-95,
+  // param.h:8-9) unless the group gives its own
+  const bool deflt = d->rate_base == 0.0 && d->rate_stim == 0.0 && d->stim_t0 == 0.0 && d->stim_t1 == 0.0;
+  E->syn.grp_rate.push_back(deflt ? 5.0 : d->rate_base);
+  E->syn.grp_rate.push_back(deflt ? 60.0 : d->rate_stim);
+  E->syn.grp_rate.push_back(deflt ? 900.0 : d->stim_t0);
+  E->syn.grp_rate.push_back(deflt ? 1000.0 : d->stim_t1);
+  E->syn.grp_seed.push_back(d->seed);
+  return 0;
+}
+
+extern "C" int gbrkc_read_synapses(gbrkc_engine *E, int field, double *host, long n) {
+  if (!E || !host) return fail(GBRKC_EINVAL, "null argument");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  if (n < 0 || n > E->sv.n) return fail(GBRKC_EINVAL, "bad count");
+  const double *src = nullptr;
+  switch (field) {
+    case GBRKC_SYNF_VAL: src = E->sv.val; break;
+    case GBRKC_SYNF_S0: src = E->sv.s0; break;
+    case GBRKC_SYNF_S1: src = E->sv.s1; break;
+    case GBRKC_SYNF_S2: src = E->sv.s2; break;
+    case GBRKC_SYNF_OLD_V: src = E->sv.old_v; break;
+    default: return fail(GBRKC_EINVAL, "bad synapse field");
+  }
+  if (n == 0) return 0;
+  CUDA_TRY(cudaMemcpy(host, src, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
 extern "C" int gbrkc_build(gbrkc_engine *E) {
   if (!E) return fail(GBRKC_EINVAL, "null engine");
   if (E->built) return fail(GBRKC_ESTATE, "already built");
@@ -1043,6 +1209,10 @@ extern "C" int gbrkc_build(gbrkc_engine *E) {
     if (!rc) rc = E->mem.upload(z, &E->d_tend);
     if (rc) return rc;
   }
+  {
+    int rc = build_synapses(E);
+    if (rc) return rc;
+  }
   E->built = true;
   int rc = launch_all(E, 0.0, 0, 0, 1);
   if (rc) { E->built = false; return rc; }
@@ -1059,7 +1229,20 @@ extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
     P.vd.soma_out = so;
     P.vf.soma_out = so;
   }
-  int rc = launch_all(E, t0, n_iv, iv0, 0);
+  int rc = 0;
+  if (E->sv.n > 0) {
+    // network mode: every system advances one interval, then the synapses
+    // update from the new presynaptic voltages (main.cu:196-305)
+    for (int k = 0; k < n_iv && !rc; k++) {
+      rc = launch_all(E, t0 + k * H_MAX, 1, iv0 + k, 0);
+      if (rc) break;
+      rc = launch_syn_update(E->sv, E->streams[0], t0 + k * H_MAX, E->syn_interval++);
+      if (rc) return fail(GBRKC_ECUDA, "synapse update: %s", cudaGetErrorString((cudaError_t)rc));
+      CUDA_TRY(cudaStreamSynchronize(E->streams[0]));
+    }
+  } else {
+    rc = launch_all(E, t0, n_iv, iv0, 0);
+  }
   if (rc) return rc;
   if (E->soma_cap > 0) E->soma_iv += n_iv;
   // A system that stops (non-finite step, loop bound) is retired: it keeps
@@ -1381,6 +1564,7 @@ int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, unsigned l
 extern "C" int gbrkc_advance_noalloc(gbrkc_engine *E, double t0, int n_iv) {
   if (!E || n_iv < 0) return fail(GBRKC_EINVAL, "bad arguments");
   if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  if (E->sv.n > 0) return fail(GBRKC_EINVAL, "engines with synapses step through gbrkc_advance");
   const int iv0 = E->soma_iv;
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];

@@ -88,7 +88,44 @@ struct PoolView {
   int ncell_pool;
   int ws_in_smem;                     // stage the workspace in shared memory
   long ws_tile_doubles;               // shared-memory workspace per team
+  // chemical synapses onto this pool (network mode; syn_mode 0 = none)
+  int syn_mode;                       // SYN_AT_ION, SYN_BUFFERED or SYN_BUFFERED_DECAY
+  const int *syn_row;                 // [stride + 1] CSR over post compartments
+  const int *syn_idx;                 // synapse ids, per compartment in (kind, id) order
+  const double *syn_val;              // per synapse: conductance value (engine-wide table)
+  const double *syn_e;                // per synapse: reversal potential
+  double *syn_buf;                    // [stride] synaptic current taken at interval start
 };
+
+// How a pool takes its synaptic current (solve_rkc.cu): granule cells add
+// every synapse's g (V_y - E) to b at each ion update (add_mfgr_val,
+// add_gogr_val, 1100-1120); Golgi cells take the sum at the start of the
+// interval and add it at each ion update (add_grgo_val_new +
+// go_update_matrix_new, 1199-1200, 1180); Purkinje cells likewise, scaled by
+// exp(-sum_dt / 0.6) (add_grpkj_val_new + pkj_update_matrix_new, 1266-1269,
+// 1247-1250).
+enum SynMode { SYN_NONE = 0, SYN_AT_ION = 1, SYN_BUFFERED = 2, SYN_BUFFERED_DECAY = 3 };
+
+// Synapse kinds of the reference's RKC network path (syn.cu) and their
+// per-synapse state: MF->GrC (AMPA, NMDA), GrC->GoC (AMPA, NMDA1, NMDA2),
+// GoC->GrC (GABA_A, GABA_B), GrC->PC (AMPA).
+enum SynKind { SYN_MFGR = 0, SYN_GRGO = 1, SYN_GOGR = 2, SYN_GRPKJ = 3, SYN_KINDS = 4 };
+
+// The engine-wide synapse table for the per-interval update kernel.
+struct SynView {
+  int n;
+  const int *kind, *grp;
+  const int *pre_type;                // pool of the presynaptic compartment (-1: Poisson input)
+  const long *pre_gi;                 // presynaptic compartment, pool index
+  const double *w;
+  double *s0, *s1, *s2, *val, *old_v;
+  const double *pre_v[NTYPES];        // elem v of every pool
+  const double *grp_rate;             // per group: base rate, stimulus rate [Hz], window t0, t1 [ms]
+  const unsigned long long *grp_seed;
+  double decay[8];                    // exp(-RKC_DT / tau) per state, in SynKind order
+};
+
+int launch_syn_update(const SynView &S, void *stream, double t, long long interval);
 
 // Team shapes the kernels are instantiated for: one thread (tiny cells, 32
 // systems per warp, blocks of MEGA_BLOCK threads with interleaved shared

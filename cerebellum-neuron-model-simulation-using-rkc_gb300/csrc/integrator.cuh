@@ -91,12 +91,12 @@ constexpr int RHO_ITMAX = 1000;              // solve_rkc.cu:572
 enum Tick { TICK_DONE = 0, TICK_MORE = 1, TICK_ION = 2 };
 constexpr int ION_WAIT_MAX = 12;             // warp iterations a due ion update may wait
 
-// One compartment's ion update (when update_ion) and its current term b
-// (*_update_ion* and *_update_matrix of the reference), at pool compartment gi
-// with stage voltage vyi.
+// One compartment's ion update (when update_ion) and its channel current
+// term b (*_update_ion* and *_update_matrix of the reference), at pool
+// compartment gi with stage voltage vyi.
 template <int CT, typename R>
-__device__ __forceinline__ double comp_ion_b(const PoolView<R> &P, long gi, double vyi, double sum_dt,
-                                            bool update_ion) {
+__device__ __forceinline__ double comp_ion_b_cell(const PoolView<R> &P, long gi, double vyi, double sum_dt,
+                                                 bool update_ion) {
   const Slots<R> sl{P.ion, P.cond, P.stride, gi};
   if (CT == PKJ) {
     if (update_ion) {
@@ -130,6 +130,38 @@ __device__ __forceinline__ double comp_ion_b(const PoolView<R> &P, long gi, doub
     }
     return (double)Go<R>::b(sl, vyi, P.iext[gi], P.rev[gi]);
   }
+}
+
+// The synaptic current of compartment gi added to its b at an ion update
+// (network mode), in the reference's expressions: b += g (V_y - E) per
+// synapse for granule cells, b += the interval-start sum for Golgi cells,
+// b += that sum * exp(-sum_dt / 0.6) for Purkinje cells (solve_rkc.cu:
+// 201-224, 259-282, 348-360).  Synapses are added one by one in (kind, id)
+// order; the reference's atomics leave that order open.
+template <typename R>
+__device__ __forceinline__ double syn_add(const PoolView<R> &P, long gi, double vyi, double sum_dt, double bi) {
+  if (P.syn_mode == SYN_AT_ION) {
+    for (int k = P.syn_row[gi]; k < P.syn_row[gi + 1]; k++) {
+      const int s = P.syn_idx[k];
+      bi = bi + P.syn_val[s] * (vyi - P.syn_e[s]);
+    }
+  } else if (P.syn_mode == SYN_BUFFERED) {
+    bi = bi + P.syn_buf[gi];
+  } else if (P.syn_mode == SYN_BUFFERED_DECAY) {
+    bi = bi + P.syn_buf[gi] * mexp(-sum_dt / 0.6);
+  }
+  return bi;
+}
+
+// comp_ion_b_cell plus, at an ion update, the synaptic current (the
+// reference's *_update_ion_and_matrix); initialisation (update_ion false)
+// takes the channel current alone, as RKC_vec_initialize does.
+template <int CT, typename R>
+__device__ __forceinline__ double comp_ion_b(const PoolView<R> &P, long gi, double vyi, double sum_dt,
+                                            bool update_ion) {
+  double bi = comp_ion_b_cell<CT, R>(P, gi, vyi, sum_dt, update_ion);
+  if (update_ion && P.syn_mode != SYN_NONE) bi = syn_add(P, gi, vyi, sum_dt, bi);
+  return bi;
 }
 
 template <int CT, typename R, class Team>
@@ -617,6 +649,22 @@ struct Sys {
           P.iext[gi] = 0;
           if (P.stim_t0[pc] <= t && t < P.stim_t1[pc]) P.iext[gi] = P.stim_amp[pc];
         }
+      }
+      tm.sync();
+    }
+    // Golgi / Purkinje synaptic current taken at the interval's start, before
+    // the pending ion update (go_solve_by_rkc 1199-1200, pkj_solve_by_rkc
+    // 1266-1269): sum of g (V_y - E) from zero, synapse by synapse
+    if (P.syn_mode == SYN_BUFFERED || P.syn_mode == SYN_BUFFERED_DECAY) {
+      const V vy = vec(LY);
+      for (int i = tm.rank(); i < nc; i += tm.size()) {
+        const long gi = off + i;
+        double acc = 0.0;
+        for (int k = P.syn_row[gi]; k < P.syn_row[gi + 1]; k++) {
+          const int sid = P.syn_idx[k];
+          acc = acc + P.syn_val[sid] * (vy[i] - P.syn_e[sid]);
+        }
+        P.syn_buf[gi] = acc;
       }
       tm.sync();
     }

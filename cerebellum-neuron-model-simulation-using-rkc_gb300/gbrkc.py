@@ -33,6 +33,20 @@ class SystemDesc(C.Structure):
     ]
 
 
+class SynapseDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("n", C.c_int),
+        ("pre_system", C.POINTER(C.c_int)), ("pre_comp", C.POINTER(C.c_int)),
+        ("post_system", C.POINTER(C.c_int)), ("post_comp", C.POINTER(C.c_int)),
+        ("weight", C.POINTER(C.c_double)),
+        ("rate_base", C.c_double), ("rate_stim", C.c_double), ("stim_t0", C.c_double), ("stim_t1", C.c_double),
+        ("seed", C.c_ulonglong),
+    ]
+
+
+SYN_MFGR, SYN_GRGO, SYN_GOGR, SYN_GRPKJ = 0, 1, 2, 3
+SYNF_VAL, SYNF_S0, SYNF_S1, SYNF_S2, SYNF_OLD_V = 0, 1, 2, 3, 4
+
 _LIB = None
 
 
@@ -49,6 +63,8 @@ def lib() -> C.CDLL:
         L.gbrkc_build.argtypes = [P]
         L.gbrkc_advance.argtypes = [P, C.c_double, C.c_int]
         L.gbrkc_advance_noalloc.argtypes = [P, C.c_double, C.c_int]
+        L.gbrkc_add_synapses.argtypes = [P, C.POINTER(SynapseDesc), C.POINTER(C.c_int)]
+        L.gbrkc_read_synapses.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.c_long]
         L.gbrkc_read.argtypes = [P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_long]
         L.gbrkc_system_ctl.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
                                        C.POINTER(C.c_int)]
@@ -146,6 +162,36 @@ class Engine:
         self._keep.append(keep)
         self.ncomp[sid.value] = (cell_type, n, rows.shape[0])
         return sid.value
+
+    def add_synapses(self, kind, post_system, post_comp, weight, pre_system=None, pre_comp=None,
+                     rates=(0.0, 0.0, 0.0, 0.0), seed=0) -> int:
+        """Add one group of chemical synapses (GBRKC_SYN_*); returns the id of
+        its first synapse.  rates = (base Hz, stimulus Hz, t0 ms, t1 ms) for
+        mossy fibres (all 0: the reference's schedule)."""
+        post_system = np.ascontiguousarray(post_system, dtype=np.int32)
+        n = post_system.size
+        post_comp = np.ascontiguousarray(np.broadcast_to(post_comp, n), dtype=np.int32)
+        weight = np.ascontiguousarray(np.broadcast_to(weight, n), dtype=np.float64)
+        d = SynapseDesc()
+        d.kind, d.n = kind, n
+        d.post_system, d.post_comp, d.weight = _ip(post_system), _ip(post_comp), _dp(weight)
+        keep = [post_system, post_comp, weight]
+        if pre_system is not None:
+            pre_system = np.ascontiguousarray(np.broadcast_to(pre_system, n), dtype=np.int32)
+            pre_comp = np.ascontiguousarray(np.broadcast_to(pre_comp, n), dtype=np.int32)
+            d.pre_system, d.pre_comp = _ip(pre_system), _ip(pre_comp)
+            keep += [pre_system, pre_comp]
+        d.rate_base, d.rate_stim, d.stim_t0, d.stim_t1 = rates
+        d.seed = seed
+        first = C.c_int()
+        _check(lib().gbrkc_add_synapses(self.h, C.byref(d), C.byref(first)))
+        self._keep.append(keep)
+        return first.value
+
+    def read_synapses(self, field: int, n: int) -> np.ndarray:
+        out = np.empty(n, dtype=np.float64)
+        _check(lib().gbrkc_read_synapses(self.h, field, _dp(out), n))
+        return out
 
     def build(self):
         _check(lib().gbrkc_build(self.h))

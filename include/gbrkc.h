@@ -127,6 +127,52 @@ float gbrkc_last_kernel_ms(gbrkc_engine *e, int cell_type);
  * its own launch (entries -1), negative on error. */
 int gbrkc_launch_layout(gbrkc_engine *e, int *ctas_per_type);
 
+/* ---- chemical synapses (network mode) ----------------------------------
+ * The reference's RKC network path (syn.cu; main.cu:300-305 with
+ * network_sim true): mossy fibre -> granule (Poisson input), granule ->
+ * Golgi, Golgi -> granule and granule (parallel fibre) -> Purkinje.  Every
+ * 0.125 ms interval, all systems advance, then each synapse decays its
+ * states by exp(-0.125 / tau), steps them by one when its presynaptic
+ * compartment's voltage crossed 0 mV upward (or its Poisson fibre fired) and
+ * recomputes its conductance (syn.cu:86-111, 263-288, 412-437, 646-668).
+ * Granule cells add g (V - E) of each synapse to b at every ion update;
+ * Golgi and Purkinje cells take the synaptic current at the start of the
+ * interval and add it at each ion update, Purkinje cells scaled by
+ * exp(-sum_dt / 0.6) (solve_rkc.cu:198-360, 1100-1120, 1180-1270).
+ * The micro-circuit's inhibition onto Purkinje cells is absent from the
+ * reference's RKC path (never updated or applied) and is not provided.
+ * Poisson draws use a counter-based generator (seed, synapse, interval)
+ * instead of the reference's cuRAND streams.  Synapses make gbrkc_advance
+ * run one launch per interval. */
+enum { GBRKC_SYN_MFGR = 0, GBRKC_SYN_GRGO = 1, GBRKC_SYN_GOGR = 2, GBRKC_SYN_GRPKJ = 3 };
+/* per-synapse state readable with gbrkc_read_synapses */
+enum { GBRKC_SYNF_VAL = 0, GBRKC_SYNF_S0 = 1, GBRKC_SYNF_S1 = 2, GBRKC_SYNF_S2 = 3, GBRKC_SYNF_OLD_V = 4 };
+
+typedef struct gbrkc_synapse_desc {
+  int kind;                       /* GBRKC_SYN_* */
+  int n;                          /* synapses in this group */
+  const int *pre_system;          /* per synapse (unused for GBRKC_SYN_MFGR) */
+  const int *pre_comp;            /* presynaptic compartment within its system */
+  const int *post_system;         /* per synapse */
+  const int *post_comp;           /* postsynaptic compartment within its system */
+  const double *weight;           /* per synapse (the reference's W_* / count factors) */
+  double rate_base, rate_stim;    /* GBRKC_SYN_MFGR firing rates [Hz]: rate_stim for */
+  double stim_t0, stim_t1;        /*   stim_t0 <= t < stim_t1 [ms], else rate_base; all 0 = */
+                                  /*   the reference's 5 / 60 Hz over 900-1000 ms */
+  unsigned long long seed;        /* GBRKC_SYN_MFGR Poisson stream */
+} gbrkc_synapse_desc;
+
+/* Add a group of synapses between systems already added (before
+ * gbrkc_build); *first_id receives the id of its first synapse (ids are
+ * consecutive, in the engine-wide table).  Kinds fix the cell types:
+ * MFGR onto granule cells, GRGO granule -> Golgi, GOGR Golgi -> granule,
+ * GRPKJ granule -> Purkinje.  (mfgr_create, grgo_create, gogr_create,
+ * grpkj_create: syn.cu:63, 183, 336, 520) */
+int gbrkc_add_synapses(gbrkc_engine *e, const gbrkc_synapse_desc *d, int *first_id);
+
+/* Copy one per-synapse field (GBRKC_SYNF_*) of the first n synapses. */
+int gbrkc_read_synapses(gbrkc_engine *e, int field, double *host, long n);
+
 /* gbrkc_advance for callers that must not trigger a device allocation
  * while they step: for example a host already running other GPU work under
  * its own memory allocator, whose budget or pool a library cudaMalloc would
@@ -148,6 +194,7 @@ int gbrkc_launch_layout(gbrkc_engine *e, int *ctas_per_type);
  *   - Results are the same as gbrkc_advance's, bit for bit.  Unlike it, this
  *     call does not update gbrkc_retired_systems; it returns GBRKC_ESOLVER
  *     whenever any system of the engine is stopped (the others advance).
+ * Engines with synapses are refused (they step through gbrkc_advance).
  * The engine itself is still allocated by gbrkc_build.  No counterpart in
  * the reference (it allocates through cudaMalloc at initialisation only). */
 int gbrkc_advance_noalloc(gbrkc_engine *e, double t0, int n_intervals);

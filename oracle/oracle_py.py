@@ -67,6 +67,16 @@ def lib() -> C.CDLL:
         L.orc_ctl.argtypes = [P, C.POINTER(C.c_double)]
         L.orc_stats.argtypes = [P, C.POINTER(C.c_longlong)]
         L.orc_pivot_swaps.restype = C.c_longlong
+        L.orc_net_create.restype = P
+        L.orc_net_add_system.argtypes = [P, P]
+        L.orc_net_add_synapses.argtypes = [P, C.c_int, C.c_int] + [C.POINTER(C.c_int)] * 4 + [
+            C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double, C.c_double, C.c_ulonglong]
+        L.orc_net_build.argtypes = [P]
+        L.orc_net_advance.argtypes = [P, C.c_double]
+        L.orc_net_nsyn.argtypes = [P]
+        L.orc_net_syn.argtypes = [P, C.c_int]
+        L.orc_net_syn.restype = C.POINTER(C.c_double)
+        L.orc_net_destroy.argtypes = [P]
         for f in ("orc_cm_exp", "orc_cm_log"):
             getattr(L, f).restype = C.c_double
             getattr(L, f).argtypes = [C.c_double]
@@ -248,3 +258,48 @@ class System:
     def set_ca(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)
         lib().orc_set_ca(self.h, _dp(x))
+
+
+class Network:
+    """Oracle network mode: Systems advanced together with the reference's
+    chemical synapses (kinds 0..3: MF->GrC, GrC->GoC, GoC->GrC, GrC->PC).
+    Systems advance in the order added.  Test infrastructure."""
+
+    def __init__(self):
+        self.h = lib().orc_net_create()
+        self.systems = []
+        self._keep = []
+
+    def add_system(self, s) -> int:
+        self.systems.append(s)
+        return lib().orc_net_add_system(self.h, s.h)
+
+    def add_synapses(self, kind, post_system, post_comp, weight, pre_system=None, pre_comp=None,
+                     rates=(0.0, 0.0, 0.0, 0.0), seed=0) -> int:
+        post_system = np.ascontiguousarray(post_system, dtype=np.int32)
+        n = post_system.size
+        post_comp = np.ascontiguousarray(np.broadcast_to(post_comp, n), dtype=np.int32)
+        weight = np.ascontiguousarray(np.broadcast_to(weight, n), dtype=np.float64)
+        pre_system = np.ascontiguousarray(np.broadcast_to(-1 if pre_system is None else pre_system, n), dtype=np.int32)
+        pre_comp = np.ascontiguousarray(np.broadcast_to(0 if pre_comp is None else pre_comp, n), dtype=np.int32)
+        self._keep.append((post_system, post_comp, weight, pre_system, pre_comp))
+        return lib().orc_net_add_synapses(self.h, kind, n, _ip(pre_system), _ip(pre_comp), _ip(post_system),
+                                          _ip(post_comp), _dp(weight), *rates, seed)
+
+    def build(self):
+        if lib().orc_net_build(self.h) != 0:
+            raise RuntimeError("synapses onto an unsupported cell type")
+
+    def advance(self, t: float) -> int:
+        return lib().orc_net_advance(self.h, t)
+
+    def syn(self, field: int) -> np.ndarray:
+        n = lib().orc_net_nsyn(self.h)
+        p = lib().orc_net_syn(self.h, field)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+    def __del__(self):
+        try:
+            lib().orc_net_destroy(self.h)
+        except Exception:
+            pass

@@ -135,6 +135,14 @@ struct orc_sys {
   double *invcm, *scratch;
   /* counters */
   long long n_steps, n_rej, n_stage, n_rho, n_ion, n_rho_iter;
+  /* chemical synapses onto this system (network mode, set by orc_net_build):
+   * 1 = g (V_y - E) per synapse at each ion update (granule), 2 = the sum taken
+   * at interval start added at each ion update (Golgi), 3 = as 2 scaled by
+   * exp(-sum_dt / 0.6) (Purkinje) -- solve_rkc.cu:198-360, 1100-1120, 1180-1270 */
+  int syn_mode;
+  int *syn_row, *syn_idx;   /* CSR over compartments: synapse ids in (kind, id) order */
+  const double *syn_val, *syn_e;
+  double *syn_buf;
 };
 
 #define VEC(s, L) ((s)->phys[(s)->map[L]])
@@ -782,6 +790,19 @@ static void ion_and_matrix(orc_sys *s, double sum_dt) {
   orc_ion_update(s, vy, sum_dt);
   orc_update_b(s, vy);
   if (s->type == ORC_IO && s->ngap > 0) io_gap_apply(s);
+  /* add_mfgr_val / add_gogr_val, go_update_matrix_new, pkj_update_matrix_new */
+  if (s->syn_mode == 1) {
+    for (int id = 0; id < s->nc; id++)
+      for (int k = s->syn_row[id]; k < s->syn_row[id + 1]; k++) {
+        int q = s->syn_idx[k];
+        s->b[id] = s->b[id] + s->syn_val[q] * (vy[id] - s->syn_e[q]);
+      }
+  } else if (s->syn_mode == 2) {
+    for (int id = 0; id < s->nc; id++) s->b[id] = s->b[id] + s->syn_buf[id];
+  } else if (s->syn_mode == 3) {
+    double decay = EXP(-sum_dt / 0.6);
+    for (int id = 0; id < s->nc; id++) s->b[id] = s->b[id] + s->syn_buf[id] * decay;
+  }
   s->n_ion++;
 }
 
@@ -1184,6 +1205,7 @@ void orc_destroy(orc_sys *s) {
   free(s->stim_comp); free(s->stim_amp); free(s->stim_t0); free(s->stim_t1);
   free(s->gap_pre); free(s->gap_post); free(s->gap_cur); free(s->gap_g);
   free(s->invcm); free(s->scratch);
+  free(s->syn_row); free(s->syn_idx); free(s->syn_buf);
   free(s);
 }
 
@@ -1540,6 +1562,19 @@ static void set_current(orc_sys *s, double t) {
 int orc_advance(orc_sys *s, double t) {
   g_canon = s->canon;
   set_current(s, t);
+  /* Golgi / Purkinje: synaptic current at interval start, before the pending
+   * ion update (add_grgo_val_new 1199-1200, add_grpkj_val_new 1266-1269) */
+  if (s->syn_mode == 2 || s->syn_mode == 3) {
+    const double *vy = VEC(s, LY);
+    for (int id = 0; id < s->nc; id++) {
+      double acc = 0.0;
+      for (int k = s->syn_row[id]; k < s->syn_row[id + 1]; k++) {
+        int q = s->syn_idx[k];
+        acc = acc + s->syn_val[q] * (vy[id] - s->syn_e[q]);
+      }
+      s->syn_buf[id] = acc;
+    }
+  }
   /* GR and IO compare with '>', GO and PKJ with '>=' (solve_rkc.cu:1148,1212,1284,1347) */
   const int ge = (s->type == ORC_GO || s->type == ORC_PKJ);
   if (s->sum_dt != 0.0) {
@@ -1601,4 +1636,184 @@ void orc_draw_jitter(int type, int n, double *out) {
     else
       out[c] = ((double)rand() / RAND_MAX) - 0.5;
   }
+}
+
+/* ------------------------------------------------------------------ */
+/* network mode: systems plus the reference's chemical synapses         */
+/* (syn.cu; main.cu:196-305 with network_sim true)                      */
+/* ------------------------------------------------------------------ */
+enum { SYN_MFGR, SYN_GRGO, SYN_GOGR, SYN_GRPKJ, SYN_KINDS };
+
+struct orc_net {
+  int nsys;
+  orc_sys *sys[64];
+  int n, cap;
+  int *kind, *grp, *pre_sys, *pre_comp, *post_sys, *post_comp;
+  double *w, *s0, *s1, *s2, *val, *old_v, *e;
+  int ngrp;
+  double rate[64][4];
+  unsigned long long seed[64];
+  double decay[8];
+  long long interval;
+};
+
+orc_net *orc_net_create(void) {
+  orc_net *n = (orc_net *)calloc(1, sizeof(orc_net));
+  /* exp(-RKC_DT / tau), syn.cuh:14-15, 21-23, 32-33, 40 */
+  static const double tau[8] = {1.2, 52.0, 1.5, 31.0, 170.0, 7.0, 59.0, 6.0};
+  for (int k = 0; k < 8; k++) n->decay[k] = exp(-0.125 / tau[k]);
+  return n;
+}
+
+int orc_net_add_system(orc_net *n, orc_sys *s) {
+  if (n->nsys >= 64) return -1;
+  n->sys[n->nsys] = s;
+  return n->nsys++;
+}
+
+#define NET_GROW(f, T) n->f = (T *)realloc(n->f, (size_t)n->cap * sizeof(T))
+int orc_net_add_synapses(orc_net *n, int kind, int count, const int *pre_sys, const int *pre_comp,
+                         const int *post_sys, const int *post_comp, const double *w, double rate_base,
+                         double rate_stim, double t0, double t1, unsigned long long seed) {
+  /* E_MFGR, E_GRGO, E_GOGR, E_GRPKJ (syn.cuh:13,20,31,38) */
+  static const double ekind[SYN_KINDS] = {0.0, 0.0, -82.0, 0.0};
+  if (n->ngrp >= 64 || kind < 0 || kind >= SYN_KINDS) return -1;
+  int g = n->ngrp++;
+  int dflt = rate_base == 0.0 && rate_stim == 0.0 && t0 == 0.0 && t1 == 0.0;
+  n->rate[g][0] = dflt ? 5.0 : rate_base;
+  n->rate[g][1] = dflt ? 60.0 : rate_stim;
+  n->rate[g][2] = dflt ? 900.0 : t0;
+  n->rate[g][3] = dflt ? 1000.0 : t1;
+  n->seed[g] = seed;
+  if (n->n + count > n->cap) {
+    n->cap = (n->n + count) * 2;
+    NET_GROW(kind, int); NET_GROW(grp, int); NET_GROW(pre_sys, int); NET_GROW(pre_comp, int);
+    NET_GROW(post_sys, int); NET_GROW(post_comp, int);
+    NET_GROW(w, double); NET_GROW(s0, double); NET_GROW(s1, double); NET_GROW(s2, double);
+    NET_GROW(val, double); NET_GROW(old_v, double); NET_GROW(e, double);
+  }
+  int first = n->n;
+  for (int i = 0; i < count; i++) {
+    int k = n->n++;
+    n->kind[k] = kind;
+    n->grp[k] = g;
+    n->pre_sys[k] = (kind == SYN_MFGR) ? -1 : pre_sys[i];
+    n->pre_comp[k] = (kind == SYN_MFGR) ? 0 : pre_comp[i];
+    n->post_sys[k] = post_sys[i];
+    n->post_comp[k] = post_comp[i];
+    n->w[k] = w[i];
+    n->s0[k] = n->s1[k] = n->s2[k] = n->val[k] = 0.0;
+    n->old_v[k] = 1000.0; /* syn.cu:176, 330, 510 */
+    n->e[k] = ekind[kind];
+  }
+  return first;
+}
+
+/* CSR of each system's incoming synapses, ids in (kind, id) order */
+int orc_net_build(orc_net *n) {
+  for (int q = 0; q < n->nsys; q++) {
+    orc_sys *s = n->sys[q];
+    int cnt = 0;
+    for (int k = 0; k < n->n; k++) cnt += (n->post_sys[k] == q);
+    if (!cnt) continue;
+    s->syn_row = ialloc((size_t)s->nc + 1);
+    s->syn_idx = ialloc((size_t)cnt);
+    s->syn_buf = zalloc((size_t)s->nc);
+    for (int k = 0; k < n->n; k++)
+      if (n->post_sys[k] == q) s->syn_row[n->post_comp[k] + 1]++;
+    for (int c = 0; c < s->nc; c++) s->syn_row[c + 1] += s->syn_row[c];
+    int *fill = ialloc((size_t)s->nc);
+    for (int kd = 0; kd < SYN_KINDS; kd++)
+      for (int k = 0; k < n->n; k++)
+        if (n->post_sys[k] == q && n->kind[k] == kd) {
+          int c = n->post_comp[k];
+          s->syn_idx[s->syn_row[c] + fill[c]++] = k;
+        }
+    free(fill);
+    s->syn_val = n->val;
+    s->syn_e = n->e;
+    s->syn_mode = (s->type == ORC_GR) ? 1 : (s->type == ORC_GO) ? 2 : (s->type == ORC_PKJ) ? 3 : 0;
+    if (!s->syn_mode) return -1;
+  }
+  return 0;
+}
+
+/* SplitMix64 finaliser (Steele, Lea & Flood 2014) over (seed, synapse,
+ * interval) -> (0, 1]: the Poisson draws, shared with the CUDA path */
+static double syn_uniform(unsigned long long seed, long long id, long long interval) {
+  unsigned long long z = seed ^ ((unsigned long long)id * 0xD1B54A32D192ED03ull) ^
+                         ((unsigned long long)interval * 0x9E3779B97F4A7C15ull);
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)((z >> 11) + 1ull) * 0x1p-53;
+}
+
+/* mfgr_update, grgo_update, gogr_update, grpkj_update (syn.cu:86-111,
+ * 263-288, 412-437, 646-668); conductances syn.cuh:11-45 */
+static void net_syn_update(orc_net *n, double t) {
+  for (int k = 0; k < n->n; k++) {
+    int kind = n->kind[k];
+    if (kind == SYN_MFGR) {
+      const double *r = n->rate[n->grp[k]];
+      double fr = (r[2] <= t && t < r[3]) ? r[1] : r[0];
+      double u = syn_uniform(n->seed[n->grp[k]], k, n->interval);
+      int f = (fr * 0.125 * 0.001 > u) ? 1 : 0;
+      double ampa = n->s0[k] * n->decay[0] + f;
+      double nmda = ampa * n->decay[1] + f; /* from the updated AMPA, syn.cu:104 */
+      n->s0[k] = ampa;
+      n->s1[k] = nmda;
+      n->val[k] = n->w[k] * (0.18e-9 * ampa + 0.025e-9 * nmda);
+      continue;
+    }
+    double pv = n->sys[n->pre_sys[k]]->v[n->pre_comp[k]];
+    int f = (pv > 0.0 && n->old_v[k] < 0.0) ? 1 : 0;
+    if (kind == SYN_GRGO) {
+      double a = n->s0[k] * n->decay[2] + f;
+      double n1 = n->s1[k] * n->decay[3] + f;
+      double n2 = n->s2[k] * n->decay[4] + f;
+      n->s0[k] = a; n->s1[k] = n1; n->s2[k] = n2;
+      n->val[k] = n->w[k] * (45.5e-9 * a + 30.0e-9 * (0.33 * n1 + 0.67 * n2));
+    } else if (kind == SYN_GOGR) {
+      double ga = n->s0[k] * n->decay[5] + f;
+      double gb = n->s1[k] * n->decay[6] + f;
+      n->s0[k] = ga; n->s1[k] = gb;
+      n->val[k] = n->w[k] * 0.028e-9 * (0.43 * ga + 0.57 * gb);
+    } else {
+      double a = n->s0[k] * n->decay[7] + f;
+      n->s0[k] = a;
+      n->val[k] = a * n->w[k] * 0.7e-9;
+    }
+    n->old_v[k] = pv;
+  }
+  n->interval++;
+}
+
+/* one interval: every system in the order added, then the synapses */
+int orc_net_advance(orc_net *n, double t) {
+  for (int q = 0; q < n->nsys; q++) {
+    int rc = orc_advance(n->sys[q], t);
+    if (rc) return rc;
+  }
+  net_syn_update(n, t);
+  return 0;
+}
+
+int orc_net_nsyn(const orc_net *n) { return n->n; }
+const double *orc_net_syn(const orc_net *n, int field) {
+  switch (field) {
+    case 0: return n->val;
+    case 1: return n->s0;
+    case 2: return n->s1;
+    case 3: return n->s2;
+    default: return n->old_v;
+  }
+}
+
+void orc_net_destroy(orc_net *n) {
+  if (!n) return;
+  free(n->kind); free(n->grp); free(n->pre_sys); free(n->pre_comp); free(n->post_sys); free(n->post_comp);
+  free(n->w); free(n->s0); free(n->s1); free(n->s2); free(n->val); free(n->old_v); free(n->e);
+  free(n);
 }

@@ -76,6 +76,23 @@ void orc_ctl(const orc_sys *s, double *out8);
 /* counters: steps, rejects, stage evals (sum of m), rho calls, ion updates,
  * power-iteration RHS evaluations */
 void orc_stats(const orc_sys *s, long long *out6);
+/* Network mode: systems advanced together with the reference's chemical
+ * synapses (syn.cu).  Systems advance in the order added; kinds 0..3 are
+ * MF->GrC, GrC->GoC, GoC->GrC, GrC->PC; rates all 0 = the reference's
+ * 5 / 60 Hz over 900-1000 ms.  Fields of orc_net_syn: 0 val, 1..3 states,
+ * 4 old_v.  The network does not own its systems. */
+typedef struct orc_net orc_net;
+orc_net *orc_net_create(void);
+int orc_net_add_system(orc_net *n, orc_sys *s);
+int orc_net_add_synapses(orc_net *n, int kind, int count, const int *pre_sys, const int *pre_comp,
+                         const int *post_sys, const int *post_comp, const double *w, double rate_base,
+                         double rate_stim, double t0, double t1, unsigned long long seed);
+int orc_net_build(orc_net *n);
+int orc_net_advance(orc_net *n, double t);
+int orc_net_nsyn(const orc_net *n);
+const double *orc_net_syn(const orc_net *n, int field);
+void orc_net_destroy(orc_net *n);
+
 /* Row swaps taken by the Na / KAHP Markov solvers so far (process-wide). */
 long long orc_pivot_swaps(void);
 /* The canonical exp / log / pow of canon_math.h. */

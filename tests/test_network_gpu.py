@@ -1,0 +1,52 @@
+"""Network mode (chemical synapses between systems) on the GPU against the
+oracle in canonical mode, bit for bit: every system's voltages and every
+synapse's states and conductance, through spikes that travel granule ->
+Golgi, Golgi -> granule and granule -> Purkinje."""
+import numpy as np
+import pytest
+
+import gbrkc as G
+from gpu_cases import build_network
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("checkpoints", [(40, 100, 160)])
+def test_network_fp64_bit_exact(oracle, checkpoints):
+    O = oracle
+    net = O.Network()
+    ids_o = build_network(O, net)
+    net.build()
+    eng = G.Engine(G.FP64)
+    ids_g = build_network(O, eng)
+    eng.build()
+    nsyn = len(net.syn(0))
+    t, done = 0.0, 0
+    for cp in checkpoints:
+        eng.advance(t, cp - done)
+        for _ in range(cp - done):
+            assert net.advance(t) == 0
+            t += G.H_MAX
+        done = cp
+        for a, b in zip(ids_o, ids_g):
+            np.testing.assert_array_equal(eng.vnew(b), net.systems[a].vnew(), err_msg=f"interval {cp} system {a}")
+        for f in range(5):
+            np.testing.assert_array_equal(eng.read_synapses(f, nsyn), net.syn(f), err_msg=f"interval {cp} field {f}")
+    s0 = net.syn(1)
+    n_mf, n_grgo, n_gogr = 32, 16, 16
+    assert s0[:n_mf].max() > 0, "mossy fibres fired"
+    assert s0[n_mf + n_grgo:n_mf + n_grgo + n_gogr].max() > 0, "a Golgi spike reached the granule cells"
+    assert s0[n_mf + n_grgo + n_gogr:].max() > 0, "a granule spike reached the Purkinje cell"
+    eng.close()
+
+
+def test_network_mixed_runs():
+    """Mixed precision steps the same network; synapses see spikes."""
+    import oracle_py as O
+    eng = G.Engine(G.MIXED)
+    build_network(O, eng)
+    eng.build()
+    eng.advance(0.0, 160)
+    s0 = eng.read_synapses(G.SYNF_S0, 32 + 16 + 16 + 40)
+    assert np.all(np.isfinite(s0)) and s0[:32].max() > 0
+    eng.close()
