@@ -546,6 +546,14 @@ extern "C" int gbrkc_add_system(gbrkc_engine *E, const gbrkc_system_desc *d, int
 
 namespace {
 
+// Systems of at least this many compartments run on a thread-block cluster
+// (GBRKC_CLUSTER_MIN_NC overrides, e.g. to exercise the path on small cases).
+int cluster_min_nc() {
+  const char *v = getenv("GBRKC_CLUSTER_MIN_NC");
+  if (v && v[0]) return atoi(v);
+  return 4096;
+}
+
 int assemble_pool(gbrkc_engine *E, PoolHost &P) {
   const int type = P.type;
   const int nion = NION[type], ncond = NCOND[type];
@@ -670,7 +678,24 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
     P.block = MEGA_BLOCK;
   }
   else if (P.max_nc <= 320) { P.team = TEAM_WARP; P.block = 128; }
+  else if (P.max_nc >= cluster_min_nc()) { P.team = TEAM_CLUSTER8; P.block = 256; }
   else { P.team = TEAM_BLOCK; P.block = 256; }
+  if (P.team == TEAM_CLUSTER8) {
+    // the workspace spread block-cyclically over 8 CTAs of 256 threads
+    const long slot = (long)((((P.max_nc + 1) & ~1) + 2047) / 2048) * 256;
+    const size_t need = (size_t)WS_VECS * slot * sizeof(double);
+    if (need <= 200 * 1024) {
+      int dev = 0, sms = 8;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      P.ws_tile = (long)WS_VECS * slot;
+      P.ws_in_smem = 1;
+      P.smem = need;
+      P.grid = 8 * std::max(1, std::min(nsys, sms / 8));
+      return 0;
+    }
+    P.team = TEAM_BLOCK;  // too large to stage: one CTA with the workspace in HBM
+  }
   const bool lanes = (P.team == TEAM_THREAD || P.team == TEAM_LANE4);
   // single-lane workspaces interleave across all MEGA_BLOCK threads of the
   // block, whichever of them hold a system
@@ -954,6 +979,9 @@ void rebalance_roles(gbrkc_engine *E, const double *role_ms, bool tune_gr) {
 int setup_mega(gbrkc_engine *E) {
   const char *no = getenv("GBRKC_NO_MEGA");
   if (no && no[0] == '1') return 0;
+  // pools of very large systems run on clusters, one launch per pool
+  for (int t = 0; t < NTYPES; t++)
+    if (!E->pools[t].systems.empty() && E->pools[t].team == TEAM_CLUSTER8) return 0;
   const PoolHost &G = E->pools[GR], &O = E->pools[GO];
   if (!G.systems.empty() && G.max_nc > LANE_MAX_NC) return 0;
   if (!O.systems.empty() && O.max_nc > 320) return 0;

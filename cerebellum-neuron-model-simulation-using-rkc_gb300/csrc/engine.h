@@ -132,7 +132,8 @@ int launch_syn_update(const SynView &S, void *stream, double t, long long interv
 // workspaces), 4 or 32 lanes per system, or a whole block per system.
 // TEAM_LANE4: one thread per system for pools whose systems all have exactly
 // 4 compartments (loops unrolled at compile time).
-enum TeamKind { TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0 };
+// TEAM_CLUSTER8: one system per cluster of 8 CTAs (very large systems).
+enum TeamKind { TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0, TEAM_CLUSTER8 = 108 };
 
 // All pools in one persistent launch: CTA b < role_end[0] integrates granule
 // systems (one per lane, on the CTA's first warps), then Golgi

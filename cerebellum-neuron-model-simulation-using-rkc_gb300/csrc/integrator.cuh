@@ -40,8 +40,14 @@ struct WVec {
   __device__ __forceinline__ double &operator[](int i) const { return p[(long)i * LS]; }
 };
 
+// Every team provides its workspace-vector type (Vec), builds the vector at
+// a slot offset (vec_at) and gives the slot length for ncp elements
+// (vstride).  CLUSTER > 0 marks a team spread over a thread-block cluster.
 struct BlockTeam {
-  static constexpr int LS = 1, NCF = 0;
+  static constexpr int LS = 1, NCF = 0, CLUSTER = 0;
+  typedef WVec<1> Vec;
+  __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off}; }
+  __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
   __device__ __forceinline__ int rank() const { return threadIdx.x; }
   __device__ __forceinline__ int size() const { return blockDim.x; }
   __device__ __forceinline__ void sync() const { __syncthreads(); }
@@ -49,7 +55,10 @@ struct BlockTeam {
 
 template <int T>
 struct TileTeam {
-  static constexpr int LS = 1, NCF = 0;
+  static constexpr int LS = 1, NCF = 0, CLUSTER = 0;
+  typedef WVec<1> Vec;
+  __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off}; }
+  __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
   unsigned mask;
   int r;
   __device__ __forceinline__ int rank() const { return r; }
@@ -66,10 +75,53 @@ struct TileTeam {
 // would otherwise serialise the loop) and the pairwise sums run in registers.
 template <int BLOCK, int NCF_ = 0>
 struct LaneTeam {
-  static constexpr int LS = BLOCK, NCF = NCF_;
+  static constexpr int LS = BLOCK, NCF = NCF_, CLUSTER = 0;
+  typedef WVec<BLOCK> Vec;
+  __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off * BLOCK}; }
+  __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
   __device__ __forceinline__ int rank() const { return 0; }
   __device__ __forceinline__ int size() const { return 1; }
   __device__ __forceinline__ void sync() const {}
+};
+
+// One system on a thread-block cluster of C CTAs of CLUSTER_BLOCK threads.
+// The workspace is spread block-cyclically over the CTAs' shared memory:
+// element i sits in CTA (i mod 256C) / 256 at slot (i / 256C) * 256 + i mod
+// 256, so the elements a thread owns in the team loops (i = rank + k * size)
+// are in its own CTA; others (a compartment's neighbours) are read and
+// written through distributed shared memory.  The team barrier is the
+// cluster barrier.
+constexpr int CLUSTER_BLOCK = 256;
+
+template <int C>
+struct CVec {
+  long off;                    // slot offset within every CTA's workspace
+  double *const *bases;        // workspace base of each CTA of the cluster
+  __device__ __forceinline__ double &operator[](int i) const {
+    constexpr int SZ = C * CLUSTER_BLOCK;
+    const int q = (i & (SZ - 1)) / CLUSTER_BLOCK;
+    const long l = (long)(i / SZ) * CLUSTER_BLOCK + (i & (CLUSTER_BLOCK - 1));
+    return bases[q][off + l];
+  }
+};
+
+template <int C>
+struct ClusterTeam {
+  static_assert((C & (C - 1)) == 0 && C <= 16, "cluster size must be a power of two up to 16");
+  static constexpr int LS = 1, NCF = 0, CLUSTER = C;
+  typedef CVec<C> Vec;
+  int crank;                   // this CTA's rank in the cluster
+  double *const *bases;        // [C] workspace bases (distributed shared memory)
+  __device__ __forceinline__ Vec vec_at(double *, long off) const { return Vec{off, bases}; }
+  __device__ __forceinline__ static long vstride(int ncp) {
+    constexpr int SZ = C * CLUSTER_BLOCK;
+    return (long)((ncp + SZ - 1) / SZ) * CLUSTER_BLOCK;
+  }
+  __device__ __forceinline__ int rank() const { return crank * CLUSTER_BLOCK + (int)threadIdx.x; }
+  __device__ __forceinline__ int size() const { return C * CLUSTER_BLOCK; }
+  __device__ __forceinline__ void sync() const {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+  }
 };
 
 // pairwise tree over a[0..N) in registers, the same order as Sys::tree_sum
@@ -168,7 +220,7 @@ template <int CT, typename R, class Team>
 struct Sys {
   static constexpr int LS = Team::LS, NCF = Team::NCF;
   static constexpr int NR = NCF > 0 ? NCF : 1;   // register staging width
-  typedef WVec<LS> V;
+  typedef typename Team::Vec V;
   const PoolView<R> &P;
   const Team &tm;
   int s, nc, ncp, ncell, ncomp, off, cell0;
@@ -210,9 +262,9 @@ struct Sys {
     }
   }
 
-  __device__ __forceinline__ V vec(int logical) const { return V{W + (long)c.map[logical] * ncp * LS}; }
-  __device__ __forceinline__ V bvec() const { return V{W + (long)WS_B * ncp * LS}; }
-  __device__ __forceinline__ V scratch() const { return V{W + (long)WS_SCRATCH * ncp * LS}; }
+  __device__ __forceinline__ V vec(int logical) const { return tm.vec_at(W, (long)c.map[logical] * Team::vstride(ncp)); }
+  __device__ __forceinline__ V bvec() const { return tm.vec_at(W, (long)WS_B * Team::vstride(ncp)); }
+  __device__ __forceinline__ V scratch() const { return tm.vec_at(W, (long)WS_SCRATCH * Team::vstride(ncp)); }
 
   // dydt at compartment i (solve_rkc.cu:178-196): (-b + sum g (y_j - y_i)) / Cm
   __device__ __forceinline__ double rhs(const V y, int i) const {
@@ -741,12 +793,29 @@ struct Sys {
 // (element stride LS).
 template <class Team>
 __device__ __forceinline__ void ws_in(const Team &tm, double *dst, const double *src, long n) {
-  for (long i = tm.rank(); i < n; i += tm.size()) dst[i * Team::LS] = src[i];
+  if constexpr (Team::CLUSTER > 0) {
+    // n = WS_VECS slots of ncp elements; each thread copies the elements it owns
+    const int ncp = (int)(n / WS_VECS);
+    for (int k = 0; k < WS_VECS; k++) {
+      const typename Team::Vec v = tm.vec_at(dst, (long)k * Team::vstride(ncp));
+      for (int i = tm.rank(); i < ncp; i += tm.size()) v[i] = src[(long)k * ncp + i];
+    }
+  } else {
+    for (long i = tm.rank(); i < n; i += tm.size()) dst[i * Team::LS] = src[i];
+  }
   tm.sync();
 }
 template <class Team>
 __device__ __forceinline__ void ws_out(const Team &tm, double *dst, const double *src, long n) {
-  for (long i = tm.rank(); i < n; i += tm.size()) dst[i] = src[i * Team::LS];
+  if constexpr (Team::CLUSTER > 0) {
+    const int ncp = (int)(n / WS_VECS);
+    for (int k = 0; k < WS_VECS; k++) {
+      const typename Team::Vec v = tm.vec_at(const_cast<double *>(src), (long)k * Team::vstride(ncp));
+      for (int i = tm.rank(); i < ncp; i += tm.size()) dst[(long)k * ncp + i] = v[i];
+    }
+  } else {
+    for (long i = tm.rank(); i < n; i += tm.size()) dst[i] = src[i * Team::LS];
+  }
   tm.sync();
 }
 

@@ -7,6 +7,7 @@
 //
 // Built with -fmad=false (see integrator.cuh).  R selects FP64 or FP32
 // gating; the instantiations live in kernels_fp64.cu / kernels_fp32.cu.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "integrator.cuh"
@@ -42,6 +43,24 @@ __global__ void __launch_bounds__(256, 1) k_advance(const __grid_constant__ Pool
     for (int s = blockIdx.x * tiles + tile; s < P.nsys; s += gridDim.x * tiles)
       run_system<CT, R, TileTeam<TS>>(P, tm, s, my, t0, n_iv, iv0, init != 0);
   }
+}
+
+// One large system per thread-block cluster of C CTAs (ClusterTeam): the
+// cluster takes systems cid, cid + nclusters, ...
+template <int CT, typename R, int C>
+__global__ void __launch_bounds__(CLUSTER_BLOCK, 1) k_advance_cluster(const __grid_constant__ PoolView<R> P, double t0,
+                                                                       int n_iv, int iv0, int init) {
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) double smem[];
+  __shared__ double *s_bases[C];
+  cg::cluster_group cl = cg::this_cluster();
+  if (threadIdx.x < C) s_bases[threadIdx.x] = cl.map_shared_rank(smem, (int)threadIdx.x);
+  cl.sync();
+  const ClusterTeam<C> tm{(int)cl.block_rank(), s_bases};
+  const int ncl = gridDim.x / C, cid = blockIdx.x / C;
+  for (int s = cid; s < P.nsys; s += ncl) run_system<CT, R, ClusterTeam<C>>(P, tm, s, smem, t0, n_iv, iv0, init != 0);
+  // no CTA leaves while a peer may still reach its shared memory
+  cl.sync();
 }
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -132,6 +151,7 @@ int launch_mega(const MegaView<R> &M, int grid, size_t smem, void *stream, doubl
 template <int CT, typename R>
 static const void *kernel_for(int team) {
   switch (team) {
+    case TEAM_CLUSTER8: return (const void *)k_advance_cluster<CT, R, 8>;
     case TEAM_LANE4:
       // instantiated for granule pools only (the others never have it)
       if constexpr (CT == GR) return (const void *)k_advance<CT, R, TEAM_LANE4>;
@@ -169,6 +189,21 @@ int launch_pool(int type, const PoolView<R> &P, int team, int grid, int block, s
   const void *k = kernel_ptr<R>(type, team);
   PoolView<R> Pc = P;
   void *args[] = {(void *)&Pc, (void *)&t0, (void *)&n_iv, (void *)&iv0, (void *)&init};
+  if (team == TEAM_CLUSTER8) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 8;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return (int)cudaLaunchKernelExC(&cfg, k, args);
+  }
   cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
   return (int)e;
 }
