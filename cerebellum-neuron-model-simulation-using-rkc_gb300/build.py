@@ -34,7 +34,7 @@ CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-un
 
 KERNEL_TUS = ["kernels_fp64.cu", "kernels_fp32.cu", "compat.cu", "noalloc.cu", "synapse.cu"]
 TU_FLAGS = {"kernels_fp32.cu": ["-prec-div=false"]}
-HOST_TUS = ["engine.cpp", "host_init.cpp"]
+HOST_TUS = ["engine.cpp", "host_init.cpp", "server.cpp"]
 
 
 def _newer(target: str, deps) -> bool:

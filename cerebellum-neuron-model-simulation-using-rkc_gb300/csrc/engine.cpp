@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <type_traits>
 #include <memory>
@@ -67,7 +68,9 @@ struct HostSystem {
   std::vector<double> io_gap_g, jitter;
   std::vector<int> stim_comp;
   std::vector<double> stim_amp, stim_t0, stim_t1;
+  std::vector<double> cond_scale;             // per cell, empty: 1
   double tol, hmin;
+  bool idle = false;                          // a free slot until reset
   // built
   int csr = -1;                               // index into the system-CSR table
   std::vector<int> gap_pre, gap_post;
@@ -373,7 +376,8 @@ struct PoolHost {
   std::vector<double> s_g, s_invcm;
   std::vector<int> gap_pre, gap_post;
   std::vector<double> gap_g;
-  std::vector<int> stim_comp, cell_soma;
+  std::vector<int> stim_comp, cell_soma, cell_spk;
+  std::vector<int> cell_sys, cell_local;  // per pool cell: engine system id, cell within it
   std::vector<double> stim_amp, stim_t0, stim_t1;
   long ws_total = 0;
   int max_nc = 0, min_nc = 1 << 30, max_ncell = 0;
@@ -390,6 +394,10 @@ struct PoolHost {
   Ctl *d_ctl = nullptr;
   double *d_soma = nullptr;
   int soma_cap = 0;
+  double *d_spk_prev = nullptr;
+  SpikeRec *d_spk_log = nullptr;         // owned here (re-sized by gbrkc_record_spikes)
+  int *d_spk_count = nullptr;
+  int spk_cap = 0;
   std::vector<char> retired;
 };
 
@@ -415,6 +423,7 @@ struct gbrkc_engine {
   int soma_cap = 0;
   int soma_iv = 0;   // intervals recorded so far
   int n_retired = 0;
+  bool pending_init = false;    // systems reset since the last launch wait for initialisation
   cudaEvent_t ev_start = nullptr, ev_end = nullptr, ev_k0[NTYPES] = {}, ev_k1[NTYPES] = {};
   float last_ms = 0.0f, last_kernel_ms[NTYPES] = {};
   // persistent mixed-type launch
@@ -436,6 +445,8 @@ struct gbrkc_engine {
   SynView sv{};
   long long syn_interval = 0;   // intervals advanced in network mode (Poisson counter)
   ~gbrkc_engine() {
+    for (auto &P : pools)
+      if (P.d_spk_log) cudaFree(P.d_spk_log);
     for (auto &s : streams)
       if (s) cudaStreamDestroy(s);
     for (cudaEvent_t e : {ev_start, ev_end})
@@ -503,6 +514,12 @@ extern "C" int gbrkc_add_system(gbrkc_engine *E, const gbrkc_system_desc *d, int
       S.stim_amp[c] = d->stim_amp[c]; S.stim_t0[c] = d->stim_t0[c]; S.stim_t1[c] = d->stim_t1[c];
     }
   }
+  if (d->cond_scale) {
+    S.cond_scale.assign(d->cond_scale, d->cond_scale + S.n);
+    for (double x : S.cond_scale)
+      if (!(x >= 0.0) || !std::isfinite(x)) return fail(GBRKC_EINVAL, "conductance scale must be finite and >= 0");
+  }
+  S.idle = d->idle != 0;
   S.tol = d->tol > 0 ? d->tol : TOL_DEFAULT[S.type];
   S.hmin = d->hmin > 0 ? d->hmin : pow(2.0, (double)HMIN_LOG2_DEFAULT[S.type]);
   if (S.n > 1 && S.gap) {
@@ -552,6 +569,70 @@ int cluster_min_nc() {
   const char *v = getenv("GBRKC_CLUSTER_MIN_NC");
   if (v && v[0]) return atoi(v);
   return 4096;
+}
+
+// Output compartments per cell: the voltage record (the soma; the
+// reference's output_file columns) and the raster (the compartment whose
+// threshold crossing output_file logs): gr.cu:257-280, go.cu:271-290,
+// pkj.cu:371-390, io.cu:260-283.
+int soma_comp(int type, int ncomp) {
+  if (type == PKJ) return ncomp - 1;
+  if (type == GO) return std::min(30, ncomp - 1);
+  if (type == GR) return (ncomp == 578) ? 16 : std::min(1, ncomp - 1);
+  return std::min(1, ncomp - 1);
+}
+int spike_comp(int type, int ncomp) {
+  if (type == PKJ) return ncomp - 1;
+  if (type == GO) return std::min(30, ncomp - 1);
+  if (type == GR) return (ncomp == 578) ? 77 : ncomp - 1;
+  return std::min(2, ncomp - 1);
+}
+double spike_threshold(int type) { return type == PKJ ? -10.0 : 10.0; }
+
+// Controller state before initialisation (RKC_vec_initialize's h_others /
+// h_work / h_bool, solve_rkc.cu:757-791): waiting for the init launch unless
+// the system is a free slot; iv_left intervals may be advanced (-1: any).
+Ctl initial_ctl(const HostSystem &S, int iv_left) {
+  Ctl c{};
+  for (int k = 0; k < 5; k++) c.map[k] = k;
+  c.tend = H_MAX;
+  c.last = 1; c.newspc = 1; c.jacatt = 0;
+  c.tol = S.tol;
+  c.hmin = S.hmin;
+  c.integ = pow(2.0, log10(S.tol));
+  c.status = S.idle ? 0 : ST_INIT;
+  c.iv_left = S.idle ? 0 : iv_left;
+  return c;
+}
+
+// System S's conductances (channel densities times its cells' scales), its
+// initial state (*_initialize_ion: gr_ion.cu:635-672, go_ion.cu:590-634,
+// pkj_ion.cu:360-395, io_ion.cu:163-194) and its stimulus, into the pool's
+// host mirrors at compartment offset off and pool cell cell0.
+void fill_state(gbrkc_engine *E, PoolHost &P, const HostSystem &S, long off, int cell0) {
+  const int type = P.type, nion = NION[type], ncond = NCOND[type];
+  const Template &T = E->templates[S.tmpl];
+  const long nc = P.nc;
+  for (int i = 0; i < S.nc; i++) {
+    const int j = i % S.ncomp, cell = i / S.ncomp;
+    const long g = off + i;
+    if (S.cond_scale.empty()) {
+      for (int k = 0; k < ncond; k++) P.cond[(size_t)k * nc + g] = T.cond[k][j];
+    } else {
+      for (int k = 0; k < ncond; k++) P.cond[(size_t)k * nc + g] = T.cond[k][j] * S.cond_scale[cell];
+    }
+    CompInit ci;
+    initial_state(type, S.jitter[cell], T.ctype[j], (type == IO) ? P.cond[(size_t)IO_g_CaH * nc + g] : 0.0, &ci);
+    P.v[g] = ci.v; P.ca[g] = ci.ca; P.ca2[g] = ci.ca2; P.rev[g] = ci.rev; P.ca_old[g] = ci.ca_old;
+    P.iext[g] = 0.0;
+    for (int k = 0; k < nion; k++) P.ion[(size_t)k * nc + g] = ci.x[k];
+  }
+  for (int c = 0; c < S.n; c++) {
+    P.stim_comp[cell0 + c] = S.stim_comp[c];
+    P.stim_amp[cell0 + c] = S.stim_amp[c];
+    P.stim_t0[cell0 + c] = S.stim_t0[c];
+    P.stim_t1[cell0 + c] = S.stim_t1[c];
+  }
 }
 
 int assemble_pool(gbrkc_engine *E, PoolHost &P) {
@@ -627,42 +708,27 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
     }
     P.sys_ws.push_back(ws);
     ws += (long)WS_VECS * ((S.nc + 1) & ~1);
-    // per compartment static data and the initial state (*_initialize_ion)
-    const double gcah = (type == IO) ? 0.0 : 0.0;
-    (void)gcah;
+    // per compartment static data, then the initial state
     for (int i = 0; i < S.nc; i++) {
-      const int j = i % S.ncomp, cell = i / S.ncomp;
+      const int j = i % S.ncomp;
       const long g = off + i;
       P.ctype[g] = (uint8_t)T.ctype[j];
       P.area[g] = T.area[j];
       P.shell[g] = T.shell[j];
-      for (int k = 0; k < ncond; k++) P.cond[(size_t)k * nc + g] = T.cond[k][j];
-      CompInit ci;
-      initial_state(type, S.jitter[cell], T.ctype[j], (type == IO) ? T.cond[IO_g_CaH][j] : 0.0, &ci);
-      P.v[g] = ci.v; P.ca[g] = ci.ca; P.ca2[g] = ci.ca2; P.rev[g] = ci.rev; P.ca_old[g] = ci.ca_old;
-      for (int k = 0; k < nion; k++) P.ion[(size_t)k * nc + g] = ci.x[k];
       if (type == PKJ && (i % 1599 == 0)) P.flags[g] |= 1;  // pkj_ion.cu:329
     }
+    P.stim_comp.resize(cell0 + S.n);
+    P.stim_amp.resize(cell0 + S.n);
+    P.stim_t0.resize(cell0 + S.n);
+    P.stim_t1.resize(cell0 + S.n);
+    fill_state(E, P, S, off, cell0);
     for (int c = 0; c < S.n; c++) {
-      P.stim_comp.push_back(S.stim_comp[c]);
-      P.stim_amp.push_back(S.stim_amp[c]);
-      P.stim_t0.push_back(S.stim_t0[c]);
-      P.stim_t1.push_back(S.stim_t1[c]);
-      int sc;
-      if (type == PKJ) sc = S.ncomp - 1;
-      else if (type == GO) sc = std::min(30, S.ncomp - 1);
-      else if (type == GR) sc = (S.ncomp == 578) ? 16 : std::min(1, S.ncomp - 1);
-      else sc = std::min(1, S.ncomp - 1);
-      P.cell_soma.push_back((int)(off + (long)c * S.ncomp + sc));
+      P.cell_soma.push_back((int)(off + (long)c * S.ncomp + soma_comp(type, S.ncomp)));
+      P.cell_spk.push_back((int)(off + (long)c * S.ncomp + spike_comp(type, S.ncomp)));
+      P.cell_sys.push_back(id);
+      P.cell_local.push_back(c);
     }
-    Ctl c{};
-    for (int k = 0; k < 5; k++) c.map[k] = k;
-    c.tend = H_MAX;
-    c.last = 1; c.newspc = 1; c.jacatt = 0;
-    c.tol = S.tol;
-    c.hmin = S.hmin;
-    c.integ = pow(2.0, log10(S.tol));
-    P.ctl.push_back(c);
+    P.ctl.push_back(initial_ctl(S, S.idle ? 0 : -1));
     off += S.nc;
     cell0 += S.n;
   }
@@ -750,8 +816,17 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
   UP(P.s_col, V.s_col); UP(P.s_g, V.s_g); UP(P.s_invcm, V.s_invcm);
   UP(P.gap_pre, V.gap_pre); UP(P.gap_post, V.gap_post); UP(P.gap_g, V.gap_g);
   UP(P.stim_comp, V.stim_comp); UP(P.stim_amp, V.stim_amp); UP(P.stim_t0, V.stim_t0);
-  UP(P.stim_t1, V.stim_t1); UP(P.cell_soma, V.cell_soma);
+  UP(P.stim_t1, V.stim_t1); UP(P.cell_soma, V.cell_soma); UP(P.cell_spk, V.cell_spk);
+  std::vector<double> prev(P.ncell, 100.0);  // raster_prev starts at 100 (main.cu:163-169)
+  UP(prev, V.spk_prev);
+  std::vector<int> zc(1, 0);
+  UP(zc, V.spk_count);
 #undef UP
+  V.spk_log = nullptr;
+  V.spk_cap = 0;
+  V.spk_th = spike_threshold(P.type);
+  P.d_spk_prev = V.spk_prev;
+  P.d_spk_count = V.spk_count;
   bool any_stim = false;
   for (int c : P.stim_comp) any_stim |= (c >= 0);
   V.stim_on = any_stim;
@@ -1258,6 +1333,12 @@ extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
     P.vf.soma_out = so;
   }
   int rc = 0;
+  if (E->pending_init) {
+    // systems reset since the last call: initialise them (only them) first
+    rc = launch_all(E, t0, 0, iv0, 1);
+    if (rc) return rc;
+    E->pending_init = false;
+  }
   if (E->sv.n > 0) {
     // network mode: every system advances one interval, then the synapses
     // update from the new presynaptic voltages (main.cu:196-305)
@@ -1524,6 +1605,259 @@ extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) 
   return 0;
 }
 
+// ------------------------------------------------------- slots and raster
+namespace {
+
+// Systems first_id .. first_id + n - 1 as one run of one pool (consecutive
+// pool positions): their pool and first position, or an error.
+int system_run(gbrkc_engine *E, int first_id, int n, PoolHost **Pout, int *pi0) {
+  if (!E || n <= 0 || first_id < 0 || first_id + (long)n > (long)E->systems.size())
+    return fail(GBRKC_EINVAL, "bad system range");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  const int type = E->systems[first_id].type;
+  PoolHost &P = E->pools[type];
+  const int p0 = E->systems[first_id].pool_index;
+  for (int k = 1; k < n; k++) {
+    const HostSystem &S = E->systems[first_id + k];
+    if (S.type != type || S.pool_index != p0 + k)
+      return fail(GBRKC_EINVAL, "systems %d..%d are not one run of one cell type", first_id, first_id + n - 1);
+  }
+  *Pout = &P;
+  *pi0 = p0;
+  return 0;
+}
+
+// Copy the host mirrors of pool positions pi0 .. pi1 - 1 (their compartments,
+// cells, edges, workspaces and controllers) to the device, with the
+// workspace, ede and v_new cleared as at build.
+template <typename R>
+int upload_run(gbrkc_engine *E, PoolHost &P, int pi0, int pi1) {
+  PoolView<R> &V = pool_view<R>(P);
+  cudaStream_t st = E->streams[0];
+  const long o0 = P.sys_off[pi0], o1 = (long)P.sys_off[pi1 - 1] + P.sys_nc[pi1 - 1];
+  const long nco = o1 - o0, nc = P.nc;
+  const int c0 = P.sys_cell0[pi0], c1 = P.sys_cell0[pi1 - 1] + P.sys_ncell[pi1 - 1];
+  const long w0 = P.sys_ws[pi0], w1 = P.sys_ws[pi1 - 1] + (long)WS_VECS * ((P.sys_nc[pi1 - 1] + 1) & ~1);
+  auto put = [&](void *dev, const void *host, size_t bytes) -> int {
+    CUDA_TRY(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, st));
+    return 0;
+  };
+  int rc = 0;
+  const size_t db = nco * sizeof(double);
+  if ((rc = put(V.v + o0, P.v.data() + o0, db)) || (rc = put(V.ca + o0, P.ca.data() + o0, db)) ||
+      (rc = put(V.ca2 + o0, P.ca2.data() + o0, db)) || (rc = put(V.rev + o0, P.rev.data() + o0, db)) ||
+      (rc = put(V.ca_old + o0, P.ca_old.data() + o0, db)) || (rc = put(V.iext + o0, P.iext.data() + o0, db)))
+    return rc;
+  const int nion = NION[P.type], ncond = NCOND[P.type];
+  std::vector<R> tmp((size_t)(nion + ncond) * nco);
+  for (int k = 0; k < nion; k++)
+    for (long i = 0; i < nco; i++) tmp[(size_t)k * nco + i] = (R)P.ion[(size_t)k * nc + o0 + i];
+  for (int k = 0; k < ncond; k++)
+    for (long i = 0; i < nco; i++) tmp[(size_t)(nion + k) * nco + i] = (R)P.cond[(size_t)k * nc + o0 + i];
+  for (int k = 0; k < nion; k++)
+    if ((rc = put(V.ion + (size_t)k * nc + o0, tmp.data() + (size_t)k * nco, nco * sizeof(R)))) return rc;
+  for (int k = 0; k < ncond; k++)
+    if ((rc = put(const_cast<R *>(V.cond) + (size_t)k * nc + o0, tmp.data() + (size_t)(nion + k) * nco,
+                  nco * sizeof(R))))
+      return rc;
+  CUDA_TRY(cudaMemsetAsync(V.ws + w0, 0, (w1 - w0) * sizeof(double), st));
+  CUDA_TRY(cudaMemsetAsync(V.ede + o0, 0, db, st));
+  CUDA_TRY(cudaMemsetAsync(V.vnew + o0, 0, db, st));
+  const size_t nce = c1 - c0;
+  std::vector<double> prev(nce, 100.0);
+  if ((rc = put(const_cast<int *>(V.stim_comp) + c0, P.stim_comp.data() + c0, nce * sizeof(int))) ||
+      (rc = put(const_cast<double *>(V.stim_amp) + c0, P.stim_amp.data() + c0, nce * sizeof(double))) ||
+      (rc = put(const_cast<double *>(V.stim_t0) + c0, P.stim_t0.data() + c0, nce * sizeof(double))) ||
+      (rc = put(const_cast<double *>(V.stim_t1) + c0, P.stim_t1.data() + c0, nce * sizeof(double))) ||
+      (rc = put(V.spk_prev + c0, prev.data(), nce * sizeof(double))))
+    return rc;
+  const int g0 = P.sys_gap0[pi0], g1 = P.sys_gap0[pi1 - 1] + P.sys_ngap[pi1 - 1];
+  if (g1 > g0 && (rc = put(const_cast<double *>(V.gap_g) + g0, P.gap_g.data() + g0, (g1 - g0) * sizeof(double))))
+    return rc;
+  if ((rc = put(V.ctl + pi0, P.ctl.data() + pi0, (pi1 - pi0) * sizeof(Ctl)))) return rc;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  bool any_stim = false;
+  for (int c : P.stim_comp) any_stim |= (c >= 0);
+  P.vd.stim_on = any_stim;
+  P.vf.stim_on = any_stim;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int gbrkc_systems_reset(gbrkc_engine *E, int first_id, int n, const gbrkc_reset_desc *d) {
+  PoolHost *P = nullptr;
+  int pi0 = 0;
+  int rc = system_run(E, first_id, n, &P, &pi0);
+  if (rc) return rc;
+  if (!d || !d->jitter) return fail(GBRKC_EINVAL, "null argument");
+  if (d->n_intervals < -1) return fail(GBRKC_EINVAL, "interval budget must be >= -1");
+  if (E->sv.n > 0) return fail(GBRKC_EINVAL, "engines with synapses cannot reset systems");
+  if (d->stim_comp && (!d->stim_amp || !d->stim_t0 || !d->stim_t1)) return fail(GBRKC_EINVAL, "incomplete stimulus");
+  // validate everything before changing anything
+  long cells = 0, edges = 0;
+  for (int k = 0; k < n; k++) {
+    const HostSystem &S = E->systems[first_id + k];
+    for (int c = 0; c < S.n; c++) {
+      if (d->stim_comp && d->stim_comp[cells + c] >= S.ncomp)
+        return fail(GBRKC_EINVAL, "stimulus compartment out of range");
+      if (d->cond_scale) {
+        const double x = d->cond_scale[cells + c];
+        if (!(x >= 0.0) || !std::isfinite(x)) return fail(GBRKC_EINVAL, "conductance scale must be finite and >= 0");
+      }
+    }
+    cells += S.n;
+    if (d->io_gap_g && S.type == IO && !S.gap_pre.empty()) edges += 4L * S.n;
+  }
+  if (d->io_gap_g && edges == 0) return fail(GBRKC_EINVAL, "io_gap_g given for systems without IO gap junctions");
+  cells = 0;
+  for (int k = 0; k < n; k++) {
+    HostSystem &S = E->systems[first_id + k];
+    const int pi = pi0 + k;
+    S.idle = false;
+    S.jitter.assign(d->jitter + cells, d->jitter + cells + S.n);
+    for (int c = 0; c < S.n; c++) {
+      const bool on = d->stim_comp && d->stim_comp[cells + c] >= 0;
+      S.stim_comp[c] = on ? d->stim_comp[cells + c] : -1;
+      S.stim_amp[c] = on ? d->stim_amp[cells + c] : 0.0;
+      S.stim_t0[c] = on ? d->stim_t0[cells + c] : 0.0;
+      S.stim_t1[c] = on ? d->stim_t1[cells + c] : 0.0;
+    }
+    if (d->cond_scale) S.cond_scale.assign(d->cond_scale + cells, d->cond_scale + cells + S.n);
+    else S.cond_scale.clear();
+    if (d->io_gap_g && S.type == IO && !S.gap_pre.empty()) {
+      // same edges, new conductances (gap.cu:4-120)
+      HostSystem G = S;
+      G.io_gap_g.assign(d->io_gap_g + 4 * cells, d->io_gap_g + 4 * (cells + S.n));
+      G.gap_pre.clear(); G.gap_post.clear(); G.gap_g.clear();
+      if ((rc = build_io_gap(G))) return rc;
+      if (G.gap_pre != S.gap_pre || G.gap_post != S.gap_post)
+        return fail(GBRKC_EINVAL, "io_gap_g changes the edge set of system %d (a conductance of 0?)", first_id + k);
+      S.io_gap_g = G.io_gap_g;
+      S.gap_g = G.gap_g;
+      std::copy(S.gap_g.begin(), S.gap_g.end(), P->gap_g.begin() + P->sys_gap0[pi]);
+    }
+    fill_state(E, *P, S, P->sys_off[pi], P->sys_cell0[pi]);
+    P->ctl[pi] = initial_ctl(S, d->n_intervals);
+    if ((int)P->retired.size() > pi) P->retired[pi] = 0;
+    cells += S.n;
+  }
+  rc = (E->precision == GBRKC_FP64) ? upload_run<double>(E, *P, pi0, pi0 + n)
+                                    : upload_run<float>(E, *P, pi0, pi0 + n);
+  if (rc) return rc;
+  E->pending_init = true;
+  return 0;
+}
+
+extern "C" int gbrkc_read_run(gbrkc_engine *E, int first_id, int n, int field, double *host, long cap) {
+  PoolHost *P = nullptr;
+  int pi0 = 0;
+  int rc = system_run(E, first_id, n, &P, &pi0);
+  if (rc) return rc;
+  const long o0 = P->sys_off[pi0], o1 = (long)P->sys_off[pi0 + n - 1] + P->sys_nc[pi0 + n - 1];
+  if (!host || cap < o1 - o0) return fail(GBRKC_EINVAL, "buffer holds %ld of %ld values", cap, o1 - o0);
+  const double *src = nullptr;
+  switch (field) {
+    case GBRKC_F_VNEW: src = P->d_vnew; break;
+    case GBRKC_F_V: src = P->d_v; break;
+    case GBRKC_F_CA: src = P->d_ca; break;
+    case GBRKC_F_REV: src = P->d_rev; break;
+    default: return fail(GBRKC_EINVAL, "field not readable by runs");
+  }
+  CUDA_TRY(cudaMemcpy(host, src + o0, (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int gbrkc_run_status(gbrkc_engine *E, int first_id, int n, int *status, int *iv_left) {
+  PoolHost *P = nullptr;
+  int pi0 = 0;
+  int rc = system_run(E, first_id, n, &P, &pi0);
+  if (rc) return rc;
+  if (status)
+    CUDA_TRY(cudaMemcpy2D(status, sizeof(int), (const char *)(P->d_ctl + pi0) + offsetof(Ctl, status), sizeof(Ctl),
+                          sizeof(int), n, cudaMemcpyDeviceToHost));
+  if (iv_left)
+    CUDA_TRY(cudaMemcpy2D(iv_left, sizeof(int), (const char *)(P->d_ctl + pi0) + offsetof(Ctl, iv_left), sizeof(Ctl),
+                          sizeof(int), n, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int gbrkc_set_budget(gbrkc_engine *E, int first_id, int n, int n_intervals) {
+  PoolHost *P = nullptr;
+  int pi0 = 0;
+  int rc = system_run(E, first_id, n, &P, &pi0);
+  if (rc) return rc;
+  if (n_intervals < -1) return fail(GBRKC_EINVAL, "interval budget must be >= -1");
+  std::vector<int> v(n, n_intervals);
+  CUDA_TRY(cudaMemcpy2D((char *)(P->d_ctl + pi0) + offsetof(Ctl, iv_left), sizeof(Ctl), v.data(), sizeof(int),
+                        sizeof(int), n, cudaMemcpyHostToDevice));
+  for (int k = 0; k < n; k++) P->ctl[pi0 + k].iv_left = n_intervals;
+  return 0;
+}
+
+extern "C" int gbrkc_record_spikes(gbrkc_engine *E, long capacity) {
+  if (!E || capacity < 0 || capacity > (1L << 30)) return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  for (int t = 0; t < NTYPES; t++) {
+    PoolHost &P = E->pools[t];
+    if (P.systems.empty()) continue;
+    if (P.d_spk_log) CUDA_TRY(cudaFree(P.d_spk_log));
+    P.d_spk_log = nullptr;
+    P.spk_cap = 0;
+    if (capacity > 0) {
+      cudaError_t e = cudaMalloc((void **)&P.d_spk_log, capacity * sizeof(SpikeRec));
+      if (e != cudaSuccess) return fail(GBRKC_ENOMEM, "spike log: %s", cudaGetErrorString(e));
+      P.spk_cap = (int)capacity;
+    }
+    CUDA_TRY(cudaMemset(P.d_spk_count, 0, sizeof(int)));
+    P.vd.spk_log = P.vf.spk_log = P.d_spk_log;
+    P.vd.spk_cap = P.vf.spk_cap = P.spk_cap;
+  }
+  return 0;
+}
+
+extern "C" int gbrkc_read_spikes(gbrkc_engine *E, int type, long cap, double *t, int *sys, int *cell, long *n) {
+  if (!E || type < 0 || type >= NTYPES || cap < 0 || !n || (cap > 0 && (!t || !sys || !cell)))
+    return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  *n = 0;
+  PoolHost &P = E->pools[type];
+  if (P.systems.empty() || !P.d_spk_log) return 0;
+  int cnt = 0;
+  CUDA_TRY(cudaMemcpy(&cnt, P.d_spk_count, sizeof(int), cudaMemcpyDeviceToHost));
+  const long avail = std::min<long>(cnt, P.spk_cap);
+  std::vector<SpikeRec> r(avail);
+  if (avail > 0) CUDA_TRY(cudaMemcpy(r.data(), P.d_spk_log, avail * sizeof(SpikeRec), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemset(P.d_spk_count, 0, sizeof(int)));
+  // the device appends in completion order: sort by time, then pool cell
+  std::sort(r.begin(), r.end(), [](const SpikeRec &a, const SpikeRec &b) {
+    return a.t < b.t || (a.t == b.t && a.cell < b.cell);
+  });
+  const long m = std::min(avail, cap);
+  for (long k = 0; k < m; k++) {
+    t[k] = r[k].t;
+    sys[k] = P.cell_sys[r[k].cell];
+    cell[k] = P.cell_local[r[k].cell];
+  }
+  *n = m;
+  if (cnt > P.spk_cap || avail > cap)
+    return fail(GBRKC_EOVERFLOW, "%ld spike(s) lost (logged %d, log capacity %d, read capacity %ld)",
+                (long)cnt - m, cnt, P.spk_cap, cap);
+  return 0;
+}
+
+extern "C" long long gbrkc_system_bytes(int precision, int cell_type, int ncomp, int ncell) {
+  if (cell_type < 0 || cell_type >= NTYPES || ncomp <= 0 || ncell <= 0) return fail(GBRKC_EINVAL, "bad shape");
+  const long long nc = (long long)ncomp * ncell;
+  const long long rb = (precision == GBRKC_FP64) ? 8 : 4;
+  long long b = nc * (WS_VECS * 8 + 10 * 8 + 2 + rb * (NION[cell_type] + NCOND[cell_type]));
+  b += (long long)ncell * (3 * 4 + 4 * 8 + 2 * 4);          // stimulus, output maps, raster
+  b += 12 * 4 + 8 + (long long)sizeof(Ctl);                  // system tables and controller
+  if (ncell > 1) b += nc * (4 + 8 + 3 * (4 + 8));            // system CSR (about 3 entries a row)
+  if (cell_type == IO && ncell > 1) b += 4LL * ncell * (4 + 4 + 8);  // gap edges
+  return b;
+}
+
 // ------------------------------------------------- gbrkc_advance_noalloc
 // gbrkc_advance without any allocation: the persistent launch's work-queue
 // counters and per-CTA timestamps come from the static scratch of
@@ -1532,7 +1866,7 @@ extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) 
 namespace {
 
 template <typename R>
-int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, unsigned long long *scratch) {
+int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, int init, unsigned long long *scratch) {
   MegaView<R> M{};
   int end = 0;
   for (int t = 0; t < NTYPES; t++) {
@@ -1565,11 +1899,12 @@ int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, unsigned l
   // the counters must start at zero; the stamps are all rewritten
   CUDA_TRY(cudaMemsetAsync(M.queue, 0, NOALLOC_QUEUE_WORDS * sizeof(unsigned long long), st));
   CUDA_TRY(cudaEventRecord(E->ev_start, st));
-  int rc = launch_mega<R>(M, end, E->mega_smem, st, t0, n_iv, iv0, 0);
+  int rc = launch_mega<R>(M, end, E->mega_smem, st, t0, n_iv, iv0, init);
   if (rc) return fail(GBRKC_ECUDA, "persistent launch: %s", cudaGetErrorString((cudaError_t)rc));
   CUDA_TRY(cudaEventRecord(E->ev_end, st));
   CUDA_TRY(cudaEventSynchronize(E->ev_end));
   CUDA_TRY(cudaEventElapsedTime(&E->last_ms, E->ev_start, E->ev_end));
+  if (init) return 0;
   unsigned long long ts[NOALLOC_MAX_CTAS], te[NOALLOC_MAX_CTAS];
   CUDA_TRY(cudaMemcpy(ts, M.t_start, end * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
   CUDA_TRY(cudaMemcpy(te, M.t_end, end * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
@@ -1601,17 +1936,22 @@ extern "C" int gbrkc_advance_noalloc(gbrkc_engine *E, double t0, int n_iv) {
     P.vf.soma_out = so;
   }
   int rc;
-  if (E->mega) {
-    unsigned long long *scratch = nullptr;
-    rc = noalloc_scratch(&scratch);
-    if (rc) return fail(GBRKC_ECUDA, "static scratch: %s", cudaGetErrorString((cudaError_t)rc));
-    rc = (E->precision == GBRKC_FP64) ? launch_mega_static<double>(E, t0, n_iv, iv0, scratch)
-                                      : launch_mega_static<float>(E, t0, n_iv, iv0, scratch);
-  } else {
-    // one launch per pool: those kernels use no scratch beyond the engine's state
-    rc = launch_all(E, t0, n_iv, iv0, 0);
+  for (int init = E->pending_init ? 1 : 0; init >= 0; init--) {
+    // systems reset since the last call are initialised (only they) first
+    const int n = init ? 0 : n_iv;
+    if (E->mega) {
+      unsigned long long *scratch = nullptr;
+      rc = noalloc_scratch(&scratch);
+      if (rc) return fail(GBRKC_ECUDA, "static scratch: %s", cudaGetErrorString((cudaError_t)rc));
+      rc = (E->precision == GBRKC_FP64) ? launch_mega_static<double>(E, t0, n, iv0, init, scratch)
+                                        : launch_mega_static<float>(E, t0, n, iv0, init, scratch);
+    } else {
+      // one launch per pool: those kernels use no scratch beyond the engine's state
+      rc = launch_all(E, t0, n, iv0, init);
+    }
+    if (rc) return rc;
+    if (init) E->pending_init = false;
   }
-  if (rc) return rc;
   if (E->soma_cap > 0) E->soma_iv += n_iv;
   // stopped systems: their status words, read in chunks with a strided copy
   int stopped = 0, first_id = -1, first_status = 0;

@@ -32,6 +32,15 @@ enum Status : int {
   ST_LOOP_CAP = 2,     // step loop exceeded its iteration bound
   ST_COEF_TABLE = 4,   // stage count beyond the coefficient table
   ST_IDID = 8,         // rkclow returned an idid other than 1/2 (solve_rkc.cu:1155)
+  ST_INIT = 16,        // waiting for initialisation (set by the host; cleared by the init launch)
+};
+
+// One threshold crossing of a cell's spike compartment, logged on the device
+// at the end of an interval: the interval's end time and the pool cell.
+struct SpikeRec {
+  double t;
+  int cell;
+  int pad;
 };
 
 // Controller state of one RKC system (h_others / h_work / h_bool of
@@ -42,6 +51,7 @@ struct Ctl {
   double cbrt_errold;  // errold^(1/3), carried from the last accepted step
   int map[5];          // logical {y, yn, fn, vtemp1, vtemp2} -> physical buffer
   int newspc, jacatt, last, status;
+  int iv_left;         // intervals this system may still advance (-1: no limit)
   long long n_steps, n_rej, n_stage, n_rho, n_rho_iter, n_ion;
 };
 
@@ -86,6 +96,15 @@ struct PoolView {
   double *soma_out;                   // [interval][pool cell] or null
   const int *cell_soma;               // per pool cell: compartment index in pool
   int ncell_pool;
+  // device raster: per pool cell the spike compartment and its value at the
+  // previous interval's end; an upward crossing of spk_th appends a SpikeRec
+  // (entries past spk_cap are counted, not written)
+  const int *cell_spk;
+  double *spk_prev;
+  SpikeRec *spk_log;
+  int *spk_count;
+  int spk_cap;
+  double spk_th;
   int ws_in_smem;                     // stage the workspace in shared memory
   long ws_tile_doubles;               // shared-memory workspace per team
   // chemical synapses onto this pool (network mode; syn_mode 0 = none)

@@ -216,6 +216,32 @@ __device__ __forceinline__ double comp_ion_b(const PoolView<R> &P, long gi, doub
   return bi;
 }
 
+// Whether a launch has work for a system: an init launch initialises the
+// systems waiting for it (ST_INIT); an advance steps the healthy systems
+// with intervals left in their budget.
+__device__ __forceinline__ bool system_selected(const Ctl &c, bool init, int n_iv) {
+  if (init) return (c.status & ST_INIT) != 0;
+  return c.status == 0 && n_iv > 0 && c.iv_left != 0;
+}
+
+// Device raster (output_file's rule, as in gr.cu:257 / pkj.cu:371): the
+// cell's spike compartment went above the threshold at the end of the
+// interval that ends at t, having been at or below it at the end of the
+// previous one (main.cu:215 passes the interval's end time).
+// The previous values are kept up to date whether or not the log is on.
+template <typename R>
+__device__ __forceinline__ void log_spike(const PoolView<R> &P, int pc, double t) {
+  const double x = P.vnew[P.cell_spk[pc]];
+  if (P.spk_log && x > P.spk_th && P.spk_prev[pc] <= P.spk_th) {
+    const int k = atomicAdd(P.spk_count, 1);
+    if (k < P.spk_cap) {
+      P.spk_log[k].t = t;
+      P.spk_log[k].cell = pc;
+    }
+  }
+  P.spk_prev[pc] = x;
+}
+
 template <int CT, typename R, class Team>
 struct Sys {
   static constexpr int LS = Team::LS, NCF = Team::NCF;
@@ -750,11 +776,17 @@ struct Sys {
         P.soma_out[(long)(iv0 + k_iv) * P.ncell_pool + pc] = P.vnew[P.cell_soma[pc]];
       }
     }
+    if (P.spk_prev) {
+      const double t = t0 + (k_iv + 1) * H_MAX;
+      for (int cc = tm.rank(); cc < ncell; cc += tm.size()) log_spike(P, cell0 + cc, t);
+    }
+    if (c.iv_left > 0) c.iv_left--;
   }
 
   // Start advancing by n intervals from t: TICK_DONE if there is nothing to
   // do, else what begin_interval returns.
   __device__ __forceinline__ int start(double t, int n, int iv0_global) {
+    if (c.iv_left >= 0 && n > c.iv_left) n = c.iv_left;
     t0 = t;
     n_iv = n;
     iv0 = iv0_global;
@@ -823,6 +855,7 @@ __device__ __forceinline__ void ws_out(const Team &tm, double *dst, const double
 template <int CT, typename R, class Team>
 __device__ __forceinline__ void run_system(const PoolView<R> &P, const Team &tm, int s, double *smem_ws, double t0,
                                            int n_iv, int iv0_global, bool init) {
+  if (!system_selected(P.ctl[s], init, n_iv)) return;
   const long wsn = (long)WS_VECS * (long)((P.sys_nc[s] + 1) & ~1);
   double *gws = P.ws + P.sys_ws[s];
   double *W = P.ws_in_smem ? smem_ws : gws;
@@ -831,6 +864,7 @@ __device__ __forceinline__ void run_system(const PoolView<R> &P, const Team &tm,
   S.c = P.ctl[s];
   if (init) {
     S.initialize();
+    S.c.status &= ~ST_INIT;
   } else {
     int r = S.start(t0, n_iv, iv0_global);
     while (r != TICK_DONE) {
@@ -870,12 +904,14 @@ __device__ __forceinline__ void run_lanes(const PoolView<R> &P, int *q, int firs
     while (s < P.nsys) {
       S.bind(s, W);
       S.c = P.ctl[s];
-      if (init) {
+      if (!system_selected(S.c, init, n_iv)) {
+      } else if (init) {
         ws_in(tm, W, P.ws + P.sys_ws[s], (long)WS_VECS * S.ncp);
         S.initialize();
+        S.c.status &= ~ST_INIT;
         ws_out(tm, P.ws + P.sys_ws[s], W, (long)WS_VECS * S.ncp);
         P.ctl[s] = S.c;
-      } else if (S.c.status == 0 && n_iv > 0) {
+      } else {
         ws_in(tm, W, P.ws + P.sys_ws[s], (long)WS_VECS * S.ncp);
         r = S.start(t0, n_iv, iv0_global);
         if (r != TICK_DONE) return;

@@ -371,9 +371,12 @@ struct LaneSys {
     for (int i = 0; i < NC; i++) P.vnew[off + i] = fma(b2, fn[i], fma(b1, v2[i], fma(a2, yn[i], a1 * v1[i])));
     c.tend += H_MAX;
     if (P.soma_out) P.soma_out[(long)(iv0 + k_iv) * P.ncell_pool + cell0] = P.vnew[P.cell_soma[cell0]];
+    if (P.spk_prev) log_spike(P, cell0, t0 + (k_iv + 1) * H_MAX);
+    if (c.iv_left > 0) c.iv_left--;
   }
 
   __device__ __forceinline__ int start(double t, int n, int iv0_global) {
+    if (c.iv_left >= 0 && n > c.iv_left) n = c.iv_left;
     t0 = t;
     n_iv = n;
     iv0 = iv0_global;
@@ -421,7 +424,7 @@ __device__ __forceinline__ void run_lanes_regs(const PoolView<R> &P, int *q, int
   int r = TICK_DONE;
   auto acquire = [&]() {
     while (s < P.nsys) {
-      if (P.ctl[s].status == 0) {
+      if (system_selected(P.ctl[s], false, n_iv)) {
         S.load(s);
         r = S.start(t0, n_iv, iv0_global);
         if (r != TICK_DONE) return;

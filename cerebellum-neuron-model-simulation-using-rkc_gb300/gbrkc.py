@@ -30,6 +30,42 @@ class SystemDesc(C.Structure):
         ("jitter", C.POINTER(C.c_double)), ("stim_comp", C.POINTER(C.c_int)),
         ("stim_amp", C.POINTER(C.c_double)), ("stim_t0", C.POINTER(C.c_double)),
         ("stim_t1", C.POINTER(C.c_double)), ("tol", C.c_double), ("hmin", C.c_double),
+        ("cond_scale", C.POINTER(C.c_double)), ("idle", C.c_int),
+    ]
+
+
+class SlotClass(C.Structure):
+    _fields_ = [("shape", SystemDesc), ("slots", C.c_longlong), ("share", C.c_double)]
+
+
+class RequestDesc(C.Structure):
+    _fields_ = [
+        ("class_id", C.c_int), ("n_systems", C.c_int), ("n_intervals", C.c_int),
+        ("jitter", C.POINTER(C.c_double)), ("stim_comp", C.POINTER(C.c_int)),
+        ("stim_amp", C.POINTER(C.c_double)), ("stim_t0", C.POINTER(C.c_double)),
+        ("stim_t1", C.POINTER(C.c_double)), ("cond_scale", C.POINTER(C.c_double)),
+        ("io_gap_g", C.POINTER(C.c_double)),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_longlong) for k in ("submitted", "admitted", "completed", "failed", "cancelled",
+                                            "queued", "resident", "rounds")] + \
+               [(k, C.c_double) for k in ("p50_ms", "p99_ms", "mean_ms", "max_ms", "busy_s", "advance_s")] + \
+               [(k, C.c_longlong) for k in ("compartment_updates", "hbm_reserved", "hbm_in_use", "slots",
+                                            "free_slots")] + \
+               [("sim_ms", C.c_double), ("lost_spike_reads", C.c_longlong)]
+
+
+REQ_QUEUED, REQ_RESIDENT, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+class ResetDesc(C.Structure):
+    _fields_ = [
+        ("jitter", C.POINTER(C.c_double)), ("stim_comp", C.POINTER(C.c_int)),
+        ("stim_amp", C.POINTER(C.c_double)), ("stim_t0", C.POINTER(C.c_double)),
+        ("stim_t1", C.POINTER(C.c_double)), ("cond_scale", C.POINTER(C.c_double)),
+        ("io_gap_g", C.POINTER(C.c_double)), ("n_intervals", C.c_int),
     ]
 
 
@@ -89,6 +125,31 @@ def lib() -> C.CDLL:
         L.gbrkc_launch_layout.argtypes = [P, C.POINTER(C.c_int)]
         L.gbrkc_compartment_updates.argtypes = [P, C.c_int]
         L.gbrkc_compartment_updates.restype = C.c_longlong
+        L.gbrkc_systems_reset.argtypes = [P, C.c_int, C.c_int, C.POINTER(ResetDesc)]
+        L.gbrkc_set_budget.argtypes = [P, C.c_int, C.c_int, C.c_int]
+        L.gbrkc_system_bytes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
+        L.gbrkc_system_bytes.restype = C.c_longlong
+        L.gbrkc_record_spikes.argtypes = [P, C.c_long]
+        L.gbrkc_read_spikes.argtypes = [P, C.c_int, C.c_long, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), C.POINTER(C.c_long)]
+        S = C.c_void_p
+        L.gbrkc_server_create.argtypes = [C.c_int, C.c_longlong, C.c_int, C.POINTER(S)]
+        L.gbrkc_server_destroy.argtypes = [S]
+        L.gbrkc_server_add_class.argtypes = [S, C.POINTER(SlotClass), C.POINTER(C.c_int)]
+        L.gbrkc_server_start.argtypes = [S]
+        L.gbrkc_server_class_slots.argtypes = [S, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.gbrkc_request_create.argtypes = [S, C.POINTER(RequestDesc), C.POINTER(C.c_int)]
+        L.gbrkc_request_advance.argtypes = [S, C.POINTER(C.c_int)]
+        L.gbrkc_request_state.argtypes = [S, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_int)]
+        L.gbrkc_request_read.argtypes = [S, C.c_int, C.POINTER(C.c_double), C.c_long]
+        L.gbrkc_request_spikes.argtypes = [S, C.c_int, C.c_long, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_long)]
+        L.gbrkc_request_destroy.argtypes = [S, C.c_int]
+        L.gbrkc_server_stats.argtypes = [S, C.POINTER(ServerStats)]
+        L.gbrkc_server_engine.argtypes = [S]
+        L.gbrkc_server_engine.restype = C.c_void_p
+        L.gbrkc_server_last_error.restype = C.c_char_p
         _LIB = L
     return _LIB
 
@@ -132,7 +193,7 @@ class Engine:
             pass
 
     def add_system(self, cell_type, nx, ny, rows, jitter, stim=None, gj_pairs=None, gap=True,
-                   io_gap_g=None, tol=0.0, hmin=0.0) -> int:
+                   io_gap_g=None, tol=0.0, hmin=0.0, cond_scale=None, idle=False) -> int:
         n = nx * ny
         rows = np.ascontiguousarray(rows, dtype=np.float64)
         jitter = np.ascontiguousarray(jitter, dtype=np.float64)
@@ -157,11 +218,56 @@ class Engine:
             d.stim_comp, d.stim_amp, d.stim_t0, d.stim_t1 = _ip(comp), _dp(amp), _dp(t0), _dp(t1)
             keep += [comp, amp, t0, t1]
         d.tol, d.hmin = tol, hmin
+        if cond_scale is not None:
+            cs = np.ascontiguousarray(np.broadcast_to(cond_scale, n), dtype=np.float64)
+            d.cond_scale = _dp(cs)
+            keep.append(cs)
+        d.idle = int(idle)
         sid = C.c_int()
         _check(lib().gbrkc_add_system(self.h, C.byref(d), C.byref(sid)))
         self._keep.append(keep)
         self.ncomp[sid.value] = (cell_type, n, rows.shape[0])
         return sid.value
+
+    def reset_systems(self, first: int, n: int, jitter, stim=None, cond_scale=None, io_gap_g=None,
+                      n_intervals: int = -1):
+        """Refill systems first .. first+n-1 (one run of one type) with new cells of the same shape."""
+        jitter = np.ascontiguousarray(jitter, dtype=np.float64)
+        cells = jitter.size
+        d = ResetDesc()
+        d.jitter = _dp(jitter)
+        keep = [jitter]
+        if stim is not None:
+            comp, amp, t0, t1 = stim
+            comp = np.ascontiguousarray(np.broadcast_to(comp, cells), dtype=np.int32)
+            amp, t0, t1 = (np.ascontiguousarray(np.broadcast_to(a, cells), dtype=np.float64) for a in (amp, t0, t1))
+            d.stim_comp, d.stim_amp, d.stim_t0, d.stim_t1 = _ip(comp), _dp(amp), _dp(t0), _dp(t1)
+            keep += [comp, amp, t0, t1]
+        if cond_scale is not None:
+            cs = np.ascontiguousarray(np.broadcast_to(cond_scale, cells), dtype=np.float64)
+            d.cond_scale = _dp(cs)
+            keep.append(cs)
+        if io_gap_g is not None:
+            gg = np.ascontiguousarray(io_gap_g, dtype=np.float64)
+            d.io_gap_g = _dp(gg)
+            keep.append(gg)
+        d.n_intervals = n_intervals
+        _check(lib().gbrkc_systems_reset(self.h, first, n, C.byref(d)))
+
+    def set_budget(self, first: int, n: int, n_intervals: int):
+        _check(lib().gbrkc_set_budget(self.h, first, n, n_intervals))
+
+    def record_spikes(self, capacity: int):
+        _check(lib().gbrkc_record_spikes(self.h, capacity))
+
+    def read_spikes(self, cell_type: int, cap: int = 1 << 20):
+        """Drain one type's device raster: (times, system ids, cells within system), sorted."""
+        t = np.empty(max(cap, 1), np.float64)
+        sy = np.empty(max(cap, 1), np.int32)
+        ce = np.empty(max(cap, 1), np.int32)
+        n = C.c_long()
+        _check(lib().gbrkc_read_spikes(self.h, cell_type, cap, _dp(t), _ip(sy), _ip(ce), C.byref(n)))
+        return t[:n.value].copy(), sy[:n.value].copy(), ce[:n.value].copy()
 
     def add_synapses(self, kind, post_system, post_comp, weight, pre_system=None, pre_comp=None,
                      rates=(0.0, 0.0, 0.0, 0.0), seed=0) -> int:
@@ -293,3 +399,123 @@ class Engine:
 
     def last_kernel_ms(self, cell_type: int) -> float:
         return float(lib().gbrkc_last_kernel_ms(self.h, cell_type))
+
+
+def system_bytes(precision: int, cell_type: int, ncomp: int, ncell: int) -> int:
+    """Device bytes one system of this shape takes (an upper estimate)."""
+    b = lib().gbrkc_system_bytes(precision, cell_type, ncomp, ncell)
+    if b < 0:
+        _check(int(b))
+    return int(b)
+
+
+def _scheck(rc: int) -> None:
+    if rc != 0:
+        raise GbrkcError(f"gbrkc server error {rc}: {lib().gbrkc_server_last_error().decode()}")
+
+
+class Server:
+    """Request server: jobs of uneven sizes and durations advanced together in one resident arena."""
+
+    def __init__(self, precision: int = MIXED, hbm_budget: int = 0, quantum: int = 8):
+        self.h = C.c_void_p()
+        _scheck(lib().gbrkc_server_create(precision, hbm_budget, quantum, C.byref(self.h)))
+        self._keep = []
+        self.cells = {}      # class id -> (cells per system, compartments per system)
+
+    def close(self):
+        if self.h:
+            lib().gbrkc_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_class(self, cell_type, nx, ny, rows, slots=0, share=0.0, gj_pairs=None, gap=True, tol=0.0,
+                  hmin=0.0) -> int:
+        rows = np.ascontiguousarray(rows, dtype=np.float64)
+        c = SlotClass()
+        d = c.shape
+        d.cell_type, d.nx, d.ny, d.ncomp = cell_type, nx, ny, rows.shape[0]
+        d.rows = _dp(rows)
+        keep = [rows]
+        if gj_pairs is not None:
+            g = np.ascontiguousarray(gj_pairs, dtype=np.int32).reshape(-1)
+            d.gj_pairs, d.n_gj_pairs = _ip(g), g.size // 2
+            keep.append(g)
+        d.gap_junctions = int(gap)
+        d.tol, d.hmin = tol, hmin
+        c.slots, c.share = slots, share
+        cid = C.c_int()
+        _scheck(lib().gbrkc_server_add_class(self.h, C.byref(c), C.byref(cid)))
+        self._keep.append(keep)
+        self.cells[cid.value] = (nx * ny, nx * ny * rows.shape[0])
+        return cid.value
+
+    def start(self):
+        _scheck(lib().gbrkc_server_start(self.h))
+
+    def class_slots(self, cid: int):
+        n, first = C.c_int(), C.c_int()
+        _scheck(lib().gbrkc_server_class_slots(self.h, cid, C.byref(n), C.byref(first)))
+        return n.value, first.value
+
+    def submit(self, cid, n_systems, n_intervals, jitter, stim=None, cond_scale=None, io_gap_g=None) -> int:
+        cells = n_systems * self.cells[cid][0]
+        jitter = np.ascontiguousarray(jitter, dtype=np.float64)
+        assert jitter.size == cells
+        d = RequestDesc()
+        d.class_id, d.n_systems, d.n_intervals = cid, n_systems, n_intervals
+        d.jitter = _dp(jitter)
+        keep = [jitter]
+        if stim is not None:
+            comp, amp, t0, t1 = stim
+            comp = np.ascontiguousarray(np.broadcast_to(comp, cells), dtype=np.int32)
+            amp, t0, t1 = (np.ascontiguousarray(np.broadcast_to(a, cells), dtype=np.float64) for a in (amp, t0, t1))
+            d.stim_comp, d.stim_amp, d.stim_t0, d.stim_t1 = _ip(comp), _dp(amp), _dp(t0), _dp(t1)
+            keep += [comp, amp, t0, t1]
+        if cond_scale is not None:
+            cs = np.ascontiguousarray(np.broadcast_to(cond_scale, cells), dtype=np.float64)
+            d.cond_scale = _dp(cs)
+            keep.append(cs)
+        if io_gap_g is not None:
+            gg = np.ascontiguousarray(io_gap_g, dtype=np.float64)
+            assert gg.size == 4 * cells
+            d.io_gap_g = _dp(gg)
+            keep.append(gg)
+        rid = C.c_int()
+        _scheck(lib().gbrkc_request_create(self.h, C.byref(d), C.byref(rid)))
+        return rid.value
+
+    def advance(self) -> int:
+        n = C.c_int()
+        _scheck(lib().gbrkc_request_advance(self.h, C.byref(n)))
+        return n.value
+
+    def state(self, rid: int):
+        st, lat, status = C.c_int(), C.c_double(), C.c_int()
+        _scheck(lib().gbrkc_request_state(self.h, rid, C.byref(st), C.byref(lat), C.byref(status)))
+        return st.value, lat.value, status.value
+
+    def read(self, rid: int, n: int) -> np.ndarray:
+        out = np.empty(n, np.float64)
+        _scheck(lib().gbrkc_request_read(self.h, rid, _dp(out), n))
+        return out
+
+    def spikes(self, rid: int, cap: int = 1 << 20):
+        t = np.empty(max(cap, 1), np.float64)
+        c = np.empty(max(cap, 1), np.int32)
+        n = C.c_long()
+        _scheck(lib().gbrkc_request_spikes(self.h, rid, cap, _dp(t), _ip(c), C.byref(n)))
+        return t[:n.value].copy(), c[:n.value].copy()
+
+    def destroy(self, rid: int):
+        _scheck(lib().gbrkc_request_destroy(self.h, rid))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _scheck(lib().gbrkc_server_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}

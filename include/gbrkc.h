@@ -30,7 +30,8 @@ enum {
   GBRKC_ECUDA = -2,    /* CUDA error (no device, launch failure, ...) */
   GBRKC_ESTATE = -3,   /* call out of order (e.g. add after build) */
   GBRKC_ENOMEM = -4,   /* device allocation failed */
-  GBRKC_ESOLVER = -5   /* a system stopped: see gbrkc_system_ctl status */
+  GBRKC_ESOLVER = -5,  /* a system stopped: see gbrkc_system_ctl status */
+  GBRKC_EOVERFLOW = -6 /* a fixed-size log or queue was full: entries were lost */
 };
 /* fields readable with gbrkc_read */
 enum {
@@ -62,6 +63,10 @@ typedef struct gbrkc_system_desc {
   const double *stim_t1;    /* ... and off at t1, evaluated at each interval start */
   double tol;               /* RKC rtol = atol; <= 0: reference per-type value */
   double hmin;              /* minimum step (ms); <= 0: reference per-type value */
+  const double *cond_scale; /* nx*ny factors on every channel density of the cell, or NULL
+                               (no counterpart in the reference: its densities are fixed) */
+  int idle;                 /* nonzero: a free slot -- neither initialised nor advanced
+                               until gbrkc_systems_reset fills it */
 } gbrkc_system_desc;
 
 /* Create an engine on the current CUDA device.  precision: GBRKC_FP64 (plain
@@ -215,6 +220,123 @@ long long gbrkc_compartment_updates(gbrkc_engine *e, int cell_type);
 /* Total compartments over all systems. */
 long gbrkc_total_compartments(gbrkc_engine *e);
 const char *gbrkc_last_error(void);
+
+/* ---- slots: re-using built systems (the request server's arena) ----
+ * A built system can be refilled in place with a new cell of the same shape
+ * (same type, morphology, grid and tolerance): new initial-voltage jitters,
+ * stimulus, conductance scales and, for IO networks, edge conductances.  It
+ * is then initialised on the device at the start of the next advance (only
+ * the reset systems are; RKC_vec_initialize, solve_rkc.cu:757-791) and
+ * integrates exactly as a freshly built system would: its own clock starts
+ * at 0, and only the stimulus windows use the advance's time.  An interval
+ * budget stops a system after that many intervals (it stays readable);
+ * a budget of 0 parks it. */
+typedef struct gbrkc_reset_desc {
+  const double *jitter;     /* one per cell of the systems, in order */
+  const int *stim_comp;     /* per cell: stimulated compartment or -1; NULL: none */
+  const double *stim_amp, *stim_t0, *stim_t1;  /* per cell (times as the advances pass them) */
+  const double *cond_scale; /* per cell, or NULL (1) */
+  const double *io_gap_g;   /* IO networks: 4 per cell, or NULL (keep) */
+  int n_intervals;          /* budget from now on; -1: none */
+} gbrkc_reset_desc;
+
+/* Reset systems first_id .. first_id+n-1, which must be consecutive systems
+ * of one cell type (one run of its pool).  Not for engines with synapses. */
+int gbrkc_systems_reset(gbrkc_engine *e, int first_id, int n, const gbrkc_reset_desc *d);
+/* A field (GBRKC_F_VNEW, _V, _CA or _REV) of systems first_id .. first_id+n-1
+ * (one run) in one copy: their compartments in order; cap >= their count. */
+int gbrkc_read_run(gbrkc_engine *e, int first_id, int n, int field, double *host, long cap);
+/* Status words (0: healthy, else GBRKC solver stop bits) and interval budgets
+ * left of one run of systems; either pointer may be NULL. */
+int gbrkc_run_status(gbrkc_engine *e, int first_id, int n, int *status, int *iv_left);
+/* Set the interval budget of systems first_id .. first_id+n-1 (one run). */
+int gbrkc_set_budget(gbrkc_engine *e, int first_id, int n, int n_intervals);
+/* Device bytes one system of this shape takes in an engine (an upper
+ * estimate for admission control), or a negative error code. */
+long long gbrkc_system_bytes(int precision, int cell_type, int ncomp, int ncell);
+
+/* ---- device raster ----
+ * At the end of every interval each cell's spike compartment is compared
+ * with the reference's output_file rule (value > threshold and the previous
+ * interval's value <= threshold; GrC/GoC/IO 10 mV on compartments 77 / 30 /
+ * 2 (GrC reduced cells: the last), PC -10 mV on the soma: gr.cu:257,
+ * go.cu:271, pkj.cu:371, io.cu:260), on the device.  gbrkc_record_spikes
+ * gives every cell type a log of `capacity` crossings (0 turns it off);
+ * gbrkc_read_spikes drains one type's log, sorted by (time, cell), as
+ * interval end times, engine system ids and cells within the system.
+ * GBRKC_EOVERFLOW reports crossings lost to a full log or a short read. */
+int gbrkc_record_spikes(gbrkc_engine *e, long capacity);
+int gbrkc_read_spikes(gbrkc_engine *e, int cell_type, long cap, double *t, int *sys, int *cell, long *n);
+
+/* ---- request server ----
+ * Simulation jobs of uneven cell counts and durations, admitted into a
+ * device-resident arena and advanced together (no counterpart in the
+ * reference, which integrates one fixed block per type per process).
+ *
+ * A slot class is one system shape (a single cell, or an nx x ny network of
+ * one type).  gbrkc_server_start sizes each class's arena -- explicit slot
+ * counts first, then shares of the rest of the HBM budget (0: 80% of the
+ * free device memory) -- and builds one engine holding every slot, idle.
+ * A request names a class, a number of systems and a duration in 0.125 ms
+ * intervals, with per-cell jitters, stimulus (times relative to the
+ * request's start), conductance scales and IO edge conductances.  Each
+ * gbrkc_request_advance is one serving round: admit the queued requests
+ * whose systems fit the free slots (first come first served; a later
+ * request that fits may overtake a head that does not, at most 8 times),
+ * advance every resident request by the quantum in one persistent launch
+ * (each stops at exactly its own interval count), route the device raster
+ * to the requests, and complete the requests that are done.  A served
+ * request's results are bit-identical to an engine of its own started at 0.
+ * Latency is submission to completion, on the host's steady clock. */
+typedef struct gbrkc_server gbrkc_server;
+enum { GBRKC_REQ_QUEUED = 0, GBRKC_REQ_RESIDENT = 1, GBRKC_REQ_DONE = 2, GBRKC_REQ_FAILED = 3 };
+
+typedef struct gbrkc_slot_class {
+  gbrkc_system_desc shape;  /* type, grid, morphology, junctions, tol, hmin (per-cell inputs ignored) */
+  long long slots;          /* systems to hold, or 0 ... */
+  double share;             /* ... a fraction of the budget left after the explicit classes */
+} gbrkc_slot_class;
+
+typedef struct gbrkc_request_desc {
+  int class_id;
+  int n_systems;            /* systems of the class's shape */
+  int n_intervals;          /* duration in 0.125 ms intervals */
+  const double *jitter;     /* per cell (n_systems x cells per system) */
+  const int *stim_comp;     /* per cell, or NULL */
+  const double *stim_amp, *stim_t0, *stim_t1;  /* per cell; times from the request's start */
+  const double *cond_scale; /* per cell, or NULL */
+  const double *io_gap_g;   /* IO networks: 4 per cell, or NULL */
+} gbrkc_request_desc;
+
+typedef struct gbrkc_server_stats_t {
+  long long submitted, admitted, completed, failed, cancelled, queued, resident, rounds;
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* latency of the completed requests */
+  double busy_s;            /* host time inside gbrkc_request_advance */
+  double advance_s;         /* of which inside the engine's advance */
+  long long compartment_updates;
+  long long hbm_reserved, hbm_in_use;      /* arena bytes: all slots, occupied slots */
+  long long slots, free_slots;
+  double sim_ms;            /* the server's clock */
+  long long lost_spike_reads;
+} gbrkc_server_stats_t;
+
+int gbrkc_server_create(int precision, long long hbm_budget, int quantum_intervals, gbrkc_server **out);
+int gbrkc_server_add_class(gbrkc_server *s, const gbrkc_slot_class *c, int *class_id);
+int gbrkc_server_start(gbrkc_server *s);
+int gbrkc_server_class_slots(gbrkc_server *s, int class_id, int *slots, int *first_system);
+int gbrkc_request_create(gbrkc_server *s, const gbrkc_request_desc *d, int *req_id);
+int gbrkc_request_advance(gbrkc_server *s, int *n_completed);
+int gbrkc_request_state(gbrkc_server *s, int req_id, int *state, double *latency_ms, int *status);
+/* final v_new of every compartment of the request, systems in order */
+int gbrkc_request_read(gbrkc_server *s, int req_id, double *host, long cap);
+/* threshold crossings: times from the request's start, cells in request order */
+int gbrkc_request_spikes(gbrkc_server *s, int req_id, long cap, double *t, int *cell, long *n);
+/* cancel a queued or resident request, or forget a finished one */
+int gbrkc_request_destroy(gbrkc_server *s, int req_id);
+int gbrkc_server_stats(gbrkc_server *s, gbrkc_server_stats_t *out);
+gbrkc_engine *gbrkc_server_engine(gbrkc_server *s);
+const char *gbrkc_server_last_error(void);
+void gbrkc_server_destroy(gbrkc_server *s);
 
 #ifdef __cplusplus
 }

@@ -28,7 +28,7 @@ class Desc(C.Structure):
         ("io_gap_g", C.POINTER(C.c_double)),
         ("tol", C.c_double), ("hmin", C.c_double),
         ("io_gap", C.c_int), ("go_gj", C.c_int), ("pkj_gj", C.c_int),
-        ("canon", C.c_int),
+        ("canon", C.c_int), ("cond_scale", C.POINTER(C.c_double)),
     ]
 
 
@@ -133,7 +133,7 @@ class System:
 
     def __init__(self, cell_type, nx, ny, rows, jitter, stim=None, gj_pairs=None,
                  tol=0.0, hmin=0.0, io_gap=True, go_gj=True, pkj_gj=True, io_gap_g=None,
-                 canon=False):
+                 canon=False, cond_scale=None):
         L = lib()
         self._keep = []
         rows = np.ascontiguousarray(rows, dtype=np.float64)
@@ -163,6 +163,10 @@ class System:
         d.tol, d.hmin = tol, hmin
         d.io_gap, d.go_gj, d.pkj_gj = int(io_gap), int(go_gj), int(pkj_gj)
         d.canon = int(canon)
+        if cond_scale is not None:
+            cs = np.ascontiguousarray(np.broadcast_to(cond_scale, n), dtype=np.float64)
+            d.cond_scale = _dp(cs)
+            self._keep.append(cs)
         self.h = L.orc_create(C.byref(d))
         if not self.h:
             raise RuntimeError("orc_create failed")

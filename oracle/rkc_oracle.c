@@ -1169,6 +1169,9 @@ orc_sys *orc_create(const orc_desc *d) {
   }
   alloc_state(s);
   if (setup_cells(s, d) != 0) { orc_destroy(s); return NULL; }
+  if (d->cond_scale)
+    for (int i = 0; i < s->nc; i++)
+      for (int k = 0; k < s->ncond; k++) s->cond[k][i] = s->cond[k][i] * d->cond_scale[i / s->ncomp];
   /* the reference computes the initial gating on the host with libm
    * (*_initialize_ion), so both modes use the platform exp here */
   g_canon = 0;

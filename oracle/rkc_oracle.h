@@ -52,6 +52,8 @@ typedef struct {
   int go_gj, pkj_gj;   /* 1 = add the linear GJ entries to the CSR (reference: n > 1) */
   int canon;           /* 1 = canonical arithmetic (canon_math.h), bit-comparable with
                           the GPU plain-FP64 path; 0 = the reference's literal expressions */
+  const double *cond_scale; /* n factors on every channel density of a cell, NULL = 1
+                          (synthetic variation; the reference's densities are fixed) */
 } orc_desc;
 
 orc_sys *orc_create(const orc_desc *d);
