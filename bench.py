@@ -114,6 +114,136 @@ def workload(name, scale=1.0):
     raise SystemExit(f"unknown config {name}")
 
 
+# ------------------------------------------------------------ serving
+def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8):
+    """Serve a Poisson request stream (configs.serve_workload) through the
+    request server on the wall clock: requests are submitted when their
+    arrival time has passed, every round admits what fits and advances all
+    resident requests one quantum.  Latency = completion - arrival.  Then a
+    sample of the same requests runs one at a time, each in its own plain
+    FP64 engine (build, advance, read back), for the throughput ratio and the
+    served results' voltage error and spike counts against FP64."""
+    import configs
+    classes, reqs = configs.serve_workload(n_requests, seed=seed)
+    prec = G.MIXED if precision == "mixed" else G.FP64
+    srv = G.Server(prec, 0, quantum)
+    cids = [srv.add_class(c.cell_type, c.nx, c.ny, c.rows, slots=c.slots, gap=c.gap) for c in classes]
+    t_build = time.perf_counter()
+    srv.start()
+    build_s = time.perf_counter() - t_build
+
+    def submit(r):
+        return srv.submit(cids[r.cls], r.n_systems, r.n_intervals, r.jitter, stim=r.stim, cond_scale=r.cond_scale,
+                          io_gap_g=r.io_gap_g)
+
+    # warm-up: one short request per class, run to completion, not counted
+    _, warm = configs.serve_workload(len(classes) * 4, seed=seed + 100)
+    seen = set()
+    for r in warm:
+        if r.cls not in seen:
+            seen.add(r.cls)
+            r.n_intervals = 16
+            submit(r)
+    while srv.stats()["resident"] + srv.stats()["queued"] > 0:
+        srv.advance()
+    st0 = srv.stats()
+    ids, arrive, done_at = [], [], {}
+    nxt = 0
+    t0 = time.perf_counter()
+    while True:
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt].arrival_s <= now:
+            ids.append(submit(reqs[nxt]))
+            arrive.append(reqs[nxt].arrival_s)
+            nxt += 1
+        st = srv.stats()
+        if st["queued"] + st["resident"] == 0:
+            if nxt == len(reqs):
+                break
+            time.sleep(max(0.0, reqs[nxt].arrival_s - (time.perf_counter() - t0)))
+            continue
+        srv.advance()
+        tnow = time.perf_counter() - t0
+        for k, rid in enumerate(ids):
+            if k not in done_at and srv.state(rid)[0] in (G.REQ_DONE, G.REQ_FAILED):
+                done_at[k] = tnow
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    lat = np.array([(done_at[k] - arrive[k]) * 1e3 for k in range(len(ids))])
+    cu = st["compartment_updates"] - st0["compartment_updates"]
+    sim_cell_ms = sum(r.n_systems * classes[r.cls].nx * classes[r.cls].ny * r.n_intervals * H_MAX for r in reqs)
+    failures = []
+    for k, rid in enumerate(ids):
+        state, _, status = srv.state(rid)
+        if state == G.REQ_FAILED:
+            r = reqs[k]
+            failures.append({"class": classes[r.cls].name, "systems": r.n_systems, "intervals": r.n_intervals,
+                             "status": status})
+    out = {"requests": len(ids), "failed": st["failed"] - st0["failed"], "failures": failures, "wall_s": wall,
+           "value": cu / wall, "unit": "compartment-updates/s",
+           "latency_ms": {"p50": float(np.percentile(lat, 50, method="inverted_cdf")),
+                          "p99": float(np.percentile(lat, 99, method="inverted_cdf")),
+                          "mean": float(lat.mean()), "max": float(lat.max()),
+                          "from": "arrival (Poisson, wall clock) to completion"},
+           "rounds": st["rounds"] - st0["rounds"], "quantum_intervals": quantum,
+           "engine_share": (st["advance_s"] - st0["advance_s"]) / wall,
+           "hbm_reserved_gb": st["hbm_reserved"] / 1e9, "slots": st["slots"],
+           "sim_cell_ms_per_wall_s": sim_cell_ms / wall, "arena_build_s": build_s,
+           "workload": (f"{len(reqs)} requests, Poisson 200/s; 20% IO 4x4 network sets (1-8), else 1-4096 GrC x4 "
+                        f"/ 1-128 GoC x131 (6 shapes) / 1-16 PC x1600 (5 shapes); 5-25 ms each; seed {seed}")}
+    # one request at a time, plain FP64, on a sample of the same requests
+    sample = []
+    for ty in (0, 1, 2, 3):
+        sample += [k for k, r in enumerate(reqs) if classes[r.cls].cell_type == ty][:max(1, n_compare // 4)]
+    seq_cu, seq_wall, err, spk_same, spk_total = 0, 0.0, 0.0, 0, 0
+    per_type = {}  # type -> [cell-ms, wall s]
+
+    def cell_ms(r):
+        c = classes[r.cls]
+        return r.n_systems * c.nx * c.ny * r.n_intervals * H_MAX
+
+    for k in sample:
+        r, c = reqs[k], classes[reqs[k].cls]
+        cells = c.nx * c.ny
+        w0 = time.perf_counter()
+        eng = G.Engine(G.FP64)
+        for j in range(r.n_systems):
+            sl = slice(j * cells, (j + 1) * cells)
+            eng.add_system(c.cell_type, c.nx, c.ny, c.rows, r.jitter[sl], stim=tuple(a[sl] for a in r.stim),
+                           gap=c.gap, cond_scale=r.cond_scale[sl],
+                           io_gap_g=None if r.io_gap_g is None else r.io_gap_g[4 * j * cells:4 * (j + 1) * cells])
+        eng.build()
+        eng.record_spikes(1 << 20)
+        eng.advance(0.0, r.n_intervals, tolerate_retire=True)
+        v = np.concatenate([eng.read(j, G.F_VNEW) for j in range(r.n_systems)])
+        dt = time.perf_counter() - w0
+        seq_wall += dt
+        seq_cu += eng.compartment_updates(-1)
+        pt = per_type.setdefault(c.cell_type, [0.0, 0.0])
+        pt[0] += cell_ms(r)
+        pt[1] += dt
+        ft, _, _ = eng.read_spikes(c.cell_type)
+        eng.close()
+        got = srv.read(ids[k], v.size)
+        err = max(err, float(np.max(np.abs(got - v))))
+        gt, _ = srv.spikes(ids[k])
+        spk_same += int(len(gt) == len(ft))
+        spk_total += 1
+    # the whole stream served one request at a time: each request's cell-ms
+    # at its type's sampled sequential rate
+    est = sum(cell_ms(r) * per_type[classes[r.cls].cell_type][1] / per_type[classes[r.cls].cell_type][0]
+              for r in reqs)
+    out["one_at_a_time_fp64"] = {"requests_sampled": len(sample), "value": seq_cu / seq_wall,
+                                 "unit": "compartment-updates/s (sample)",
+                                 "stream_makespan_s_est": est,
+                                 "includes": "engine build, advance and read-back per request"}
+    out["vs_one_at_a_time_fp64"] = est / wall
+    out["served_vs_fp64"] = {"max_abs_err_mv": err, "spike_counts_equal": f"{spk_same}/{spk_total}",
+                             "precision": precision}
+    srv.close()
+    return out
+
+
 # ------------------------------------------------------------ CPU side
 def _oracle_worker(args):
     """Run a slice of a sampled workload in the oracle (reference arithmetic)."""
@@ -230,7 +360,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbrkc", choices=["gbrkc", "reference"])
-    ap.add_argument("--config", default="mixed", choices=["mixed", "pkj3x3"])
+    ap.add_argument("--config", default="mixed", choices=["mixed", "pkj3x3", "serve"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
     ap.add_argument("--step-ms", type=float, default=5.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -238,17 +368,35 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population fraction of the mixed batch (small profiling cases; 1 = the benchmark)")
+    ap.add_argument("--serve-requests", type=int, default=None,
+                    help="requests of the serving stream (default 48 beside the mixed workload, 128 for "
+                         "--config serve; 0: none)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
         return
-    precision = args.precision or ("mixed" if args.config == "mixed" else "fp64")
+    precision = args.precision or ("fp64" if args.config == "pkj3x3" else "mixed")
     rank, world, dist = dist_init(args.gpus)
     import torch
     import gbrkc as G
     import configs
+    if args.config == "serve":
+        # the serving stream on its own: value = compartment-updates/s over the stream's wall time
+        sv = run_serve(G, precision, args.serve_requests or 128)
+        if rank == 0:
+            out = {"metric": "compartment-updates/s", "value": sv["value"], "unit": "compartment-updates/s",
+                   "n_gpus": world, "steps": 1, "warmup": args.warmup, "ms_per_step": sv["wall_s"] * 1e3,
+                   "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                   "dtype": "f64 state+stages, f32 gating" if precision == "mixed" else "f64",
+                   "data": "synthetic (seeded request stream)",
+                   "config": {"workload": sv["workload"], "precision": precision}, "serving": sv,
+                   "gpu_launches": sv["rounds"]}
+            print(json.dumps(out))
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     specs, wl = workload(args.config, args.scale)
     eng = G.Engine(G.MIXED if precision == "mixed" else G.FP64)
     configs.add_to(eng, specs)
@@ -393,6 +541,13 @@ def main():
         e2e = {"value": e_units / e_wall, "unit": "compartment-updates/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "timing": "host wall clock incl. pinned copies"}
 
+    n_compartments, n_retired = eng.total_compartments(), eng.retired()
+    serving = None
+    n_serve = 48 if args.serve_requests is None else args.serve_requests
+    if n_serve > 0 and rank == 0 and args.config == "mixed":
+        eng.close()
+        serving = run_serve(G, precision, n_serve)
+
     cpu = None
     if not args.no_cpu and rank == 0:
         # bounded single-thread sample of the same workload in the oracle
@@ -413,16 +568,18 @@ def main():
                "data": "synthetic (seeded morphologies, jitter and step currents)",
                "config": {"workload": wl, "precision": precision, "step_sim_ms": args.step_ms,
                           "cells": {k: v[0] for k, v in counts.items()},
-                          "compartments": eng.total_compartments(),
+                          "compartments": n_compartments,
                           "l2": "flushed (256 MB write) between timed steps",
                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                           "setup_s": round(setup_s, 2), "wall_s": round(wall, 3),
-                          "retired_systems": eng.retired(),
+                          "retired_systems": n_retired,
                           "sim_ms_per_wall_s": args.steps * args.step_ms / (t_max_ms * 1e-3),
                           "units_per_step": units / args.steps},
                "roofline": roofline, "gpu_launches": launches, "clocks": clk}
         if e2e:
             out["e2e"] = e2e
+        if serving:
+            out["serving"] = serving
         if cpu:
             out["cpu_baseline"] = cpu
         print(json.dumps(out))

@@ -114,6 +114,69 @@ def scaled_mixed_batch(fraction: float, seed=2):
                        n_pkj=max(1, int(256 * fraction)), io_side=16)
 
 
+@dataclass
+class ServeClass:
+    name: str
+    cell_type: int
+    nx: int
+    ny: int
+    rows: np.ndarray
+    slots: int
+    max_systems: int     # largest request of this class
+    stim_comp: int
+    gap: bool = False
+
+
+@dataclass
+class Request:
+    cls: int             # index into the class list
+    n_systems: int
+    n_intervals: int
+    arrival_s: float     # wall-clock arrival after the start
+    jitter: np.ndarray
+    stim: tuple
+    cond_scale: np.ndarray
+    io_gap_g: Optional[np.ndarray] = None
+
+
+def serve_workload(n_requests=64, seed=5, rate_hz=200.0, ts_ms=(5.0, 25.0), io_fraction=0.2):
+    """Request stream of the serving benchmark: Poisson arrivals at rate_hz;
+    each request is either an inferior-olive 4x4 gap-junction network set
+    (io_fraction; 1-8 networks, edge conductances G_C x U[0.5,1.5]) or
+    U{1..max} cells of one granule / Golgi / Purkinje shape; duration
+    U[ts_ms] rounded to whole 0.125 ms intervals; per-cell step currents
+    U[0, AMP_MAX] from t = 0 and channel densities x U[0.8, 1.2].  Request
+    sizes and durations are scaled down from 1-4096 cells and 50-1000 ms so
+    that the whole stream finishes in tens of seconds."""
+    rng = np.random.default_rng(seed)
+    classes = [ServeClass("gr", M.GR, 1, 1, M.gr_reduced4(), 8192, 4096, 1)]
+    for k in GO_STABLE_VARIANTS:
+        classes.append(ServeClass(f"go{k}", M.GO, 1, 1, M.go_synthetic(2000 + k), 192, 128, 30))
+    for k in PKJ_STABLE_SEEDS:
+        r = M.pkj_synthetic(k)
+        classes.append(ServeClass(f"pkj{k}", M.PKJ, 1, 1, r, 24, 16, r.shape[0] - 1))
+    classes.append(ServeClass("io4x4", M.IO, 4, 4, M.io_rows(), 32, 8, 0, gap=True))
+    by_type = {t: [i for i, c in enumerate(classes) if c.cell_type == t] for t in (M.GR, M.GO, M.PKJ, M.IO)}
+    reqs = []
+    t = 0.0
+    for _ in range(n_requests):
+        t += rng.exponential(1.0 / rate_hz)
+        if rng.uniform() < io_fraction:
+            ci = by_type[M.IO][0]
+        else:
+            ty = (M.GR, M.GO, M.PKJ)[rng.integers(0, 3)]
+            ci = by_type[ty][rng.integers(0, len(by_type[ty]))]
+        c = classes[ci]
+        n_sys = int(rng.integers(1, c.max_systems + 1))
+        cells = n_sys * c.nx * c.ny
+        n_iv = int(round(rng.uniform(*ts_ms) / 0.125))
+        amp = rng.uniform(0, AMP_MAX[c.cell_type], cells)
+        stim = (np.full(cells, c.stim_comp, np.int32), amp, np.zeros(cells), np.full(cells, 1e9))
+        gg = G_C_IO * rng.uniform(0.5, 1.5, 4 * cells) if c.cell_type == M.IO else None
+        reqs.append(Request(ci, n_sys, n_iv, t, _jitter(rng, cells), stim, rng.uniform(0.8, 1.2, cells), gg))
+    return classes, reqs
+
+
 def add_to(engine, specs):
     ids = []
     for s in specs:

@@ -27,6 +27,22 @@ __device__ __forceinline__ float mabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double mmin(double a, double b) { return fmin(a, b); }
 __device__ __forceinline__ float mmin(float a, float b) { return fminf(a, b); }
 
+// c * x / (1 - exp(-x / k)), the form of many Hodgkin-Huxley rate functions,
+// with a removable singularity at x = 0 (limit c * k).  FP64 evaluates the
+// reference's expression as written (the voltage would have to hit the
+// singular point exactly).  FP32 gating rounds the voltage to float first, so
+// x = 0 comes up about 10^8 times more often (0 / 0 = NaN stops the cell);
+// there, for |x / k| < 1e-3, the series c k (1 + u/2 + u^2/12), u = x / k, is
+// used instead -- the guard NEURON's hh.mod applies in its vtrap function.
+template <typename R>
+__device__ __forceinline__ R hh_xr(R c, R x, R k) {
+  if constexpr (sizeof(R) == 4) {
+    const R u = x / k;
+    if (mabs(u) < R(1e-3)) return c * k * (R(1) + u * (R(0.5) + u * R(1.0 / 12.0)));
+  }
+  return c * x / (R(1) - mexp(-x / k));
+}
+
 // trapezoid gate step of every RKC ion kernel: (2 dt x_inf + (2 tau - dt) x) / (2 tau + dt)
 template <typename R>
 __device__ __forceinline__ R trap(R dt, R inf, R tau, R x) {
@@ -165,8 +181,9 @@ template <typename R> struct Pkj {
 template <typename R> struct Io {
   __device__ static R ar(R v) { return (R(1.7)) / (R(1.0) + mexp((-(v - R(5.0))) / R(13.9))); }
   __device__ static R as(R x) { return mmin(R(0.00002) * x, R(0.01)); }
-  __device__ static R ax(R v) { return (R(0.13) * (v + R(25.0))) / (R(1.0) - mexp(-(v + R(25.0)) / R(10.0))); }
-  __device__ static R br(R v) { return (R(0.02) * (v + R(8.5))) / (mexp((v + R(8.5)) / R(5.0)) - R(1.0)); }
+  // 0.13 (v + 25) / (1 - exp(-(v + 25) / 10)) and 0.02 (v + 8.5) / (exp((v + 8.5) / 5) - 1)
+  __device__ static R ax(R v) { return hh_xr(R(0.13), v + R(25.0), R(10.0)); }
+  __device__ static R br(R v) { return -hh_xr(R(0.02), v + R(8.5), R(-5.0)); }
   __device__ static R bx(R v) { return R(1.69) * mexp(R(-0.0125) * (v + R(35.0))); }
   __device__ static R n_tau(R v) { return R(47.0) * mexp((-(-v - R(50.0))) / R(900.0)) + R(5.0); }
 
@@ -567,7 +584,7 @@ template <typename R> struct Go {
     Ca_val = (Ca_val + ca) / 2.0;
     const R v = (R)v_val, dt = (R)DT, c = (R)Ca_val;
     {  // m_NaT
-      R a = R(0.417) * (v + R(25.0)) / (R(1) - mexp(-(v + R(25.0)) / R(10.0)));
+      R a = hh_xr(R(0.417), v + R(25.0), R(10.0));
       R b = R(16.68) * mexp(R(-0.055) * (v + R(50.0)));
       s.x(GO_m_NaT) = trap(dt, a / (a + b), R(1.0) / (a + b), s.x(GO_m_NaT));
     }
@@ -577,10 +594,15 @@ template <typename R> struct Go {
       s.x(GO_h_NaT) = trap(dt, a / (a + b), R(1.0) / (a + b), s.x(GO_h_NaT));
     }
     {  // r_NaR
-      R a = ((R(1.11) - R(68.5) * (v - R(4.48)) / (mexp(-(v - R(4.48)) / R(6.8)) - R(1.0))) * R(1.0e-4));
+      // (1.11 - 68.5 (v - 4.48) / (exp(-(v - 4.48) / 6.8) - 1)) 1e-4
+      R a = ((R(1.11) + hh_xr(R(68.5), v - R(4.48), R(6.8))) * R(1.0e-4));
       R x = (v + R(44.0)) / R(0.11);
       if (x > R(200.0)) x = R(200.0);
-      R b = ((R(66.0) + R(21.7) * (v + R(44)) / (mexp(x) - R(1.0))) * R(1.0e-3));
+      R b;
+      if (sizeof(R) == 4 && mabs(x) < R(1e-3))  // the same guard: 21.7 (v + 44) / (e^x - 1) -> 21.7 * 0.11
+        b = (R(66.0) + R(21.7) * R(0.11) * (R(1) - x * (R(0.5) - x * R(1.0 / 12.0)))) * R(1.0e-3);
+      else
+        b = ((R(66.0) + R(21.7) * (v + R(44)) / (mexp(x) - R(1.0))) * R(1.0e-3));
       s.x(GO_r_NaR) = trap(dt, a / (a + b), R(1.0) / (a + b), s.x(GO_r_NaR));
     }
     {  // s_NaR
@@ -589,12 +611,12 @@ template <typename R> struct Go {
       s.x(GO_s_NaR) = trap(dt, a / (a + b), R(1.0) / (a + b), s.x(GO_s_NaR));
     }
     {  // p_NaP
-      R a = (R(0.421) * (v + R(40.0)) / (R(1.0) - mexp(-(v + R(40.0)) / R(5.0))));
-      R b = (R(-0.287) * (v + R(40.0)) / (R(1.0) - mexp((v + R(40.0)) / R(5.0))));
+      R a = hh_xr(R(0.421), v + R(40.0), R(5.0));
+      R b = hh_xr(R(-0.287), v + R(40.0), R(-5.0));  // -0.287 (v + 40) / (1 - exp((v + 40) / 5))
       s.x(GO_p_NaP) = trap(dt, (R(1) / (R(1.0) + mexp(-(v + R(43.0)) / R(5.0)))), (R(5.0) / (a + b)), s.x(GO_p_NaP));
     }
     {  // n_KV
-      R a = R(0.062) * (v + R(26.0)) / (R(1.0) - mexp(-(v + R(26.0)) / R(10.0)));
+      R a = hh_xr(R(0.062), v + R(26.0), R(10.0));
       R b = R(0.78) * mexp(-(v + R(36.0)) / R(80.0));
       s.x(GO_n_KV) = trap(dt, a / (a + b), R(1.0) / (a + b), s.x(GO_n_KV));
     }

@@ -129,6 +129,8 @@ def lib() -> C.CDLL:
         L.gbrkc_set_budget.argtypes = [P, C.c_int, C.c_int, C.c_int]
         L.gbrkc_system_bytes.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int]
         L.gbrkc_system_bytes.restype = C.c_longlong
+        L.gbrkc_run_status.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.gbrkc_read_run.argtypes = [P, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_long]
         L.gbrkc_record_spikes.argtypes = [P, C.c_long]
         L.gbrkc_read_spikes.argtypes = [P, C.c_int, C.c_long, C.POINTER(C.c_double), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), C.POINTER(C.c_long)]
@@ -256,6 +258,18 @@ class Engine:
 
     def set_budget(self, first: int, n: int, n_intervals: int):
         _check(lib().gbrkc_set_budget(self.h, first, n, n_intervals))
+
+    def run_status(self, first: int, n: int):
+        """Status words and interval budgets left of systems first .. first+n-1 (one run)."""
+        st = np.empty(n, np.int32)
+        left = np.empty(n, np.int32)
+        _check(lib().gbrkc_run_status(self.h, first, n, _ip(st), _ip(left)))
+        return st, left
+
+    def read_run(self, first: int, n: int, field: int, n_values: int) -> np.ndarray:
+        out = np.empty(n_values, np.float64)
+        _check(lib().gbrkc_read_run(self.h, first, n, field, _dp(out), n_values))
+        return out
 
     def record_spikes(self, capacity: int):
         _check(lib().gbrkc_record_spikes(self.h, capacity))
