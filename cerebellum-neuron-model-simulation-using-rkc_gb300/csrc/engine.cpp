@@ -744,20 +744,28 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
     P.block = MEGA_BLOCK;
   }
   else if (P.max_nc <= 320) { P.team = TEAM_WARP; P.block = 128; }
-  else if (P.max_nc >= cluster_min_nc()) { P.team = TEAM_CLUSTER8; P.block = 256; }
+  else if (P.max_nc >= cluster_min_nc()) { P.team = TEAM_CLUSTER16; P.block = 256; }
   else { P.team = TEAM_BLOCK; P.block = 256; }
-  if (P.team == TEAM_CLUSTER8) {
-    // the workspace spread block-cyclically over 8 CTAs of 256 threads
-    const long slot = (long)((((P.max_nc + 1) & ~1) + 2047) / 2048) * 256;
-    const size_t need = (size_t)WS_VECS * slot * sizeof(double);
-    if (need <= 200 * 1024) {
-      int dev = 0, sms = 8;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (P.team == TEAM_CLUSTER16) {
+    // the workspace spread block-cyclically over the cluster's CTAs of 256
+    // threads: 16 CTAs where the device co-schedules them (more FP64 pipes
+    // per system), else 8; GBRKC_CLUSTER_SIZE=8 or 16 forces one
+    const char *cs = getenv("GBRKC_CLUSTER_SIZE");
+    const int forced = cs ? atoi(cs) : 0;
+    for (int team : {TEAM_CLUSTER16, TEAM_CLUSTER8}) {
+      const int C = team_cluster_size(team);
+      if (forced && forced != C) continue;
+      const long slot = (long)((((P.max_nc + 1) & ~1) + 256 * C - 1) / (256 * C)) * 256;
+      const size_t need = ((size_t)WS_VECS * slot + CLUSTER_RED_DOUBLES) * sizeof(double);
+      if (need > 200 * 1024 || slot / 256 > CLUSTER_MAX_ROWS) continue;
+      const int cap = (E->precision == GBRKC_FP64) ? cluster_capacity<double>(P.type, team, need)
+                                                   : cluster_capacity<float>(P.type, team, need);
+      if (cap < 1) continue;
+      P.team = team;
       P.ws_tile = (long)WS_VECS * slot;
       P.ws_in_smem = 1;
       P.smem = need;
-      P.grid = 8 * std::max(1, std::min(nsys, sms / 8));
+      P.grid = C * std::max(1, std::min(nsys, cap));
       return 0;
     }
     P.team = TEAM_BLOCK;  // too large to stage: one CTA with the workspace in HBM
@@ -1056,7 +1064,7 @@ int setup_mega(gbrkc_engine *E) {
   if (no && no[0] == '1') return 0;
   // pools of very large systems run on clusters, one launch per pool
   for (int t = 0; t < NTYPES; t++)
-    if (!E->pools[t].systems.empty() && E->pools[t].team == TEAM_CLUSTER8) return 0;
+    if (!E->pools[t].systems.empty() && team_cluster_size(E->pools[t].team) > 0) return 0;
   const PoolHost &G = E->pools[GR], &O = E->pools[GO];
   if (!G.systems.empty() && G.max_nc > LANE_MAX_NC) return 0;
   if (!O.systems.empty() && O.max_nc > 320) return 0;
@@ -1557,7 +1565,8 @@ extern "C" float gbrkc_last_advance_ms(gbrkc_engine *E) { return E ? E->last_ms 
 
 extern "C" int gbrkc_launch_layout(gbrkc_engine *E, int *ctas_per_type) {
   if (!E || !E->built) return fail(GBRKC_ESTATE, "engine not built");
-  for (int t = 0; t < NTYPES; t++) ctas_per_type[t] = E->mega ? E->role_ctas[t] : -1;
+  for (int t = 0; t < NTYPES; t++)
+    ctas_per_type[t] = E->mega ? E->role_ctas[t] : E->pools[t].systems.empty() ? 0 : E->pools[t].grid;
   return E->mega ? 1 : 0;
 }
 extern "C" float gbrkc_last_kernel_ms(gbrkc_engine *E, int type) {

@@ -151,8 +151,16 @@ int launch_syn_update(const SynView &S, void *stream, double t, long long interv
 // workspaces), 4 or 32 lanes per system, or a whole block per system.
 // TEAM_LANE4: one thread per system for pools whose systems all have exactly
 // 4 compartments (loops unrolled at compile time).
-// TEAM_CLUSTER8: one system per cluster of 8 CTAs (very large systems).
-enum TeamKind { TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0, TEAM_CLUSTER8 = 108 };
+// TEAM_CLUSTER8 / TEAM_CLUSTER16: one system per cluster of 8 / 16 CTAs
+// (very large systems; 16 is a non-portable cluster size, used where the
+// device can co-schedule it).
+enum TeamKind {
+  TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0,
+  TEAM_CLUSTER8 = 108, TEAM_CLUSTER16 = 116
+};
+constexpr int team_cluster_size(int team) {
+  return team == TEAM_CLUSTER8 ? 8 : team == TEAM_CLUSTER16 ? 16 : 0;
+}
 
 // All pools in one persistent launch: CTA b < role_end[0] integrates granule
 // systems (one per lane, on the CTA's first warps), then Golgi
@@ -170,6 +178,13 @@ struct MegaView {
 };
 
 constexpr int MEGA_BLOCK = 256;
+// Cluster teams: CTAs of CLUSTER_BLOCK threads; at most CLUSTER_MAX_ROWS rows
+// of CLUSTER_BLOCK elements per CTA and vector (the workspace of WS_VECS
+// vectors fits 200 KB of shared memory), followed by the reduction area:
+// block sums (double-buffered), warp partials, result.
+constexpr int CLUSTER_BLOCK = 256;
+constexpr int CLUSTER_MAX_ROWS = 14;
+constexpr int CLUSTER_RED_DOUBLES = 2 * CLUSTER_MAX_ROWS + 8 * CLUSTER_MAX_ROWS + 2;
 constexpr int LANE_MAX_NC = 8;   // largest system integrated by a single lane
 
 template <typename R>
@@ -184,5 +199,9 @@ int launch_pool(int type, const PoolView<R> &P, int team, int grid, int block, s
                 void *stream, double t0, int n_iv, int iv0, int init);
 template <typename R>
 int prepare_pool_kernel(int type, int team, size_t smem);
+// How many clusters of a cluster team's kernel the device can run at once
+// with this shared memory (0: the shape does not fit).
+template <typename R>
+int cluster_capacity(int type, int team, size_t smem);
 
 }  // namespace gbrkc

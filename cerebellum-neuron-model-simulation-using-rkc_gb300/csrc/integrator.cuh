@@ -91,7 +91,6 @@ struct LaneTeam {
 // are in its own CTA; others (a compartment's neighbours) are read and
 // written through distributed shared memory.  The team barrier is the
 // cluster barrier.
-constexpr int CLUSTER_BLOCK = 256;
 
 template <int C>
 struct CVec {
@@ -112,6 +111,7 @@ struct ClusterTeam {
   typedef CVec<C> Vec;
   int crank;                   // this CTA's rank in the cluster
   double *const *bases;        // [C] workspace bases (distributed shared memory)
+  long red_off;                // reduction area, after the workspace (CLUSTER_RED_DOUBLES)
   __device__ __forceinline__ Vec vec_at(double *, long off) const { return Vec{off, bases}; }
   __device__ __forceinline__ static long vstride(int ncp) {
     constexpr int SZ = C * CLUSTER_BLOCK;
@@ -259,6 +259,7 @@ struct Sys {
   double t0;
   int k_iv, n_iv, iv0, rej_run;
   long long attempts0;
+  mutable int red_buf = 0;     // cluster reductions: block-sum buffer in use
 
   __device__ Sys(const PoolView<R> &P_, const Team &tm_) : P(P_), tm(tm_) {}
   __device__ Sys(const PoolView<R> &P_, const Team &tm_, int s_, double *W_) : P(P_), tm(tm_) { bind(s_, W_); }
@@ -313,6 +314,7 @@ struct Sys {
 
   // pairwise tree over a[0..n): stride doubling, identical to the oracle
   __device__ __forceinline__ double tree_sum(const V a, int n) const {
+    if constexpr (Team::CLUSTER > 0) return cluster_tree_sum(a, n);
     tm.sync();
     for (int stride = 1; stride < n; stride *= 2) {
       const int step = 2 * stride;
@@ -322,6 +324,79 @@ struct Sys {
     const double r = a[0];
     tm.sync();
     return r;
+  }
+
+  // tree_sum on a cluster team, the same additions in the same order with
+  // one cluster barrier instead of one per level.  Element i is owned by the
+  // thread that writes it in the team loops (every caller fills a[] that
+  // way), and aligned blocks of CLUSTER_BLOCK elements lie in one CTA, one
+  // element per thread: levels 0-4 are warp shuffles, 5-7 combine the 8 warp
+  // partials of a block, and levels 8 and up combine block sums -- read by
+  // one warp of every CTA through distributed shared memory after the
+  // barrier, every CTA computing the same value.  The block sums are double
+  // buffered: the next reduction's writes come after the next barrier, which
+  // no CTA passes before every CTA has read this one's.
+  __device__ __forceinline__ double cluster_tree_sum(const V a, int n) const {
+    constexpr int C = Team::CLUSTER, B = CLUSTER_BLOCK, RR = (CLUSTER_MAX_ROWS * C + 31) / 32;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5, q = tm.crank;
+    const int rows = (int)(Team::vstride(ncp) / B);
+    double *red = tm.bases[q] + tm.red_off;
+    double *wp = red + 2 * CLUSTER_MAX_ROWS, *res = wp + 8 * CLUSTER_MAX_ROWS;
+    const int buf = red_buf;
+    red_buf ^= 1;
+    for (int k = 0; k < rows; k++) {
+      const int i0 = (k * C + q) * B;
+      if (i0 >= n) break;
+      const int i = i0 + t;
+      double x = (i < n) ? a[i] : 0.0;
+#pragma unroll
+      for (int st = 1; st < 32; st *= 2) {
+        const double y = __shfl_down_sync(0xffffffffu, x, st);
+        if ((lane & (2 * st - 1)) == 0 && i + st < n) x = x + y;
+      }
+      if (lane == 0) wp[k * 8 + warp] = x;
+    }
+    __syncthreads();
+    if (t < rows) {
+      const int i0 = (t * C + q) * B;
+      if (i0 < n) {
+        double w[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) w[j] = wp[t * 8 + j];
+#pragma unroll
+        for (int st = 1; st < 8; st *= 2)
+#pragma unroll
+          for (int j = 0; j + st < 8; j += 2 * st)
+            if (i0 + (j + st) * 32 < n) w[j] = w[j] + w[j + st];
+        red[buf * CLUSTER_MAX_ROWS + t] = w[0];
+      }
+    }
+    tm.sync();
+    if (warp == 0) {
+      const int nb = (n + B - 1) / B;
+      double v[RR];
+#pragma unroll
+      for (int r = 0; r < RR; r++) {
+        const int b = lane + 32 * r;
+        v[r] = (b < nb) ? tm.bases[b % C][tm.red_off + buf * CLUSTER_MAX_ROWS + b / C] : 0.0;
+      }
+#pragma unroll
+      for (int st = 1; st < 32; st *= 2)
+#pragma unroll
+        for (int r = 0; r < RR; r++) {
+          if (32 * r >= nb) break;
+          const double y = __shfl_down_sync(0xffffffffu, v[r], st);
+          if ((lane & (2 * st - 1)) == 0 && lane + 32 * r + st < nb) v[r] = v[r] + y;
+        }
+#pragma unroll
+      for (int st = 1; st < RR; st *= 2)
+#pragma unroll
+        for (int r = 0; r + st < RR; r += 2 * st)
+          if (32 * (r + st) < nb) v[r] = v[r] + v[r + st];
+      if (lane == 0) *res = v[0];
+    }
+    __syncthreads();
+    return *res;
   }
 
   template <class A>

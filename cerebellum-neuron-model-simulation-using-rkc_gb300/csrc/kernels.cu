@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK, 1) k_advance_cluster(const __gr
   cg::cluster_group cl = cg::this_cluster();
   if (threadIdx.x < C) s_bases[threadIdx.x] = cl.map_shared_rank(smem, (int)threadIdx.x);
   cl.sync();
-  const ClusterTeam<C> tm{(int)cl.block_rank(), s_bases};
+  const ClusterTeam<C> tm{(int)cl.block_rank(), s_bases, P.ws_tile_doubles};
   const int ncl = gridDim.x / C, cid = blockIdx.x / C;
   for (int s = cid; s < P.nsys; s += ncl) run_system<CT, R, ClusterTeam<C>>(P, tm, s, smem, t0, n_iv, iv0, init != 0);
   // no CTA leaves while a peer may still reach its shared memory
@@ -152,6 +152,7 @@ template <int CT, typename R>
 static const void *kernel_for(int team) {
   switch (team) {
     case TEAM_CLUSTER8: return (const void *)k_advance_cluster<CT, R, 8>;
+    case TEAM_CLUSTER16: return (const void *)k_advance_cluster<CT, R, 16>;
     case TEAM_LANE4:
       // instantiated for granule pools only (the others never have it)
       if constexpr (CT == GR) return (const void *)k_advance<CT, R, TEAM_LANE4>;
@@ -180,7 +181,43 @@ int prepare_pool_kernel(int type, int team, size_t smem) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
   }
+  if (team_cluster_size(team) > 8) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return (int)e;
+  }
   return 0;
+}
+
+static cudaLaunchConfig_t cluster_config(int team, int grid, size_t smem, cudaStream_t stream,
+                                         cudaLaunchAttribute *attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(CLUSTER_BLOCK);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = team_cluster_size(team);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+template <typename R>
+int cluster_capacity(int type, int team, size_t smem) {
+  if (prepare_pool_kernel<R>(type, team, smem) != 0) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchAttribute attr[1];
+  const cudaLaunchConfig_t cfg = cluster_config(team, team_cluster_size(team), smem, 0, attr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kernel_ptr<R>(type, team), &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
 }
 
 template <typename R>
@@ -189,19 +226,10 @@ int launch_pool(int type, const PoolView<R> &P, int team, int grid, int block, s
   const void *k = kernel_ptr<R>(type, team);
   PoolView<R> Pc = P;
   void *args[] = {(void *)&Pc, (void *)&t0, (void *)&n_iv, (void *)&iv0, (void *)&init};
-  if (team == TEAM_CLUSTER8) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = (cudaStream_t)stream;
+  if (team_cluster_size(team) > 0) {
+    if (block != CLUSTER_BLOCK || grid % team_cluster_size(team) != 0) return (int)cudaErrorInvalidConfiguration;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 8;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    const cudaLaunchConfig_t cfg = cluster_config(team, grid, smem, (cudaStream_t)stream, attr);
     return (int)cudaLaunchKernelExC(&cfg, k, args);
   }
   cudaError_t e = cudaLaunchKernel(k, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);

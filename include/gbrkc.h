@@ -129,7 +129,8 @@ float gbrkc_last_kernel_ms(gbrkc_engine *e, int cell_type);
 
 /* Launch layout: returns 1 when all cell types advance in one persistent
  * launch (CTAs per type written to ctas_per_type[4]), 0 when each type has
- * its own launch (entries -1), negative on error. */
+ * its own launch (entries: that launch's CTAs, 0 for an empty type),
+ * negative on error. */
 int gbrkc_launch_layout(gbrkc_engine *e, int *ctas_per_type);
 
 /* ---- chemical synapses (network mode) ----------------------------------

@@ -1,8 +1,8 @@
-"""Large systems on a thread-block cluster (8 CTAs, workspace spread
+"""Large systems on a thread-block cluster (8 or 16 CTAs, workspace spread
 block-cyclically over their shared memory, neighbour reads through
 distributed shared memory): bit for bit with the oracle, like every other
 team.  A low size threshold (GBRKC_CLUSTER_MIN_NC) sends the test cases down
-that path."""
+that path; GBRKC_CLUSTER_SIZE picks the cluster size."""
 import numpy as np
 import pytest
 
@@ -13,19 +13,24 @@ from test_gpu_parity import HORIZON, run_pair
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("csize", [8, 16])
 @pytest.mark.parametrize("name", ["pkj_cell", "pkj_2x1_gj", "gr_full"])
-def test_cluster_team_bit_exact(oracle, monkeypatch, name):
+def test_cluster_team_bit_exact(oracle, monkeypatch, name, csize):
     monkeypatch.setenv("GBRKC_CLUSTER_MIN_NC", "500")
+    monkeypatch.setenv("GBRKC_CLUSTER_SIZE", str(csize))
     n = HORIZON.get(name, 64)
     s, eng, sid = run_pair(oracle, name, [1, n // 2 - 1, n // 2])
-    assert eng.launch_layout()[0] is False
+    persistent, ctas = eng.launch_layout()
+    assert persistent is False and max(ctas) == csize, ctas
     eng.close()
 
 
-def test_cluster_io_network(oracle, monkeypatch):
+@pytest.mark.parametrize("csize", [8, 16])
+def test_cluster_io_network(oracle, monkeypatch, csize):
     """A 12x12 olive network (432 compartments, nonlinear gap junctions
     crossing CTA boundaries) on a cluster, against the oracle."""
     monkeypatch.setenv("GBRKC_CLUSTER_MIN_NC", "400")
+    monkeypatch.setenv("GBRKC_CLUSTER_SIZE", str(csize))
     O = oracle
     O.libc_srand(0)
     jit = O.draw_jitter(O.IO, 144)
@@ -35,6 +40,7 @@ def test_cluster_io_network(oracle, monkeypatch):
     eng = G.Engine(G.FP64)
     sid = eng.add_system(M.IO, 12, 12, M.io_rows(), jit, stim=stim, gap=True)
     eng.build()
+    assert max(eng.launch_layout()[1]) == csize
     t = 0.0
     for chunk in (1, 15, 16):
         eng.advance(t, chunk)
