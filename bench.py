@@ -114,6 +114,65 @@ def workload(name, scale=1.0):
     raise SystemExit(f"unknown config {name}")
 
 
+# ------------------------------------------------------------ FP64 comparison
+def fp64_compare(G, configs, specs, n_iv, warmup, k, step_ms, step_units, flush, torch):
+    """Plain FP64 on the same systems and time window as the first k timed
+    mixed steps (throughput ratio), then the mixed precision's accuracy on
+    a 1/16 sample of the workload: max |V_mixed - V_fp64| over every
+    compartment after 1 ms and after 5 ms, and the device raster's spike
+    counts over 20 ms."""
+    eng = G.Engine(G.FP64)
+    configs.add_to(eng, specs)
+    eng.build()
+    t = 0.0
+    for _ in range(warmup):
+        eng.advance(t, n_iv, tolerate_retire=True)
+        t += n_iv * H_MAX
+    ms, units = 0.0, 0
+    for _ in range(k):
+        flush.zero_()
+        torch.cuda.synchronize()
+        u0 = eng.compartment_updates(-1)
+        eng.advance(t, n_iv, tolerate_retire=True)
+        t += n_iv * H_MAX
+        ms += eng.last_advance_ms()
+        units += eng.compartment_updates(-1) - u0
+    eng.close()
+    fp64 = units / (ms * 1e-3)
+    mixed = sum(step_units[:k]) / (sum(step_ms[:k]) * 1e-3)
+    sample = configs.scaled_mixed_batch(1.0 / 16)
+    res = {}
+    for prec in (G.FP64, G.MIXED):
+        e = G.Engine(prec)
+        ids = configs.add_to(e, sample)
+        e.build()
+        e.record_spikes(1 << 20)
+        v = []
+        tt = 0.0
+        for n in (8, 32, 120):          # to 1 ms, 5 ms, 20 ms
+            e.advance(tt, n, tolerate_retire=True)
+            tt += n * H_MAX
+            v.append(np.concatenate([e.read(i, G.F_VNEW) for i in ids]))
+        counts = {}
+        for ty in range(4):
+            _, sy, ce = e.read_spikes(ty)
+            for a, b in zip(sy.tolist(), ce.tolist()):
+                counts[(a, b)] = counts.get((a, b), 0) + 1
+        res[prec] = (v, counts, e.retired())
+        e.close()
+    (v64, s64, r64), (v32, s32, r32) = res[G.FP64], res[G.MIXED]
+    return {"fp64_value": fp64, "mixed_value": mixed, "ratio": mixed / fp64, "steps": k,
+            "unit": "compartment-updates/s (same systems, same window)",
+            "accuracy_sample": "mixed batch x1/16 (256 GrC, 64 GoC, 16 PC, IO 16x16), from t = 0",
+            "max_abs_err_mv": {"1ms": float(np.max(np.abs(v32[0] - v64[0]))),
+                               "5ms": float(np.max(np.abs(v32[1] - v64[1]))),
+                               "20ms": float(np.max(np.abs(v32[2] - v64[2])))},
+            "spikes_20ms": {"fp64": sum(s64.values()), "mixed": sum(s32.values()),
+                            "cells_with_equal_counts": sum(1 for c in set(s64) | set(s32) if s64.get(c) == s32.get(c)),
+                            "cells_spiking": len(set(s64) | set(s32))},
+            "stopped_systems": {"fp64": r64, "mixed": r32}}
+
+
 # ------------------------------------------------------------ serving
 def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8):
     """Serve a Poisson request stream (configs.serve_workload) through the
@@ -368,6 +427,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population fraction of the mixed batch (small profiling cases; 1 = the benchmark)")
+    ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=None,
                     help="requests of the serving stream (default 48 beside the mixed workload, 128 for "
                          "--config serve; 0: none)")
@@ -413,6 +473,7 @@ def main():
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     dev_ms, kern_ms = 0.0, {k: 0.0 for k in range(4)}
+    step_ms, step_units = [], []
     units0 = eng.compartment_updates(-1)
     units_t0 = {k: eng.compartment_updates(k) for k in range(4)}
     if dist is not None:
@@ -422,9 +483,12 @@ def main():
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
+        u0 = eng.compartment_updates(-1)
         eng.advance(t, n_iv, tolerate_retire=True)
         t += n_iv * H_MAX
         dev_ms += eng.last_advance_ms()
+        step_ms.append(eng.last_advance_ms())
+        step_units.append(eng.compartment_updates(-1) - u0)
         for k in range(4):
             kern_ms[k] += eng.last_kernel_ms(k)
     torch.cuda.synchronize()
@@ -542,6 +606,14 @@ def main():
                "d2h_bytes_per_step": d2h, "timing": "host wall clock incl. pinned copies"}
 
     n_compartments, n_retired = eng.total_compartments(), eng.retired()
+
+    # the same systems in plain FP64 over the first timed steps (same warm-up),
+    # and the mixed precision's voltage error and spike counts against FP64
+    vs_fp64 = None
+    if precision == "mixed" and rank == 0 and not args.no_fp64_compare and args.config == "mixed":
+        eng.close()
+        vs_fp64 = fp64_compare(G, configs, specs, n_iv, args.warmup, min(3, args.steps), step_ms, step_units,
+                               flush, torch)
     serving = None
     n_serve = 48 if args.serve_requests is None else args.serve_requests
     if n_serve > 0 and rank == 0 and args.config == "mixed":
@@ -580,6 +652,8 @@ def main():
             out["e2e"] = e2e
         if serving:
             out["serving"] = serving
+        if vs_fp64:
+            out["vs_plain_fp64"] = vs_fp64
         if cpu:
             out["cpu_baseline"] = cpu
         print(json.dumps(out))

@@ -79,7 +79,7 @@ def build(verbose: bool = False) -> str:
     cli_src = os.path.join(CSRC, "cli.cpp")
     if os.path.exists(cli_src) and _newer(CLI, [cli_src, LIB]):
         cmd = [CXX] + CXXFLAGS + [cli_src, "-o", CLI, f"-L{HERE}", "-lgbrkc", f"-Wl,-rpath,{HERE}",
-                                  f"-L{CUDA_HOME}/lib64", "-lcudart"]
+                                  f"-L{CUDA_HOME}/lib64", "-lcudart", "-pthread"]
         subprocess.run(cmd, check=True)
     return LIB
 

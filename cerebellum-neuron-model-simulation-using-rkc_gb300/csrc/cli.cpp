@@ -1,6 +1,6 @@
 // gbrkc_main: the reference's command line over gbrkc_compat.h.
 //
-//   gbrkc_main S_gr gx gy S_go ox oy S_pkj px py S_io ix iy [TS_ms]
+//   gbrkc_main S_gr gx gy S_go ox oy S_pkj px py S_io ix iy [TS_ms [batch]]
 //
 // S is the solver name per type, matched on its first three letters as the
 // reference does (main.cu:60-102); only RKC is provided.  A type with
@@ -9,13 +9,25 @@
 // files are the reference's: <type>_v_by_RKC.csv, <type>_raster_by_RKC.csv,
 // comptime.csv (appended) and an empty debug_file.csv.  The jitter stream is
 // seeded with srand(0) first, as main.cu:38 does.  TS_ms (default 1500, the
-// reference's TS) is this tool's addition.
+// reference's TS) is this tool's addition, and so is batch: with batch > 1
+// each type advances `batch` intervals per device launch with its protocol,
+// voltage record and raster evaluated on the device
+// (gbrkc_compat_advance_batch), and a writer thread formats the same CSV
+// rows from the recorded columns while the GPU runs the next batch.  The
+// files are byte-identical to the per-interval path's.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
+
+#include <algorithm>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
 
 #include "../../include/gbrkc_compat.h"
 
@@ -41,6 +53,68 @@ void go_update(TypeRun &r) { go_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr); }
 void pkj_update(TypeRun &r) { pkj_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr, nullptr); }
 void io_update(TypeRun &r) { io_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr); }
 
+// One batch of recorded output of one type, written by the writer thread in
+// the order the batches were queued.
+struct Batch {
+  FILE *fv, *fr;
+  int type, n, cells, cols;
+  double t0;  // start of the batch's first interval
+  std::vector<double> rows;
+  std::vector<double> spk_t;
+  std::vector<int> spk_cell;
+};
+
+class Writer {
+ public:
+  Writer() : th_([this] { run(); }) {}
+  ~Writer() { finish(); }
+  void push(Batch &&b) {
+    std::lock_guard<std::mutex> g(m_);
+    q_.push_back(std::move(b));
+    cv_.notify_one();
+  }
+  void finish() {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      done_ = true;
+      cv_.notify_one();
+    }
+    if (th_.joinable()) th_.join();
+  }
+
+ private:
+  void run() {
+    for (;;) {
+      Batch b;
+      {
+        std::unique_lock<std::mutex> l(m_);
+        cv_.wait(l, [this] { return done_ || !q_.empty(); });
+        if (q_.empty()) return;
+        b = std::move(q_.front());
+        q_.pop_front();
+      }
+      write(b);
+    }
+  }
+  // output_file's rows: "%lf," time then the columns; raster "%lf,%d\n"
+  static void write(const Batch &b) {
+    size_t s = 0;
+    for (int i = 0; i < b.n; i++) {
+      const double t = b.t0 + (i + 1) * H_MAX;
+      fprintf(b.fv, "%lf,", t);
+      const double *r = b.rows.data() + (size_t)i * b.cells * b.cols;
+      for (int j = 0; j < b.cells * b.cols; j++) fprintf(b.fv, "%lf,", r[j]);
+      fprintf(b.fv, "\n");
+      while (s < b.spk_t.size() && b.spk_t[s] == t) fprintf(b.fr, "%lf,%d\n", t, b.spk_cell[s++]);
+    }
+  }
+  std::mutex m_;
+  std::condition_variable cv_;
+  std::deque<Batch> q_;
+  bool done_ = false;
+  std::thread th_;
+};
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -49,6 +123,11 @@ int main(int argc, char **argv) {
     return 1;
   }
   const double ts = (argc > 13) ? atof(argv[13]) : 1500.0;
+  const int batch = (argc > 14) ? atoi(argv[14]) : 1;
+  if (batch < 1) {
+    printf("batch must be >= 1\n");
+    return 1;
+  }
   srand(0);  // the initial-voltage jitter stream, seeded as main.cu:38 does
   TypeRun runs[4] = {
       {"gr", gr_initialize, gr_solve_initialize, gr_set_current_launch, gr_output_file, gr_finalize, gr_solve_finalize},
@@ -94,6 +173,50 @@ int main(int argc, char **argv) {
   double t = 0.0;
   const clock_t start = clock();
   clock_t half = start;
+  if (batch > 1) {
+    // intervals the per-interval loop below would run
+    long total = 0;
+    for (double tt = 0.0; tt < ts - 0.0001; tt += H_MAX) total++;
+    Writer w;
+    for (long done = 0; done < total;) {
+      const int n = (int)std::min<long>(batch, total - done);
+      for (int k = 0; k < 4; k++) {
+        TypeRun &r = runs[k];
+        if (r.p->n <= 0) continue;
+        Batch b;
+        b.fv = r.fv;
+        b.fr = r.fr;
+        b.type = k;
+        b.n = n;
+        b.cells = r.p->n;
+        b.cols = (k == 3) ? 3 : 1;
+        b.t0 = t;
+        b.rows.resize((size_t)n * b.cells * b.cols);
+        const long cap = (long)b.cells * (n / 2 + 1);
+        b.spk_t.resize(cap);
+        b.spk_cell.resize(cap);
+        const long m = gbrkc_compat_advance_batch(k, n, b.rows.data(), (long)b.rows.size(), b.spk_t.data(),
+                                                  b.spk_cell.data(), cap);
+        if (m == -5) {
+          w.finish();
+          printf("isnan in %s, time=%f\n", r.name, t);
+          return 1;
+        }
+        if (m < 0) {
+          printf("batched advance of %s failed (%ld)\n", r.name, m);
+          return 1;
+        }
+        b.spk_t.resize(m);
+        b.spk_cell.resize(m);
+        w.push(std::move(b));
+      }
+      const double t_prev = t;
+      for (int i = 0; i < n; i++) t += H_MAX;
+      if (t_prev < 500.0 && t >= 500.0) half = clock();
+      done += n;
+    }
+    w.finish();
+  }
   while (t < ts - 0.0001) {
     for (int k = 0; k < 4; k++) {
       TypeRun &r = runs[k];

@@ -29,6 +29,8 @@ struct Block {
   gbrkc_engine *eng = nullptr;
   int sid = -1;
   int n = 0, ncomp = 0;
+  int stim_comp = 0;              // compartment of every cell the protocol drives
+  int batch_cap = 0;              // batched output: intervals the recorder holds
   double t = 0.0;                 // start of the next interval
   neuron_t *d_neuron = nullptr;   // device copy of the mirror (for stimulus kernels)
   double **d_elem = nullptr;      // device table behind d_neuron->elem
@@ -170,6 +172,7 @@ neuron_t *initialize(int type, int nx, int ny, const char *solver, neuron_t *p) 
     check(gbrkc_field_device_ptr(B.eng, B.sid, GBRKC_F_IEXT, &B.h_elem[i_ext]), "elem[i_ext]");
     const int sc = (type == GBRKC_IO) ? 0 : (type == GBRKC_GO) ? 30 : soma_comp(type, B.ncomp);
     cuda_check(cudaMemcpyToSymbol(d_stim_comp, &sc, sizeof(int), type * sizeof(int)), "stimulus site");
+    B.stim_comp = sc;
   }
   // device mirror for the stimulus kernels
   cuda_check(cudaMalloc(&B.d_elem, n_elem * sizeof(double *)), "device table");
@@ -428,4 +431,41 @@ void launch_stim(int type, neuron_t *d, double t) {
   }
   cuda_check(cudaGetLastError(), "stimulus launch");
 }
+
+constexpr Protocol protocol(int type) {
+  return type == GBRKC_GR ? PR_GR : type == GBRKC_GO ? PR_GO : type == GBRKC_PKJ ? PR_PKJ : PR_IO;
+}
 }  // namespace
+
+extern "C" long gbrkc_compat_advance_batch(int type, int n, double *rows, long row_cap, double *spk_t, int *spk_cell,
+                                           long spk_cap) {
+  if (type < 0 || type >= NTYPES || n <= 0 || !rows || spk_cap < 0) return GBRKC_EINVAL;
+  Block &B = g_block[type];
+  if (B.n == 0) return 0;
+  const int cols = (type == GBRKC_IO) ? 3 : 1;
+  if (row_cap < (long)n * B.n * cols) return GBRKC_EINVAL;
+  if (n > B.batch_cap) {
+    // the protocol as the engine's stimulus table, evaluated at every interval
+    // start on the device exactly as X_set_current does before each advance
+    const Protocol pr = protocol(type);
+    std::vector<int> comp(B.n, B.stim_comp);
+    std::vector<double> amp(B.n, pr.amp), t0(B.n, pr.t0), t1(B.n, pr.t1);
+    check(gbrkc_set_stim(B.eng, B.sid, comp.data(), amp.data(), t0.data(), t1.data()), "stimulus table");
+    if (cols > 1 && B.batch_cap == 0) check(gbrkc_record_width(B.eng, type, cols), "recorder");
+    check(gbrkc_record_soma(B.eng, n), "recorder");
+    check(gbrkc_record_spikes(B.eng, (long)B.n * (n / 2 + 1)), "raster");
+    B.batch_cap = n;
+  }
+  check(gbrkc_rewind_soma(B.eng), "recorder");
+  const int rc = gbrkc_advance(B.eng, B.t, n);
+  if (rc == GBRKC_ESOLVER) return rc;
+  check(rc, TYPE_NAME[type]);
+  B.t += n * H_MAX;
+  check(gbrkc_read_soma(B.eng, B.sid, n, rows), "recorder");
+  std::vector<int> sys(spk_cap > 0 ? spk_cap : 1);
+  long m = 0;
+  const int src = gbrkc_read_spikes(B.eng, type, spk_cap, spk_t, sys.data(), spk_cell, &m);
+  if (src == GBRKC_EOVERFLOW) return src;
+  check(src, "raster");
+  return m;
+}

@@ -394,6 +394,8 @@ struct PoolHost {
   Ctl *d_ctl = nullptr;
   double *d_soma = nullptr;
   int soma_cap = 0;
+  int rec_w = 1;                         // compartments recorded per cell
+  int *d_cell_soma = nullptr;
   double *d_spk_prev = nullptr;
   SpikeRec *d_spk_log = nullptr;         // owned here (re-sized by gbrkc_record_spikes)
   int *d_spk_count = nullptr;
@@ -863,6 +865,8 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
     p.b4 = pow(p.b, 4.0);
   }
   V.soma_out = nullptr;
+  V.rec_w = P.rec_w;
+  P.d_cell_soma = const_cast<int *>(V.cell_soma);
   V.ncell_pool = P.ncell;
   V.ws_in_smem = P.ws_in_smem;
   V.ws_tile_doubles = P.ws_tile;
@@ -1532,7 +1536,7 @@ extern "C" int gbrkc_read_soma_type(gbrkc_engine *E, int type, int n_iv, double 
   PoolHost &P = E->pools[type];
   if (P.systems.empty()) return 0;
   if (!P.d_soma || n_iv > E->soma_iv) return fail(GBRKC_EINVAL, "no such recording");
-  CUDA_TRY(cudaMemcpyAsync(host, P.d_soma, (size_t)n_iv * P.ncell * sizeof(double), cudaMemcpyDeviceToHost,
+  CUDA_TRY(cudaMemcpyAsync(host, P.d_soma, (size_t)n_iv * P.ncell * P.rec_w * sizeof(double), cudaMemcpyDeviceToHost,
                            E->streams[type]));
   CUDA_TRY(cudaStreamSynchronize(E->streams[type]));
   return 0;
@@ -1593,10 +1597,32 @@ extern "C" int gbrkc_record_soma(gbrkc_engine *E, int n_max) {
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
     if (P.systems.empty() || n_max == 0) { P.d_soma = nullptr; continue; }
-    std::vector<double> z((size_t)n_max * P.ncell, 0.0);
+    std::vector<double> z((size_t)n_max * P.ncell * P.rec_w, 0.0);
     int rc = E->mem.upload(z, &P.d_soma);
     if (rc) return rc;
   }
+  return 0;
+}
+
+extern "C" int gbrkc_record_width(gbrkc_engine *E, int type, int width) {
+  if (!E || type < 0 || type >= NTYPES || width < 1) return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  PoolHost &P = E->pools[type];
+  if (P.systems.empty()) return 0;
+  if (E->soma_cap > 0) return fail(GBRKC_ESTATE, "set the width before gbrkc_record_soma");
+  std::vector<int> first(P.ncell);
+  for (size_t k = 0; k < P.systems.size(); k++) {
+    const HostSystem &S = E->systems[P.systems[k]];
+    if (width > S.ncomp) return fail(GBRKC_EINVAL, "width %d exceeds a cell's %d compartments", width, S.ncomp);
+    for (int c = 0; c < S.n; c++) {
+      const long base = P.sys_off[k] + (long)c * S.ncomp;
+      first[P.sys_cell0[k] + c] = (int)(width == 1 ? base + soma_comp(type, S.ncomp) : base);
+    }
+  }
+  CUDA_TRY(cudaMemcpy(P.d_cell_soma, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice));
+  P.cell_soma = first;
+  P.rec_w = width;
+  P.vd.rec_w = P.vf.rec_w = width;
   return 0;
 }
 
@@ -1606,11 +1632,12 @@ extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) 
   int rc = system_loc(E, id, &P, &S);
   if (rc) return rc;
   if (!P->d_soma || n_iv > E->soma_iv || !host) return fail(GBRKC_EINVAL, "no such recording");
-  const int c0 = P->sys_cell0[S->pool_index];
-  std::vector<double> all((size_t)n_iv * P->ncell);
+  const int c0 = P->sys_cell0[S->pool_index], w = P->rec_w;
+  std::vector<double> all((size_t)n_iv * P->ncell * w);
   CUDA_TRY(cudaMemcpy(all.data(), P->d_soma, all.size() * sizeof(double), cudaMemcpyDeviceToHost));
   for (int k = 0; k < n_iv; k++)
-    for (int c = 0; c < S->n; c++) host[(size_t)k * S->n + c] = all[(size_t)k * P->ncell + c0 + c];
+    for (int c = 0; c < S->n * w; c++)
+      host[(size_t)k * S->n * w + c] = all[((size_t)k * P->ncell + c0) * w + c];
   return 0;
 }
 

@@ -93,8 +93,9 @@ struct PoolView {
   int coef_mmax;
   NaPar na[9];
   // outputs
-  double *soma_out;                   // [interval][pool cell] or null
-  const int *cell_soma;               // per pool cell: compartment index in pool
+  double *soma_out;                   // [interval][pool cell][rec_w] or null
+  const int *cell_soma;               // per pool cell: first recorded compartment (pool index)
+  int rec_w;                          // compartments recorded per cell
   int ncell_pool;
   // device raster: per pool cell the spike compartment and its value at the
   // previous interval's end; an upward crossing of spk_th appends a SpikeRec

@@ -848,7 +848,8 @@ struct Sys {
     if (P.soma_out) {
       for (int cc = tm.rank(); cc < ncell; cc += tm.size()) {
         const int pc = cell0 + cc;
-        P.soma_out[(long)(iv0 + k_iv) * P.ncell_pool + pc] = P.vnew[P.cell_soma[pc]];
+        for (int k = 0; k < P.rec_w; k++)
+          P.soma_out[((long)(iv0 + k_iv) * P.ncell_pool + pc) * P.rec_w + k] = P.vnew[P.cell_soma[pc] + k];
       }
     }
     if (P.spk_prev) {

@@ -129,10 +129,21 @@ __global__ void __launch_bounds__(MEGA_BLOCK, 1) k_mega(const __grid_constant__ 
   if (threadIdx.x == 0) M.t_end[blockIdx.x] = global_ns();
 }
 
+// The dynamic shared-memory limit is a per-kernel attribute shared by every
+// engine in the process: only ever raise it, so that a later engine with
+// smaller needs cannot break an earlier one's launches.
+static cudaError_t raise_smem_limit(const void *k, size_t smem) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, k);
+  if (e != cudaSuccess) return e;
+  if ((size_t)a.maxDynamicSharedSizeBytes >= smem) return cudaSuccess;
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 template <typename R>
 int prepare_mega_kernel(size_t smem, int *blocks_per_sm) {
   const void *k = (const void *)k_mega<R>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit(k, smem);
   if (e != cudaSuccess) return (int)e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k, MEGA_BLOCK, smem);
   return (int)e;
@@ -178,7 +189,7 @@ template <typename R>
 int prepare_pool_kernel(int type, int team, size_t smem) {
   const void *k = kernel_ptr<R>(type, team);
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = raise_smem_limit(k, smem);
     if (e != cudaSuccess) return (int)e;
   }
   if (team_cluster_size(team) > 8) {

@@ -370,7 +370,9 @@ struct LaneSys {
 #pragma unroll
     for (int i = 0; i < NC; i++) P.vnew[off + i] = fma(b2, fn[i], fma(b1, v2[i], fma(a2, yn[i], a1 * v1[i])));
     c.tend += H_MAX;
-    if (P.soma_out) P.soma_out[(long)(iv0 + k_iv) * P.ncell_pool + cell0] = P.vnew[P.cell_soma[cell0]];
+    if (P.soma_out)
+      for (int k = 0; k < P.rec_w; k++)
+        P.soma_out[((long)(iv0 + k_iv) * P.ncell_pool + cell0) * P.rec_w + k] = P.vnew[P.cell_soma[cell0] + k];
     if (P.spk_prev) log_spike(P, cell0, t0 + (k_iv + 1) * H_MAX);
     if (c.iv_left > 0) c.iv_left--;
   }

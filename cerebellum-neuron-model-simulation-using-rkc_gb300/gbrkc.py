@@ -121,6 +121,7 @@ def lib() -> C.CDLL:
                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.gbrkc_read_soma_type.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.gbrkc_rewind_soma.argtypes = [P]
+        L.gbrkc_record_width.argtypes = [P, C.c_int, C.c_int]
         L.gbrkc_retired_systems.argtypes = [P]
         L.gbrkc_launch_layout.argtypes = [P, C.POINTER(C.c_int)]
         L.gbrkc_compartment_updates.argtypes = [P, C.c_int]
@@ -398,6 +399,9 @@ class Engine:
     def read_soma_type(self, cell_type: int, n_intervals: int, out: np.ndarray):
         _check(lib().gbrkc_read_soma_type(self.h, cell_type, n_intervals, _dp(out)))
         return out
+
+    def record_width(self, cell_type: int, width: int):
+        _check(lib().gbrkc_record_width(self.h, cell_type, width))
 
     def rewind_soma(self):
         _check(lib().gbrkc_rewind_soma(self.h))

@@ -120,6 +120,11 @@ int gbrkc_set_stim_type(gbrkc_engine *e, int cell_type, const int *comp, const d
 /* Soma recording of every cell of one type, [interval][cell] (one copy), and
  * restart of the recording window without reallocating. */
 int gbrkc_read_soma_type(gbrkc_engine *e, int cell_type, int n_intervals, double *host);
+/* Record `width` compartments per cell of a type instead of the soma: the
+ * cell's compartments 0 .. width-1 (the IO output_file writes all three).
+ * Call before gbrkc_record_soma; the soma reads then return
+ * [interval][cell][width]. */
+int gbrkc_record_width(gbrkc_engine *e, int cell_type, int width);
 int gbrkc_rewind_soma(gbrkc_engine *e);
 
 /* Device time of the last gbrkc_advance (CUDA events on the launching

@@ -172,6 +172,21 @@ void pkj_synapse_update(const double t, const double DT, synapse_t *grpkj, synap
 gap_t *io_gap_create(const int nx, const int ny);
 void io_gap_finalize(gap_t *g);
 
+/* Batched output -- this library's addition, no counterpart in the
+ * reference.  Advance the type's block by n intervals in one device launch:
+ * its stimulus protocol (the X_set_current rule above) is applied on the
+ * device at each interval start, the output_file columns (the soma; IO: its
+ * three compartments per cell) are recorded on the device for every
+ * interval into rows (n x cells x columns doubles, interval-major), and the
+ * raster crossings are found on the device (output_file's rule) and written
+ * as (interval end time, cell) pairs sorted by time then cell.  The values
+ * are the ones the per-interval path gives, bit for bit.  Returns the number
+ * of crossings (at most spk_cap), GBRKC_ESOLVER (-5) when the block stopped
+ * (a non-finite voltage), GBRKC_EOVERFLOW (-6) when spk_cap was too small,
+ * GBRKC_EINVAL (-1) on bad arguments. */
+long gbrkc_compat_advance_batch(int type, int n, double *rows, long row_cap, double *spk_t, int *spk_cell,
+                                long spk_cap);
+
 /* comptime.csv row (output.cu:3-36). */
 void output_time(const int n_gr, const char *type1, const int n_go, const char *type2, const int n_pkj,
                  const char *type3, const int n_io, const char *type4, const double comp_time, const int sim_time);

@@ -82,3 +82,32 @@ def test_go_pkj_blocks_match_oracle(tmp_path, oracle):
             ref = s.vnew()[soma::ncomp]
             assert v[k, 0] == pytest.approx(t, abs=1e-9)
             np.testing.assert_allclose(v[k, 1:], ref, atol=1.5e-6, rtol=0, err_msg=f"{name} interval {k}")
+
+
+def test_batched_cli_writes_identical_files(tmp_path):
+    """gbrkc_main with batch > 1 (several intervals per launch, voltage
+    record and raster on the device, CSV from a writer thread) writes the
+    same bytes as the per-interval path, for every type."""
+    files = {"Gr.txt": M.write_rows(M.gr_synthetic(11), M.GR), "Go_131.txt": M.write_rows(M.go_synthetic(3), M.GO),
+             "Pkj.txt": M.write_rows(M.pkj_synthetic(4), M.PKJ),
+             "Pkj_GJ.csv": "\n".join(f"{a},{b}" for a, b in M.PKJ_GJ_PAIRS) + "\n",
+             "IO.txt": M.write_rows(M.io_rows(), M.IO)}
+    dims = [(2, 1), (1, 1), (1, 1), (4, 4)]
+    out = {}
+    for batch in (1, 70):
+        d = tmp_path / f"b{batch}"
+        d.mkdir()
+        for name, text in files.items():
+            (d / name).write_text(text)
+        args = [CLI]
+        for nx, ny in dims:
+            args += ["RKC", str(nx), str(ny)]
+        args += ["60", str(batch)]
+        r = subprocess.run(args, cwd=d, env=dict(os.environ, GBRKC_MODEL_DIR=str(d)), capture_output=True,
+                           text=True, timeout=600)
+        assert r.returncode == 0, r.stdout + r.stderr
+        out[batch] = {f: (d / f).read_bytes() for f in sorted(os.listdir(d)) if f.endswith("_by_RKC.csv")}
+    assert sorted(out[1]) == sorted(out[70]) and len(out[1]) == 8
+    for f in out[1]:
+        assert out[1][f] == out[70][f], f
+    assert out[1]["gr_v_by_RKC.csv"].count(b"\n") == 480
