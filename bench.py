@@ -114,6 +114,66 @@ def workload(name, scale=1.0):
     raise SystemExit(f"unknown config {name}")
 
 
+# ------------------------------------------------------------ network
+def run_network(args, G, configs, torch, precision, rank, world, dist):
+    """configs[2]'s shape: 2048 GrC, 512 GoC, 512 PC as independent systems
+    coupled by 780 404 chemical synapses with delays (configs.network_batch).
+    Network mode advances every system one interval per launch, then updates
+    every synapse; a step is --step-ms of simulated time, timed on the host
+    wall clock around the synchronous advance (launches included)."""
+    specs, groups = configs.network_batch()
+    eng = G.Engine(G.MIXED if precision == "mixed" else G.FP64)
+    configs.add_network(eng, specs, groups)
+    t0 = time.perf_counter()
+    eng.build()
+    setup_s = time.perf_counter() - t0
+    n_iv = int(round(args.step_ms / H_MAX))
+    t = 0.0
+    for _ in range(args.warmup):
+        eng.advance(t, n_iv, tolerate_retire=True)
+        t += n_iv * H_MAX
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    u0 = eng.compartment_updates(-1)
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.advance(t, n_iv, tolerate_retire=True)
+        t += n_iv * H_MAX
+    torch.cuda.synchronize()
+    wall = barrier_max(dist, time.perf_counter() - w0)
+    clk = clocks.stop()
+    units = barrier_sum(dist, eng.compartment_updates(-1) - u0)
+    nsyn = sum(len(g["post_system"]) for g in groups)
+    n_spk = eng.read_synapses(G.SYNF_S0, nsyn)
+    peak, peak_kind = peaks()
+    bpu = ALG_BYTES[precision]
+    achieved = bpu * units / wall / 1e9
+    if rank == 0:
+        counts = configs.type_counts(specs)
+        out = {"metric": "compartment-updates/s", "value": units / wall, "unit": "compartment-updates/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64 state+stages, f32 gating" if precision == "mixed" else "f64",
+               "data": "synthetic (seeded cells, synapses, weights and delays)",
+               "config": {"workload": "network: 2048 GrC x4 + 512 GoC x131 + 512 PC x1600, 780404 synapses "
+                                      "(MF->GrC Poisson 5-50 Hz, GrC->GoC, GoC->GrC, GrC->PC), lognormal weights, "
+                                      "delays U[1,5] ms", "precision": precision, "step_sim_ms": args.step_ms,
+                          "cells": {k: v[0] for k, v in counts.items()}, "synapses": nsyn,
+                          "synapses_with_activity": int(np.count_nonzero(n_spk)),
+                          "retired_systems": eng.retired(), "setup_s": round(setup_s, 2),
+                          "timing": "host wall clock; one persistent launch and one synapse launch per interval",
+                          "sim_ms_per_wall_s": args.steps * args.step_ms / wall},
+               "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": None, "kernel": "k_mega + k_syn_update",
+                            "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_update": bpu},
+               "gpu_launches": 2 * args.steps * n_iv, "clocks": clk}
+        print(json.dumps(out))
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 # ------------------------------------------------------------ FP64 comparison
 def fp64_compare(G, configs, specs, n_iv, warmup, k, step_ms, step_units, flush, torch):
     """Plain FP64 on the same systems and time window as the first k timed
@@ -419,7 +479,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbrkc", choices=["gbrkc", "reference"])
-    ap.add_argument("--config", default="mixed", choices=["mixed", "pkj3x3", "serve"])
+    ap.add_argument("--config", default="mixed", choices=["mixed", "pkj3x3", "serve", "network"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
     ap.add_argument("--step-ms", type=float, default=5.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -442,6 +502,9 @@ def main():
     import torch
     import gbrkc as G
     import configs
+    if args.config == "network":
+        run_network(args, G, configs, torch, precision, rank, world, dist)
+        return
     if args.config == "serve":
         # the serving stream on its own: value = compartment-updates/s over the stream's wall time
         sv = run_serve(G, precision, args.serve_requests or 128)

@@ -177,6 +177,87 @@ def serve_workload(n_requests=64, seed=5, rate_hz=200.0, ts_ms=(5.0, 25.0), io_f
     return classes, reqs
 
 
+# mossy fibre -> granule, granule -> Golgi, Golgi -> granule, granule -> Purkinje
+SYN_MFGR, SYN_GRGO, SYN_GOGR, SYN_GRPKJ = 0, 1, 2, 3
+
+
+# Shapes that stay finite in the network workload (screened on the GPU in
+# both precisions over 12 ms): Golgi variant 3 and Purkinje tree 9 diverge
+# under its synaptic drive in the reference scheme itself.
+NET_GO_VARIANTS = (0, 1, 5, 6, 7)
+NET_PKJ_SEEDS = (7, 8, 12, 13)
+
+
+def network_batch(seed=3, n_gr=2048, n_go=512, n_pkj=512, n_syn=780404, mf_groups=8, sigma=0.25,
+                  scale=(1.0, 1.0, 1.0, 1.0)):
+    """Network workload: n_gr reduced granule cells, n_go Golgi cells (the
+    screened tree variants), n_pkj Purkinje cells (screened trees), each its
+    own system (shapes NET_GO_VARIANTS, NET_PKJ_SEEDS), coupled by n_syn
+    chemical synapses with the reference's
+    kinetics: 4 mossy fibres per granule cell (Poisson, groups at 5-50 Hz),
+    100 granule cells onto each Golgi soma, 4 Golgi cells onto each granule
+    soma, and the rest granule -> Purkinje onto random dendritic
+    compartments.  Weights are lognormal (sigma 0.25; at 0.5 the mossy-fibre
+    tail drives some granule cells to divergence) around the reference's,
+    scaled by the postsynaptic cell's input count as syn.cu:57, 175, 328, 511
+    do (W_MFGR / 4, W_GRGO / (n / 4), W_GOGR / (4 n), W_GRPKJ / (512 n / 10)
+    with the constants of syn.cuh:54-58); every synapse has a transmission
+    delay of U[1, 5] ms
+    (8-40 intervals).  No injected current.  Returns (specs, groups); each
+    group is the keyword arguments of Engine.add_synapses with system
+    indices into specs."""
+    rng = np.random.default_rng(seed)
+    gr_rows = M.gr_reduced4()
+    go_rows = [M.go_synthetic(2000 + k) for k in NET_GO_VARIANTS]
+    pk_rows = [M.pkj_synthetic(k) for k in NET_PKJ_SEEDS]
+    specs = [Spec(M.GR, 1, 1, gr_rows, _jitter(rng, 1), tag="gr") for _ in range(n_gr)]
+    specs += [Spec(M.GO, 1, 1, go_rows[i % len(go_rows)], _jitter(rng, 1), tag="go") for i in range(n_go)]
+    specs += [Spec(M.PKJ, 1, 1, pk_rows[i % len(pk_rows)], _jitter(rng, 1), tag="pkj") for i in range(n_pkj)]
+    gr = np.arange(n_gr)
+    go = n_gr + np.arange(n_go)
+    pk = n_gr + n_go + np.arange(n_pkj)
+
+    def lognormal(median, n):
+        return median * np.exp(sigma * rng.standard_normal(n))
+
+    def delay(n):
+        return rng.integers(8, 41, n)
+
+    groups = []
+    per = n_gr // mf_groups
+    for g in range(mf_groups):
+        cells = gr[g * per:(g + 1) * per] if g < mf_groups - 1 else gr[g * per:]
+        n = 4 * len(cells)
+        groups.append(dict(kind=SYN_MFGR, post_system=np.repeat(cells, 4), post_comp=np.tile(np.arange(4), len(cells)),
+                           weight=scale[0] * lognormal(10000.0, n), rates=(5.0 + 45.0 * g / max(1, mf_groups - 1), 0.0, 0.0, 0.0),
+                           seed=1000 + g, delay=delay(n)))
+    n = 100 * n_go
+    groups.append(dict(kind=SYN_GRGO, post_system=np.repeat(go, 100), post_comp=0, weight=scale[1] * lognormal(16.0 / (100 / 4.0), n),
+                       pre_system=rng.choice(gr, n), pre_comp=3, delay=delay(n)))
+    n = 4 * n_gr
+    groups.append(dict(kind=SYN_GOGR, post_system=np.repeat(gr, 4), post_comp=1,
+                       weight=scale[2] * lognormal(640000.0 / (4 * 4.0), n),
+                       pre_system=rng.choice(go, n), pre_comp=30, delay=delay(n)))
+    n = n_syn - sum(len(g["post_system"]) for g in groups)
+    post = rng.choice(pk, n)
+    n_in = np.bincount(post - pk[0], minlength=n_pkj)[post - pk[0]]
+    groups.append(dict(kind=SYN_GRPKJ, post_system=post, post_comp=rng.integers(0, 1599, n),
+                       weight=scale[3] * 300000.0 / (512 * n_in / 10.0) * np.exp(sigma * rng.standard_normal(n)),
+                       pre_system=rng.choice(gr, n), pre_comp=3, delay=delay(n)))
+    return specs, groups
+
+
+def add_network(engine, specs, groups):
+    ids = np.asarray(add_to(engine, specs))
+    for g in groups:
+        kw = dict(g)
+        kw["post_system"] = ids[np.asarray(kw["post_system"])]
+        if "pre_system" in kw:
+            kw["pre_system"] = ids[np.asarray(kw["pre_system"])]
+        engine.add_synapses(kw.pop("kind"), kw.pop("post_system"), kw.pop("post_comp"), kw.pop("weight"), **kw)
+    return ids
+
+
 def add_to(engine, specs):
     ids = []
     for s in specs:

@@ -441,6 +441,7 @@ struct gbrkc_engine {
   // chemical synapses (network mode), as added
   struct {
     std::vector<int> kind, grp, pre_sys, pre_comp, post_sys, post_comp;
+    std::vector<unsigned char> delay;
     std::vector<double> w, grp_rate;
     std::vector<unsigned long long> grp_seed;
   } syn;
@@ -1184,6 +1185,17 @@ int build_synapses(gbrkc_engine *E) {
     unsigned long long *u;
     if ((rc = M.upload(E->syn.grp_seed, &u))) return rc;
     V.grp_seed = u;
+    V.ring = nullptr;
+    V.delay = nullptr;
+    bool any_delay = false;
+    for (unsigned char x : E->syn.delay) any_delay |= (x != 0);
+    if (any_delay) {
+      std::vector<unsigned long long> ring(n, 0ull);
+      if ((rc = M.upload(ring, &V.ring))) return rc;
+      unsigned char *dl;
+      if ((rc = M.upload(E->syn.delay, &dl))) return rc;
+      V.delay = dl;
+    }
   }
   for (int k = 0; k < 8; k++) V.decay[k] = exp(-0.125 / TAU[k]);
   for (int t = 0; t < NTYPES; t++) V.pre_v[t] = E->pools[t].d_v;
@@ -1235,6 +1247,8 @@ extern "C" int gbrkc_add_synapses(gbrkc_engine *E, const gbrkc_synapse_desc *d, 
   static const int PRE[SYN_KINDS] = {-1, GR, GO, GR}, POST[SYN_KINDS] = {GR, GO, GR, PKJ};
   const int nsys = (int)E->systems.size();
   for (int i = 0; i < d->n; i++) {
+    if (d->delay && (d->delay[i] < 0 || d->delay[i] > 63))
+      return fail(GBRKC_EINVAL, "synapse %d: delay %d outside 0..63 intervals", i, d->delay[i]);
     const int q = d->post_system[i];
     if (q < 0 || q >= nsys || E->systems[q].type != POST[d->kind] || d->post_comp[i] < 0 ||
         d->post_comp[i] >= E->systems[q].nc)
@@ -1256,6 +1270,7 @@ extern "C" int gbrkc_add_synapses(gbrkc_engine *E, const gbrkc_synapse_desc *d, 
     E->syn.post_sys.push_back(d->post_system[i]);
     E->syn.post_comp.push_back(d->post_comp[i]);
     E->syn.w.push_back(d->weight[i]);
+    E->syn.delay.push_back(d->delay ? (unsigned char)d->delay[i] : 0);
   }
   // mossy-fibre rates: 5 Hz, 60 Hz for S_Stimuli <= t < E_Stimuli (syn.cu:93-95,
   // param.h:8-9) unless the group gives its own

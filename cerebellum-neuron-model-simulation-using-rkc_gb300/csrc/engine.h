@@ -140,6 +140,8 @@ struct SynView {
   const double *w;
   double *s0, *s1, *s2, *val, *old_v;
   const double *pre_v[NTYPES];        // elem v of every pool
+  unsigned long long *ring;           // per synapse: the last 64 intervals' events, newest in bit 0 (or null)
+  const unsigned char *delay;         // per synapse: intervals between an event and its effect
   const double *grp_rate;             // per group: base rate, stimulus rate [Hz], window t0, t1 [ms]
   const unsigned long long *grp_seed;
   double decay[8];                    // exp(-RKC_DT / tau) per state, in SynKind order

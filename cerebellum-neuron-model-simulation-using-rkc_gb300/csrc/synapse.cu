@@ -11,6 +11,11 @@
 // finaliser of Steele, Lea & Flood 2014 over seed, synapse and interval), so
 // the draws are reproducible and identical in the oracle.
 //
+// A transmission delay of d intervals (this library's addition; 0 is the
+// reference's rule) keeps each synapse's last 64 events in a bit ring: the
+// event detected now enters bit 0, and the one detected d intervals ago
+// drives the update.
+//
 // Built with -fmad=false like the other kernel units: the arithmetic is the
 // reference's expressions in their order, bit-identical to the oracle.
 #include <cuda_runtime.h>
@@ -36,6 +41,13 @@ __host__ __device__ __forceinline__ double syn_uniform(unsigned long long seed, 
   return (double)((z >> 11) + 1ull) * 0x1p-53;  // (0, 1], like curand_uniform
 }
 
+__device__ __forceinline__ int delayed(const SynView &S, int id, int f_now) {
+  if (!S.ring) return f_now;
+  const unsigned long long r = (S.ring[id] << 1) | (unsigned long long)f_now;
+  S.ring[id] = r;
+  return (int)((r >> S.delay[id]) & 1ull);
+}
+
 __global__ void k_syn_update(const __grid_constant__ SynView S, double t, long long interval) {
   const int id = blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= S.n) return;
@@ -45,7 +57,7 @@ __global__ void k_syn_update(const __grid_constant__ SynView S, double t, long l
     const double *r = S.grp_rate + 4 * g;
     const double fr = (r[2] <= t && t < r[3]) ? r[1] : r[0];
     const double u = syn_uniform(S.grp_seed[g], id, interval);
-    const int f = (fr * RKC_DT_MS * 0.001 > u) ? 1 : 0;
+    const int f = delayed(S, id, (fr * RKC_DT_MS * 0.001 > u) ? 1 : 0);
     const double ampa = S.s0[id] * S.decay[0] + f;
     // the NMDA state steps from the already-updated AMPA value (syn.cu:104)
     const double nmda = ampa * S.decay[1] + f;
@@ -55,7 +67,7 @@ __global__ void k_syn_update(const __grid_constant__ SynView S, double t, long l
     return;
   }
   const double pv = S.pre_v[S.pre_type[id]][S.pre_gi[id]];
-  const int f = (pv > 0.0 && S.old_v[id] < 0.0) ? 1 : 0;
+  const int f = delayed(S, id, (pv > 0.0 && S.old_v[id] < 0.0) ? 1 : 0);
   if (kind == SYN_GRGO) {
     const double a = S.s0[id] * S.decay[2] + f;
     const double n1 = S.s1[id] * S.decay[3] + f;

@@ -76,7 +76,7 @@ class SynapseDesc(C.Structure):
         ("post_system", C.POINTER(C.c_int)), ("post_comp", C.POINTER(C.c_int)),
         ("weight", C.POINTER(C.c_double)),
         ("rate_base", C.c_double), ("rate_stim", C.c_double), ("stim_t0", C.c_double), ("stim_t1", C.c_double),
-        ("seed", C.c_ulonglong),
+        ("seed", C.c_ulonglong), ("delay", C.POINTER(C.c_int)),
     ]
 
 
@@ -285,10 +285,10 @@ class Engine:
         return t[:n.value].copy(), sy[:n.value].copy(), ce[:n.value].copy()
 
     def add_synapses(self, kind, post_system, post_comp, weight, pre_system=None, pre_comp=None,
-                     rates=(0.0, 0.0, 0.0, 0.0), seed=0) -> int:
+                     rates=(0.0, 0.0, 0.0, 0.0), seed=0, delay=None) -> int:
         """Add one group of chemical synapses (GBRKC_SYN_*); returns the id of
         its first synapse.  rates = (base Hz, stimulus Hz, t0 ms, t1 ms) for
-        mossy fibres (all 0: the reference's schedule)."""
+        mossy fibres (all 0: the reference's schedule); delay in intervals."""
         post_system = np.ascontiguousarray(post_system, dtype=np.int32)
         n = post_system.size
         post_comp = np.ascontiguousarray(np.broadcast_to(post_comp, n), dtype=np.int32)
@@ -304,6 +304,10 @@ class Engine:
             keep += [pre_system, pre_comp]
         d.rate_base, d.rate_stim, d.stim_t0, d.stim_t1 = rates
         d.seed = seed
+        if delay is not None:
+            dl = np.ascontiguousarray(np.broadcast_to(delay, n), dtype=np.int32)
+            d.delay = _ip(dl)
+            keep.append(dl)
         first = C.c_int()
         _check(lib().gbrkc_add_synapses(self.h, C.byref(d), C.byref(first)))
         self._keep.append(keep)

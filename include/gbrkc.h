@@ -171,6 +171,10 @@ typedef struct gbrkc_synapse_desc {
   double stim_t0, stim_t1;        /*   stim_t0 <= t < stim_t1 [ms], else rate_base; all 0 = */
                                   /*   the reference's 5 / 60 Hz over 900-1000 ms */
   unsigned long long seed;        /* GBRKC_SYN_MFGR Poisson stream */
+  const int *delay;               /* per synapse: transmission delay in 0.125 ms intervals,
+                                     0..63, or NULL (0: the reference's same-interval rule).
+                                     No counterpart in the reference (its synapses act in the
+                                     interval of the presynaptic crossing or fibre draw) */
 } gbrkc_synapse_desc;
 
 /* Add a group of synapses between systems already added (before

@@ -71,6 +71,7 @@ def lib() -> C.CDLL:
         L.orc_net_add_system.argtypes = [P, P]
         L.orc_net_add_synapses.argtypes = [P, C.c_int, C.c_int] + [C.POINTER(C.c_int)] * 4 + [
             C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double, C.c_double, C.c_ulonglong]
+        L.orc_net_set_delays.argtypes = [P, C.c_int, C.c_int, C.POINTER(C.c_int)]
         L.orc_net_build.argtypes = [P]
         L.orc_net_advance.argtypes = [P, C.c_double]
         L.orc_net_nsyn.argtypes = [P]
@@ -279,7 +280,7 @@ class Network:
         return lib().orc_net_add_system(self.h, s.h)
 
     def add_synapses(self, kind, post_system, post_comp, weight, pre_system=None, pre_comp=None,
-                     rates=(0.0, 0.0, 0.0, 0.0), seed=0) -> int:
+                     rates=(0.0, 0.0, 0.0, 0.0), seed=0, delay=None) -> int:
         post_system = np.ascontiguousarray(post_system, dtype=np.int32)
         n = post_system.size
         post_comp = np.ascontiguousarray(np.broadcast_to(post_comp, n), dtype=np.int32)
@@ -287,8 +288,13 @@ class Network:
         pre_system = np.ascontiguousarray(np.broadcast_to(-1 if pre_system is None else pre_system, n), dtype=np.int32)
         pre_comp = np.ascontiguousarray(np.broadcast_to(0 if pre_comp is None else pre_comp, n), dtype=np.int32)
         self._keep.append((post_system, post_comp, weight, pre_system, pre_comp))
-        return lib().orc_net_add_synapses(self.h, kind, n, _ip(pre_system), _ip(pre_comp), _ip(post_system),
-                                          _ip(post_comp), _dp(weight), *rates, seed)
+        first = lib().orc_net_add_synapses(self.h, kind, n, _ip(pre_system), _ip(pre_comp), _ip(post_system),
+                                           _ip(post_comp), _dp(weight), *rates, seed)
+        if delay is not None:
+            d = np.ascontiguousarray(np.broadcast_to(delay, n), dtype=np.int32)
+            if lib().orc_net_set_delays(self.h, first, n, _ip(d)) != 0:
+                raise ValueError("delays must be 0..63 intervals")
+        return first
 
     def build(self):
         if lib().orc_net_build(self.h) != 0:

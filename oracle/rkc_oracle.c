@@ -1653,6 +1653,8 @@ struct orc_net {
   int n, cap;
   int *kind, *grp, *pre_sys, *pre_comp, *post_sys, *post_comp;
   double *w, *s0, *s1, *s2, *val, *old_v, *e;
+  unsigned long long *ring; /* last 64 events per synapse, newest in bit 0 */
+  int *delay;               /* intervals between an event and its effect */
   int ngrp;
   double rate[64][4];
   unsigned long long seed[64];
@@ -1694,6 +1696,7 @@ int orc_net_add_synapses(orc_net *n, int kind, int count, const int *pre_sys, co
     NET_GROW(post_sys, int); NET_GROW(post_comp, int);
     NET_GROW(w, double); NET_GROW(s0, double); NET_GROW(s1, double); NET_GROW(s2, double);
     NET_GROW(val, double); NET_GROW(old_v, double); NET_GROW(e, double);
+    NET_GROW(ring, unsigned long long); NET_GROW(delay, int);
   }
   int first = n->n;
   for (int i = 0; i < count; i++) {
@@ -1708,6 +1711,8 @@ int orc_net_add_synapses(orc_net *n, int kind, int count, const int *pre_sys, co
     n->s0[k] = n->s1[k] = n->s2[k] = n->val[k] = 0.0;
     n->old_v[k] = 1000.0; /* syn.cu:176, 330, 510 */
     n->e[k] = ekind[kind];
+    n->ring[k] = 0ull;
+    n->delay[k] = 0;
   }
   return first;
 }
@@ -1753,6 +1758,24 @@ static double syn_uniform(unsigned long long seed, long long id, long long inter
   return (double)((z >> 11) + 1ull) * 0x1p-53;
 }
 
+/* transmission delay (an addition to the reference, whose synapses act in
+ * the interval of the event): the event detected now enters bit 0 of the
+ * synapse's ring, and the one detected delay intervals ago drives it */
+static int net_delayed(orc_net *n, int k, int f_now) {
+  unsigned long long r = (n->ring[k] << 1) | (unsigned long long)f_now;
+  n->ring[k] = r;
+  return (int)((r >> n->delay[k]) & 1ull);
+}
+
+int orc_net_set_delays(orc_net *n, int first, int count, const int *delay) {
+  if (first < 0 || count < 0 || first + count > n->n) return -1;
+  for (int i = 0; i < count; i++) {
+    if (delay[i] < 0 || delay[i] > 63) return -1;
+    n->delay[first + i] = delay[i];
+  }
+  return 0;
+}
+
 /* mfgr_update, grgo_update, gogr_update, grpkj_update (syn.cu:86-111,
  * 263-288, 412-437, 646-668); conductances syn.cuh:11-45 */
 static void net_syn_update(orc_net *n, double t) {
@@ -1762,7 +1785,7 @@ static void net_syn_update(orc_net *n, double t) {
       const double *r = n->rate[n->grp[k]];
       double fr = (r[2] <= t && t < r[3]) ? r[1] : r[0];
       double u = syn_uniform(n->seed[n->grp[k]], k, n->interval);
-      int f = (fr * 0.125 * 0.001 > u) ? 1 : 0;
+      int f = net_delayed(n, k, (fr * 0.125 * 0.001 > u) ? 1 : 0);
       double ampa = n->s0[k] * n->decay[0] + f;
       double nmda = ampa * n->decay[1] + f; /* from the updated AMPA, syn.cu:104 */
       n->s0[k] = ampa;
@@ -1771,7 +1794,7 @@ static void net_syn_update(orc_net *n, double t) {
       continue;
     }
     double pv = n->sys[n->pre_sys[k]]->v[n->pre_comp[k]];
-    int f = (pv > 0.0 && n->old_v[k] < 0.0) ? 1 : 0;
+    int f = net_delayed(n, k, (pv > 0.0 && n->old_v[k] < 0.0) ? 1 : 0);
     if (kind == SYN_GRGO) {
       double a = n->s0[k] * n->decay[2] + f;
       double n1 = n->s1[k] * n->decay[3] + f;
@@ -1818,5 +1841,6 @@ void orc_net_destroy(orc_net *n) {
   if (!n) return;
   free(n->kind); free(n->grp); free(n->pre_sys); free(n->pre_comp); free(n->post_sys); free(n->post_comp);
   free(n->w); free(n->s0); free(n->s1); free(n->s2); free(n->val); free(n->old_v); free(n->e);
+  free(n->ring); free(n->delay);
   free(n);
 }

@@ -86,6 +86,9 @@ void orc_stats(const orc_sys *s, long long *out6);
 typedef struct orc_net orc_net;
 orc_net *orc_net_create(void);
 int orc_net_add_system(orc_net *n, orc_sys *s);
+/* per-synapse transmission delays (0..63 intervals) of synapses first ..
+ * first+count-1; 0 (the default) is the reference's rule */
+int orc_net_set_delays(orc_net *n, int first, int count, const int *delay);
 int orc_net_add_synapses(orc_net *n, int kind, int count, const int *pre_sys, const int *pre_comp,
                          const int *post_sys, const int *post_comp, const double *w, double rate_base,
                          double rate_stim, double t0, double t1, unsigned long long seed);

@@ -48,13 +48,15 @@ def add_to_engine(G, O, eng, name, seed=0):
 NET_NGR, NET_NGO, NET_NPK_SYN = 8, 2, 5
 
 
-def build_network(O, target, seed=5, mf_rate=400.0):
+def build_network(O, target, seed=5, mf_rate=400.0, delays=False):
     """A small network in the reference's topology: 8 reduced granule cells,
     2 Golgi cells and 1 Purkinje cell, each its own system; mossy fibres onto
     every granule compartment, granule axon -> Golgi soma, Golgi comp 30 ->
     granule soma, granule axon -> 5 random Purkinje compartments per cell,
     with weights scaled like the reference's (W_* / counts, syn.cuh:46-50).
-    `target` is an oracle Network or a gbrkc Engine; returns the system ids."""
+    `target` is an oracle Network or a gbrkc Engine; returns the system ids.
+    delays: seeded transmission delays of 1-40 intervals (0.125-5 ms) per
+    synapse instead of the reference's same-interval rule."""
     import numpy as np
     rng = np.random.default_rng(seed)
     O.libc_srand(0)
@@ -70,12 +72,18 @@ def build_network(O, target, seed=5, mf_rate=400.0):
         else:
             ids.append(target.add_system(t, 1, 1, rows, jit))
     gr, go, pk = ids[:NET_NGR], ids[NET_NGR:NET_NGR + NET_NGO], ids[-1]
+    drng = np.random.default_rng(seed + 100)
+
+    def dl(n):
+        return drng.integers(1, 41, n) if delays else None
+
     target.add_synapses(0, np.repeat(gr, 4), np.tile(np.arange(4), NET_NGR), 10000.0,
-                        rates=(mf_rate, 0.0, 0.0, 0.0), seed=7)
+                        rates=(mf_rate, 0.0, 0.0, 0.0), seed=7, delay=dl(4 * NET_NGR))
     target.add_synapses(1, np.tile(go, NET_NGR), 0, 16.0 / (NET_NGR / 4.0), pre_system=np.repeat(gr, NET_NGO),
-                        pre_comp=3)
+                        pre_comp=3, delay=dl(NET_NGR * NET_NGO))
     target.add_synapses(2, np.tile(gr, NET_NGO), 1, 640000.0 / (NET_NGO * 4.0), pre_system=np.repeat(go, NET_NGR),
-                        pre_comp=30)
+                        pre_comp=30, delay=dl(NET_NGR * NET_NGO))
     target.add_synapses(3, np.full(NET_NGR * NET_NPK_SYN, pk), rng.integers(0, 1599, NET_NGR * NET_NPK_SYN),
-                        300000.0 / (512 * NET_NGR / 10.0), pre_system=np.repeat(gr, NET_NPK_SYN), pre_comp=3)
+                        300000.0 / (512 * NET_NGR / 10.0), pre_system=np.repeat(gr, NET_NPK_SYN), pre_comp=3,
+                        delay=dl(NET_NGR * NET_NPK_SYN))
     return ids

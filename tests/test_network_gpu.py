@@ -11,14 +11,16 @@ from gpu_cases import build_network
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("delays", [False, True])
 @pytest.mark.parametrize("checkpoints", [(40, 100, 160)])
-def test_network_fp64_bit_exact(oracle, checkpoints):
+def test_network_fp64_bit_exact(oracle, checkpoints, delays):
+    """delays: every synapse acts 1-40 intervals after its event (bit rings)."""
     O = oracle
     net = O.Network()
-    ids_o = build_network(O, net)
+    ids_o = build_network(O, net, delays=delays)
     net.build()
     eng = G.Engine(G.FP64)
-    ids_g = build_network(O, eng)
+    ids_g = build_network(O, eng, delays=delays)
     eng.build()
     nsyn = len(net.syn(0))
     t, done = 0.0, 0
