@@ -450,16 +450,22 @@ def dist_init(n):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
     dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return rank, world, dist
+
+
+def _reduce_device(dist):
+    # NCCL reduces device tensors, gloo host tensors
+    return "cuda" if dist.get_backend() == "nccl" else "cpu"
 
 
 def barrier_max(dist, x):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device(dist))
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -468,7 +474,7 @@ def barrier_sum(dist, x):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device(dist))
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
