@@ -218,3 +218,35 @@ def test_served_request_matches_oracle(oracle):
     np.testing.assert_array_equal(sc, np.array(ref_c)[order])
     assert len(st) > 0, "the stimulus should make the granule cells fire"
     srv.close()
+
+
+@pytest.mark.parametrize("precision", [G.FP64, G.MIXED])
+def test_reset_then_noalloc_advance(precision):
+    """The allocation-free advance initialises refilled systems the same way."""
+    rng = np.random.default_rng(21)
+    engines = []
+    for _ in range(2):
+        eng = G.Engine(precision)
+        for name in ("gr", "go", "pkj"):
+            t, nx, ny, _, _, _, gap = SHAPES[name]
+            for k in range(2):
+                eng.add_system(t, nx, ny, rows(name), np.zeros(nx * ny), gap=gap, idle=True)
+        eng.build()
+        engines.append(eng)
+    inp = {name: inputs(name, 2, np.random.default_rng(5)) for name in ("gr", "go", "pkj")}
+    for eng in engines:
+        for j, name in enumerate(("gr", "go", "pkj")):
+            d = inp[name]
+            eng.reset_systems(2 * j, 2, d["jitter"], stim=d["stim"], cond_scale=d["cond_scale"], n_intervals=12)
+    a, b = engines
+    a.advance(0.0, 8)
+    b.advance_noalloc(0.0, 8)
+    a.advance(1.0, 8)
+    b.advance_noalloc(1.0, 8)
+    for s in range(6):
+        np.testing.assert_array_equal(a.vnew(s), b.vnew(s), err_msg=f"system {s}")
+        assert a.ctl(s)[1] == b.ctl(s)[1]
+    ref = fresh(precision, "go", 2, 12, inp["go"])
+    np.testing.assert_array_equal(np.concatenate([b.vnew(2), b.vnew(3)]), ref[G.F_VNEW])
+    for eng in engines:
+        eng.close()
