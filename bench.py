@@ -234,7 +234,7 @@ def fp64_compare(G, configs, specs, n_iv, warmup, k, step_ms, step_units, flush,
 
 
 # ------------------------------------------------------------ serving
-def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8):
+def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_scale=1):
     """Serve a Poisson request stream (configs.serve_workload) through the
     request server on the wall clock: requests are submitted when their
     arrival time has passed, every round admits what fits and advances all
@@ -243,7 +243,7 @@ def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8):
     FP64 engine (build, advance, read back), for the throughput ratio and the
     served results' voltage error and spike counts against FP64."""
     import configs
-    classes, reqs = configs.serve_workload(n_requests, seed=seed)
+    classes, reqs = configs.serve_workload(n_requests, seed=seed, slots_scale=slots_scale)
     prec = G.MIXED if precision == "mixed" else G.FP64
     srv = G.Server(prec, 0, quantum)
     cids = [srv.add_class(c.cell_type, c.nx, c.ny, c.rows, slots=c.slots, gap=c.gap) for c in classes]
@@ -256,7 +256,7 @@ def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8):
                           io_gap_g=r.io_gap_g)
 
     # warm-up: one short request per class, run to completion, not counted
-    _, warm = configs.serve_workload(len(classes) * 4, seed=seed + 100)
+    _, warm = configs.serve_workload(len(classes) * 4, seed=seed + 100, slots_scale=slots_scale)
     seen = set()
     for r in warm:
         if r.cls not in seen:
@@ -494,6 +494,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population fraction of the mixed batch (small profiling cases; 1 = the benchmark)")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--serve-slots", type=int, default=1, help="multiplier on the serving arenas' slot counts")
     ap.add_argument("--serve-requests", type=int, default=None,
                     help="requests of the serving stream (default 48 beside the mixed workload, 128 for "
                          "--config serve; 0: none)")
@@ -513,7 +514,7 @@ def main():
         return
     if args.config == "serve":
         # the serving stream on its own: value = compartment-updates/s over the stream's wall time
-        sv = run_serve(G, precision, args.serve_requests or 128)
+        sv = run_serve(G, precision, args.serve_requests or 128, slots_scale=args.serve_slots)
         if rank == 0:
             out = {"metric": "compartment-updates/s", "value": sv["value"], "unit": "compartment-updates/s",
                    "n_gpus": world, "steps": 1, "warmup": args.warmup, "ms_per_step": sv["wall_s"] * 1e3,
@@ -687,7 +688,7 @@ def main():
     n_serve = 48 if args.serve_requests is None else args.serve_requests
     if n_serve > 0 and rank == 0 and args.config == "mixed":
         eng.close()
-        serving = run_serve(G, precision, n_serve)
+        serving = run_serve(G, precision, n_serve, slots_scale=args.serve_slots)
 
     cpu = None
     if not args.no_cpu and rank == 0:

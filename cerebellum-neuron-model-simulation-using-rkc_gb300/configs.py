@@ -139,7 +139,7 @@ class Request:
     io_gap_g: Optional[np.ndarray] = None
 
 
-def serve_workload(n_requests=64, seed=5, rate_hz=200.0, ts_ms=(5.0, 25.0), io_fraction=0.2):
+def serve_workload(n_requests=64, seed=5, rate_hz=200.0, ts_ms=(5.0, 25.0), io_fraction=0.2, slots_scale=1):
     """Request stream of the serving benchmark: Poisson arrivals at rate_hz;
     each request is either an inferior-olive 4x4 gap-junction network set
     (io_fraction; 1-8 networks, edge conductances G_C x U[0.5,1.5]) or
@@ -147,15 +147,20 @@ def serve_workload(n_requests=64, seed=5, rate_hz=200.0, ts_ms=(5.0, 25.0), io_f
     U[ts_ms] rounded to whole 0.125 ms intervals; per-cell step currents
     U[0, AMP_MAX] from t = 0 and channel densities x U[0.8, 1.2].  Request
     sizes and durations are scaled down from 1-4096 cells and 50-1000 ms so
-    that the whole stream finishes in tens of seconds."""
+    that the whole stream finishes in tens of seconds.  The arenas hold about
+    half the stream's cells at once (32768 granule slots, 768 per Golgi
+    shape, 96 per Purkinje shape, 128 olive networks; 0.42 GB of HBM);
+    slots_scale multiplies them.  A quarter of that queues more and halves
+    the throughput (measured on the GB300: 3.5e9 against 6.5e9
+    compartment-updates/s, p99 12.6 s against 6.7 s)."""
     rng = np.random.default_rng(seed)
-    classes = [ServeClass("gr", M.GR, 1, 1, M.gr_reduced4(), 8192, 4096, 1)]
+    classes = [ServeClass("gr", M.GR, 1, 1, M.gr_reduced4(), 32768 * slots_scale, 4096, 1)]
     for k in GO_STABLE_VARIANTS:
-        classes.append(ServeClass(f"go{k}", M.GO, 1, 1, M.go_synthetic(2000 + k), 192, 128, 30))
+        classes.append(ServeClass(f"go{k}", M.GO, 1, 1, M.go_synthetic(2000 + k), 768 * slots_scale, 128, 30))
     for k in PKJ_STABLE_SEEDS:
         r = M.pkj_synthetic(k)
-        classes.append(ServeClass(f"pkj{k}", M.PKJ, 1, 1, r, 24, 16, r.shape[0] - 1))
-    classes.append(ServeClass("io4x4", M.IO, 4, 4, M.io_rows(), 32, 8, 0, gap=True))
+        classes.append(ServeClass(f"pkj{k}", M.PKJ, 1, 1, r, 96 * slots_scale, 16, r.shape[0] - 1))
+    classes.append(ServeClass("io4x4", M.IO, 4, 4, M.io_rows(), 128 * slots_scale, 8, 0, gap=True))
     by_type = {t: [i for i, c in enumerate(classes) if c.cell_type == t] for t in (M.GR, M.GO, M.PKJ, M.IO)}
     reqs = []
     t = 0.0

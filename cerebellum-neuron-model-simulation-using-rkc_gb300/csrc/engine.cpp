@@ -434,7 +434,9 @@ struct gbrkc_engine {
   size_t mega_smem = 0;
   int role_ctas[NTYPES] = {};
   int role_cap[NTYPES] = {};
-  int gr_warps = 0;             // granule warps in all (32 systems each)
+  int gr_warps = 0;             // granule warps of the next launch (32 lanes each)
+  int gr_warps_max = 0;         // one lane per granule system
+  long gr_active = -1;          // granule systems with work (-1: not known yet)
   double role_work[NTYPES] = {};  // smoothed CTA-ms per role
   int *d_queue = nullptr;
   unsigned long long *d_tstart = nullptr, *d_tend = nullptr;
@@ -885,6 +887,39 @@ template <typename R> PoolView<R> &pool_view(PoolHost &P);
 template <> PoolView<double> &pool_view<double>(PoolHost &P) { return P.vd; }
 template <> PoolView<float> &pool_view<float>(PoolHost &P) { return P.vf; }
 
+// Granule warps for the next persistent launch: one lane per granule system
+// with work (parked slots, finished budgets and stopped systems need none;
+// lanes take further systems from the queue, so any count is correct), and
+// the granule CTAs re-fitted to them (at most 8 lane warps a CTA, no CTA
+// without one), the other roles giving or taking the difference.
+void fit_granule_warps(gbrkc_engine *E) {
+  if (!E->mega || E->role_ctas[GR] == 0) return;
+  int want = E->gr_warps_max;
+  if (E->gr_active >= 0) want = (int)std::max(1L, std::min((long)E->gr_warps_max, (E->gr_active + 31) / 32));
+  E->gr_warps = want;
+  const int per = MEGA_BLOCK / 32;
+  int c = std::max((want + per - 1) / per, std::min(want, E->role_ctas[GR]));
+  while (c > E->role_ctas[GR]) {  // take from the other role with the most CTAs
+    int best = -1;
+    for (int t = 0; t < NTYPES; t++)
+      if (t != GR && E->role_ctas[t] > 1 && (best < 0 || E->role_ctas[t] > E->role_ctas[best])) best = t;
+    if (best < 0) break;
+    E->role_ctas[best]--;
+    E->role_ctas[GR]++;
+  }
+  while (c < E->role_ctas[GR]) {  // give to the other role with the most work per CTA
+    int best = -1;
+    double bv = -1.0;
+    for (int t = 0; t < NTYPES; t++) {
+      if (t == GR || E->role_ctas[t] == 0 || E->role_ctas[t] >= E->role_cap[t]) continue;
+      const double v = E->role_work[t] / E->role_ctas[t];
+      if (v > bv) { bv = v; best = t; }
+    }
+    E->role_ctas[GR]--;
+    if (best >= 0) E->role_ctas[best]++;
+  }
+}
+
 template <typename R>
 int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
   MegaView<R> M{};
@@ -1107,7 +1142,7 @@ int setup_mega(gbrkc_engine *E) {
   // first split: granule warps two to a CTA (or spread over every CTA when
   // granules are alone); the rest by compartment count with per-type weights;
   // refined after every launch
-  E->gr_warps = (int)((E->pools[GR].systems.size() + 31) / 32);
+  E->gr_warps = E->gr_warps_max = (int)((E->pools[GR].systems.size() + 31) / 32);
   const double w[NTYPES] = {0.0, 1.0, 0.35, 3.0};
   double ms[NTYPES];
   int others = 0;
@@ -1360,6 +1395,7 @@ extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
     P.vf.soma_out = so;
   }
   int rc = 0;
+  fit_granule_warps(E);
   if (E->pending_init) {
     // systems reset since the last call: initialise them (only them) first
     rc = launch_all(E, t0, 0, iv0, 1);
@@ -1391,6 +1427,11 @@ extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
     std::vector<Ctl> c(P.systems.size());
     CUDA_TRY(cudaMemcpy(c.data(), P.d_ctl, c.size() * sizeof(Ctl), cudaMemcpyDeviceToHost));
     if (P.retired.size() != c.size()) P.retired.assign(c.size(), 0);
+    if (t == GR) {
+      long active = 0;
+      for (const Ctl &x : c) active += (x.status == 0 && x.iv_left != 0);
+      E->gr_active = active;
+    }
     for (size_t i = 0; i < c.size(); i++)
       if (c[i].status && !P.retired[i]) {
         P.retired[i] = 1;
@@ -1797,6 +1838,7 @@ extern "C" int gbrkc_systems_reset(gbrkc_engine *E, int first_id, int n, const g
                                     : upload_run<float>(E, *P, pi0, pi0 + n);
   if (rc) return rc;
   E->pending_init = true;
+  if (P->type == GR && E->gr_active >= 0) E->gr_active += n;
   return 0;
 }
 
@@ -1979,6 +2021,7 @@ extern "C" int gbrkc_advance_noalloc(gbrkc_engine *E, double t0, int n_iv) {
   if (!E || n_iv < 0) return fail(GBRKC_EINVAL, "bad arguments");
   if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
   if (E->sv.n > 0) return fail(GBRKC_EINVAL, "engines with synapses step through gbrkc_advance");
+  fit_granule_warps(E);
   const int iv0 = E->soma_iv;
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
