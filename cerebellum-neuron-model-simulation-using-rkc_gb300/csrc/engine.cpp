@@ -435,7 +435,8 @@ struct gbrkc_engine {
   int role_ctas[NTYPES] = {};
   int role_cap[NTYPES] = {};
   int gr_warps = 0;             // granule warps of the next launch (32 lanes each)
-  int gr_warps_max = 0;         // one lane per granule system
+  int gr_warps_max = 0;         // granule warps the CTAs can hold beside the other roles
+  int lanes = 16;               // lanes of a warp that take single-lane systems
   long gr_active = -1;          // granule systems with work (-1: not known yet)
   double role_work[NTYPES] = {};  // smoothed CTA-ms per role
   int *d_queue = nullptr;
@@ -472,6 +473,14 @@ extern "C" int gbrkc_engine_create(int precision, gbrkc_engine **out) {
   if (e != cudaSuccess || ndev == 0) return fail(GBRKC_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
   std::unique_ptr<gbrkc_engine> E(new gbrkc_engine());
   E->precision = precision;
+  // lanes per warp that take single-lane systems: fewer systems in a warp
+  // diverge less but need more warps (measured on the GB300: 1024 granule
+  // cells on 32 SMs took 115 / 103 / 95 ms per simulated ms with 32 / 16 / 8
+  // lanes; the mixed workload's persistent launch 596 / 574 / 628 / 1135 ms
+  // per 5 ms with 32 / 16 / 8 / 4 in mixed precision, while in FP64 16 lanes
+  // were slower than 32); GBRKC_LANES overrides
+  E->lanes = (precision == GBRKC_MIXED) ? 16 : 32;
+  if (const char *l = getenv("GBRKC_LANES")) E->lanes = std::max(1, std::min(32, atoi(l)));
   for (auto &s : E->streams) CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreate(&E->ev_start));
   CUDA_TRY(cudaEventCreate(&E->ev_end));
@@ -868,6 +877,7 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
     p.b4 = pow(p.b, 4.0);
   }
   V.soma_out = nullptr;
+  V.lanes = E->lanes;
   V.rec_w = P.rec_w;
   P.d_cell_soma = const_cast<int *>(V.cell_soma);
   V.ncell_pool = P.ncell;
@@ -894,8 +904,14 @@ template <> PoolView<float> &pool_view<float>(PoolHost &P) { return P.vf; }
 // without one), the other roles giving or taking the difference.
 void fit_granule_warps(gbrkc_engine *E) {
   if (!E->mega || E->role_ctas[GR] == 0) return;
-  int want = E->gr_warps_max;
-  if (E->gr_active >= 0) want = (int)std::max(1L, std::min((long)E->gr_warps_max, (E->gr_active + 31) / 32));
+  PoolHost &G = E->pools[GR];
+  const long active = (E->gr_active >= 0) ? E->gr_active : (long)G.systems.size();
+  // the preferred lanes per warp, doubled while the warps would need more
+  // than half of the CTAs' warp slots (the other roles need the rest)
+  int lanes = E->lanes;
+  while (lanes < 32 && (active + lanes - 1) / lanes > E->gr_warps_max / 2) lanes = std::min(32, 2 * lanes);
+  G.vd.lanes = G.vf.lanes = lanes;
+  const int want = (int)std::max(1L, std::min((long)E->gr_warps_max, (active + lanes - 1) / lanes));
   E->gr_warps = want;
   const int per = MEGA_BLOCK / 32;
   int c = std::max((want + per - 1) / per, std::min(want, E->role_ctas[GR]));
@@ -930,6 +946,8 @@ int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
     end += E->role_ctas[t];
     M.role_end[t] = end;
   }
+  if (end > E->mega_grid || end <= 0)
+    return fail(GBRKC_ESTATE, "persistent launch: %d role CTAs for a grid of %d", end, E->mega_grid);
   M.gr_nc4 = E->pools[GR].team == TEAM_LANE4;
   // granule warps spread as evenly as whole warps allow: the first
   // lane_extra CTAs take lane_warps + 1
@@ -1042,7 +1060,7 @@ void rebalance_roles(gbrkc_engine *E, const double *role_ms, bool tune_gr) {
         nother++;
         other_ctas += E->role_ctas[t];
       }
-    const int lo = std::max(1, (E->gr_warps + MEGA_BLOCK / 32 - 1) / (MEGA_BLOCK / 32));
+    const int lo = std::max(1, std::min(E->mega_grid - nother, (E->gr_warps + MEGA_BLOCK / 32 - 1) / (MEGA_BLOCK / 32)));
     const int hi = std::max(lo, std::min(E->gr_warps, E->mega_grid - nother));
     int c = E->role_ctas[GR];
     if (tune_gr && others > 0.0 && role_ms[GR] > 0.0 && other_ctas > 0) {
@@ -1142,7 +1160,15 @@ int setup_mega(gbrkc_engine *E) {
   // first split: granule warps two to a CTA (or spread over every CTA when
   // granules are alone); the rest by compartment count with per-type weights;
   // refined after every launch
-  E->gr_warps = E->gr_warps_max = (int)((E->pools[GR].systems.size() + 31) / 32);
+  // lanes take further systems from the queue, so the warps never need to
+  // exceed what the CTAs left after one per other role can hold
+  {
+    int others_n = 0;
+    for (int t = 1; t < NTYPES; t++) others_n += !E->pools[t].systems.empty();
+    E->gr_warps_max = (E->mega_grid - others_n) * (MEGA_BLOCK / 32);
+    const long need = ((long)E->pools[GR].systems.size() + 31) / 32;
+    E->gr_warps = (int)std::min<long>(need, E->gr_warps_max);
+  }
   const double w[NTYPES] = {0.0, 1.0, 0.35, 3.0};
   double ms[NTYPES];
   int others = 0;
@@ -1971,6 +1997,8 @@ int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, int init, 
   if (end > NOALLOC_MAX_CTAS)
     return fail(GBRKC_EINVAL, "persistent launch of %d CTAs exceeds the static scratch (%d CTAs)", end,
                 NOALLOC_MAX_CTAS);
+  if (end > E->mega_grid || end <= 0)
+    return fail(GBRKC_ESTATE, "persistent launch: %d role CTAs for a grid of %d", end, E->mega_grid);
   M.gr_nc4 = E->pools[GR].team == TEAM_LANE4;
   M.lane_warps = 0;
   M.lane_extra = 0;

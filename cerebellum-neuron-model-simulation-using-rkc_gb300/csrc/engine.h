@@ -106,6 +106,7 @@ struct PoolView {
   int *spk_count;
   int spk_cap;
   double spk_th;
+  int lanes;                          // single-lane pools: lanes of each warp that take systems
   int ws_in_smem;                     // stage the workspace in shared memory
   long ws_tile_doubles;               // shared-memory workspace per team
   // chemical synapses onto this pool (network mode; syn_mode 0 = none)

@@ -973,7 +973,9 @@ __device__ __forceinline__ void run_lanes(const PoolView<R> &P, int *q, int firs
   Team tm;
   double *W = smem + threadIdx.x;
   Sys<CT, R, Team> S(P, tm);
-  int s = q ? atomicAdd(q, 1) : first;
+  // only the warp's first P.lanes lanes take systems (fewer systems per warp
+  // diverge less: a warp runs the union of its lanes' paths)
+  int s = ((int)(threadIdx.x & 31) >= P.lanes) ? P.nsys : (q ? atomicAdd(q, 1) : first);
   int r = TICK_DONE;
   // take systems until one needs stepping (or the queue is empty)
   auto acquire = [&]() {

@@ -20,13 +20,15 @@ __global__ void __launch_bounds__(256, 1) k_advance(const __grid_constant__ Pool
                                                  int iv0, int init) {
   extern __shared__ __align__(16) double smem[];
   if (TS == TEAM_THREAD || TS == TEAM_LANE4) {
-    // warp w of block b starts at system 32 (w * grid + b) + lane: the first
-    // warps of every block are filled before any block's later warps
-    const int first = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * 32 + ((int)threadIdx.x & 31);
+    // the first P.lanes lanes of warp w of block b start at system
+    // P.lanes (w * grid + b) + lane: the first warps of every block are
+    // filled before any block's later warps
+    const int first = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * P.lanes + ((int)threadIdx.x & 31);
+    const int stride = (int)gridDim.x * (MEGA_BLOCK / 32) * P.lanes;
     if (TS == TEAM_LANE4)
-      run_lanes_regs<CT, R, MEGA_BLOCK, 4>(P, nullptr, first, gridDim.x * MEGA_BLOCK, smem, t0, n_iv, iv0, init != 0);
+      run_lanes_regs<CT, R, MEGA_BLOCK, 4>(P, nullptr, first, stride, smem, t0, n_iv, iv0, init != 0);
     else
-      run_lanes<CT, R, MEGA_BLOCK>(P, nullptr, first, gridDim.x * MEGA_BLOCK, smem, t0, n_iv, iv0, init != 0);
+      run_lanes<CT, R, MEGA_BLOCK>(P, nullptr, first, stride, smem, t0, n_iv, iv0, init != 0);
   } else if (TS == TEAM_BLOCK) {
     BlockTeam tm;
     for (int s = blockIdx.x; s < P.nsys; s += gridDim.x) {

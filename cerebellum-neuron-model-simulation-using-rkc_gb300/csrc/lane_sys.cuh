@@ -422,7 +422,7 @@ __device__ __forceinline__ void run_lanes_regs(const PoolView<R> &P, int *q, int
     return;
   }
   LaneSys<CT, R, NC, BLOCK> S(P, smem + threadIdx.x);
-  int s = q ? atomicAdd(q, 1) : first;
+  int s = ((int)(threadIdx.x & 31) >= P.lanes) ? P.nsys : (q ? atomicAdd(q, 1) : first);
   int r = TICK_DONE;
   auto acquire = [&]() {
     while (s < P.nsys) {
