@@ -1,6 +1,6 @@
 """Benchmark: compartment-updates/s of the RKC hot path on one GB300.
 
-Default workload (BASELINE config "mixed-type batch"): 4096 reduced granule
+Default workload (the mixed-type batch): 4096 reduced granule
 cells, 1024 Golgi cells, 256 Purkinje cells and one 16x16 inferior-olive
 gap-junction network, FP32 gating with FP64 voltage, advanced together.
 A step advances every system by --step-ms of simulated time (default 5 ms =
@@ -116,7 +116,7 @@ def workload(name, scale=1.0):
 
 # ------------------------------------------------------------ network
 def run_network(args, G, configs, torch, precision, rank, world, dist):
-    """configs[2]'s shape: 2048 GrC, 512 GoC, 512 PC as independent systems
+    """The network workload: 2048 GrC, 512 GoC, 512 PC as independent systems
     coupled by 780 404 chemical synapses with delays (configs.network_batch).
     Network mode advances every system one interval per launch, then updates
     every synapse; a step is --step-ms of simulated time, timed on the host
