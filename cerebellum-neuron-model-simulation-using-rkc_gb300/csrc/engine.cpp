@@ -949,7 +949,6 @@ int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
   if (end > E->mega_grid || end <= 0)
     return fail(GBRKC_ESTATE, "persistent launch: %d role CTAs for a grid of %d", end, E->mega_grid);
   M.gr_nc4 = E->pools[GR].team == TEAM_LANE4;
-  M.go_tile = E->pools[GO].team == TEAM_TILE16 ? TEAM_TILE16 : TEAM_WARP;
   // granule warps spread as evenly as whole warps allow: the first
   // lane_extra CTAs take lane_warps + 1
   M.lane_warps = 0;
@@ -1129,13 +1128,8 @@ int setup_mega(gbrkc_engine *E) {
   if (!O.systems.empty() && O.max_nc > 320) return 0;
   // granule CTAs run up to MEGA_BLOCK single-lane systems (capped below at one
   // warp per CTA); Golgi 8 warps; Purkinje / olive one system per CTA
-  // Golgi systems on 32-lane tiles; GBRKC_GO_TILE=16 puts two in a warp
-  // (measured on the mixed workload: the Golgi role then needs ~63 CTAs
-  // instead of ~42 for the same makespan, and the step is 6% slower)
-  const char *gt = getenv("GBRKC_GO_TILE");
-  const int go_tile = (gt && atoi(gt) == 16) ? TEAM_TILE16 : TEAM_WARP;
-  const int teams[NTYPES] = {32, MEGA_BLOCK / go_tile, 1, 1};
-  const int team_kind[NTYPES] = {(G.min_nc == 4 && G.max_nc == 4 && G.max_ncell == 1) ? TEAM_LANE4 : TEAM_THREAD, go_tile,
+  const int teams[NTYPES] = {32, MEGA_BLOCK / TEAM_WARP, 1, 1};
+  const int team_kind[NTYPES] = {(G.min_nc == 4 && G.max_nc == 4 && G.max_ncell == 1) ? TEAM_LANE4 : TEAM_THREAD, TEAM_WARP,
                                  TEAM_BLOCK, TEAM_BLOCK};
   size_t smem = 0;
   int nonempty = 0;
@@ -2006,7 +2000,6 @@ int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, int init, 
   if (end > E->mega_grid || end <= 0)
     return fail(GBRKC_ESTATE, "persistent launch: %d role CTAs for a grid of %d", end, E->mega_grid);
   M.gr_nc4 = E->pools[GR].team == TEAM_LANE4;
-  M.go_tile = E->pools[GO].team == TEAM_TILE16 ? TEAM_TILE16 : TEAM_WARP;
   M.lane_warps = 0;
   M.lane_extra = 0;
   if (E->role_ctas[GR] > 0) {

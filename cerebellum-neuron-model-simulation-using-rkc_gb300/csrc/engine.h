@@ -159,7 +159,7 @@ int launch_syn_update(const SynView &S, void *stream, double t, long long interv
 // (very large systems; 16 is a non-portable cluster size, used where the
 // device can co-schedule it).
 enum TeamKind {
-  TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_TILE16 = 16, TEAM_WARP = 32, TEAM_BLOCK = 0,
+  TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0,
   TEAM_CLUSTER8 = 108, TEAM_CLUSTER16 = 116
 };
 constexpr int team_cluster_size(int team) {
@@ -176,7 +176,6 @@ struct MegaView {
   int role_end[NTYPES];
   int lane_warps, lane_extra;  // granule CTA b runs lane_warps (+1 if b < lane_extra) warps
   int gr_nc4;                 // every granule system has 4 compartments
-  int go_tile;                // lanes per Golgi system: 32 or 16
   int *queue;                 // [NTYPES] next-system counters, zeroed per launch
   unsigned long long *t_start; // [grid] globaltimer at each CTA's start
   unsigned long long *t_end;   // [grid] globaltimer at each CTA's finish

@@ -123,12 +123,7 @@ __global__ void __launch_bounds__(MEGA_BLOCK, 1) k_mega(const __grid_constant__ 
           run_lanes<GR, R, MEGA_BLOCK>(M.pool[GR], M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
       }
       break;
-    case GO:
-      if (M.go_tile == TEAM_TILE16)
-        role_tiles<GO, R, TEAM_TILE16>(M.pool[GO], M.queue + GO, smem, t0, n_iv, iv0, init);
-      else
-        role_tiles<GO, R, TEAM_WARP>(M.pool[GO], M.queue + GO, smem, t0, n_iv, iv0, init);
-      break;
+    case GO: role_tiles<GO, R, TEAM_WARP>(M.pool[GO], M.queue + GO, smem, t0, n_iv, iv0, init); break;
     case PKJ: role_block<PKJ, R>(M.pool[PKJ], M.queue + PKJ, smem, t0, n_iv, iv0, init); break;
     default: role_block<IO, R>(M.pool[IO], M.queue + IO, smem, t0, n_iv, iv0, init); break;
   }
@@ -178,7 +173,6 @@ static const void *kernel_for(int team) {
     case TEAM_THREAD: return (const void *)k_advance<CT, R, TEAM_THREAD>;
     case TEAM_TILE4: return (const void *)k_advance<CT, R, TEAM_TILE4>;
     case TEAM_WARP: return (const void *)k_advance<CT, R, TEAM_WARP>;
-    case TEAM_TILE16: return (const void *)k_advance<CT, R, TEAM_TILE16>;
     default: return (const void *)k_advance<CT, R, TEAM_BLOCK>;
   }
 }
