@@ -41,7 +41,7 @@ struct TypeRun {
   void (*out)(neuron_t *, double *, double *, double, FILE *, FILE *);
   void (*fin)(neuron_t *, neuron_t *, FILE *, FILE *);
   void (*solve_fin)(int, neuron_solve_t *, neuron_solve_t *);
-  char solver[GBRKC_MAX_BUF];
+  char solver[GBRKC_MAX_BUF] = {};
   neuron_t *p = nullptr, *d = nullptr;
   neuron_solve_t *ps = nullptr, *ds = nullptr;
   FILE *fv = nullptr, *fr = nullptr;

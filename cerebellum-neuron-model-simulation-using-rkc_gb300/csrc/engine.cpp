@@ -1474,8 +1474,8 @@ extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
 extern "C" int gbrkc_retired_systems(gbrkc_engine *E) { return E ? E->n_retired : 0; }
 
 extern "C" int gbrkc_read(gbrkc_engine *E, int id, int field, int k, double *host, long n) {
-  PoolHost *P;
-  HostSystem *S;
+  PoolHost *P = nullptr;
+  HostSystem *S = nullptr;
   int rc = system_loc(E, id, &P, &S);
   if (rc) return rc;
   if (!host || n < 0 || n > S->nc) return fail(GBRKC_EINVAL, "bad buffer");
@@ -1513,8 +1513,8 @@ extern "C" int gbrkc_read(gbrkc_engine *E, int id, int field, int k, double *hos
 }
 
 extern "C" int gbrkc_field_device_ptr(gbrkc_engine *E, int id, int field, double **ptr) {
-  PoolHost *P;
-  HostSystem *S;
+  PoolHost *P = nullptr;
+  HostSystem *S = nullptr;
   int rc = system_loc(E, id, &P, &S);
   if (rc) return rc;
   if (!ptr) return fail(GBRKC_EINVAL, "null output");
@@ -1533,8 +1533,8 @@ extern "C" int gbrkc_field_device_ptr(gbrkc_engine *E, int id, int field, double
 }
 
 extern "C" int gbrkc_system_ctl(gbrkc_engine *E, int id, double *ctl8, long long *stats6, int *status) {
-  PoolHost *P;
-  HostSystem *S;
+  PoolHost *P = nullptr;
+  HostSystem *S = nullptr;
   int rc = system_loc(E, id, &P, &S);
   if (rc) return rc;
   Ctl c;
@@ -1553,8 +1553,8 @@ extern "C" int gbrkc_system_ctl(gbrkc_engine *E, int id, double *ctl8, long long
 
 extern "C" int gbrkc_set_stim(gbrkc_engine *E, int id, const int *comp, const double *amp,
                               const double *t0, const double *t1) {
-  PoolHost *P;
-  HostSystem *S;
+  PoolHost *P = nullptr;
+  HostSystem *S = nullptr;
   int rc = system_loc(E, id, &P, &S);
   if (rc) return rc;
   if (!comp || !amp || !t0 || !t1) return fail(GBRKC_EINVAL, "null stimulus");
@@ -1709,8 +1709,8 @@ extern "C" int gbrkc_record_width(gbrkc_engine *E, int type, int width) {
 }
 
 extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) {
-  PoolHost *P;
-  HostSystem *S;
+  PoolHost *P = nullptr;
+  HostSystem *S = nullptr;
   int rc = system_loc(E, id, &P, &S);
   if (rc) return rc;
   if (!P->d_soma || n_iv > E->soma_iv || !host) return fail(GBRKC_EINVAL, "no such recording");
