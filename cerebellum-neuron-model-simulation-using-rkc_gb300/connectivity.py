@@ -25,7 +25,9 @@ in the reference's enumeration order (which fixes the synapse ids):
   weight W_GRPKJ / (512 n / 10), n = the Purkinje cell's connection count.
 
 The reference draws f with cuRAND; here f comes from the caller's numpy
-Generator.  Weight constants: syn.cuh:54-58.
+Generator, or from splitmix_uniform(seed, k) -- the draws the drop-in's
+network mode makes (k counts the draws in order).  Weight constants:
+syn.cuh:54-58.
 """
 from __future__ import annotations
 
@@ -39,6 +41,20 @@ N_SYN_PER_GRPKJ = 25
 GR_AXON0 = 250 + 77          # granule axon compartment level with the soma row
 GR_SOMA, GO_SOMA, GO_OUT = 16, 0, 30
 SYN_MFGR, SYN_GRGO, SYN_GOGR, SYN_GRPKJ = 0, 1, 2, 3
+
+
+_M64 = (1 << 64) - 1
+
+
+def splitmix_uniform(seed: int, idx: int, counter: int = 0) -> float:
+    """The SplitMix64 finaliser over (seed, index, counter) as a double in
+    (0, 1] -- the same formula as the library's splitmix.h."""
+    z = (seed ^ ((idx * 0xD1B54A32D192ED03) & _M64) ^ ((counter * 0x9E3779B97F4A7C15) & _M64)) & _M64
+    z = (z + 0x9E3779B97F4A7C15) & _M64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+    z ^= z >> 31
+    return float((z >> 11) + 1) * 2.0 ** -53
 
 
 def read_pkj_location(path: str):
@@ -56,10 +72,11 @@ def _big_xy(i, nx):
     return float(int(i % nx) * 32.0 + 8.0), float(int(i // nx) * 32.0 + 8.0)
 
 
-def reference_synapses(nx_gr, ny_gr, nx_go, ny_go, nx_pkj, ny_pkj, pkj_x=None, rng=None):
+def reference_synapses(nx_gr, ny_gr, nx_go, ny_go, nx_pkj, ny_pkj, pkj_x=None, rng=None, uniform=None):
     """Synapse groups of the reference network, keyed by kind: dicts of
     pre_cell, pre_comp, post_cell, post_comp, weight (cell = index within its
-    type's grid; compartments within the cell)."""
+    type's grid; compartments within the cell).  uniform(k), if given, is the
+    k-th draw in (0, 1] of the Purkinje targets (else rng)."""
     n_gr, n_go, n_pkj = nx_gr * ny_gr, nx_go * ny_go, nx_pkj * ny_pkj
     out = {}
     # MF -> GrC
@@ -110,13 +127,16 @@ def reference_synapses(nx_gr, ny_gr, nx_go, ny_go, nx_pkj, ny_pkj, pkj_x=None, r
     rng = rng if rng is not None else np.random.default_rng(0)
     pre_cell, pre_comp, post_cell, post_comp, w = [], [], [], [], []
     x = None if pkj_x is None else np.asarray(pkj_x, float)
+    k_draw = 0
     for i_gr, i_pkj in pairs:
         dx = (i_gr % nx_gr) * 16.0 - (8.0 + (i_pkj % nx_pkj) * 32.0)
         dy = (i_gr // nx_gr) * 16.0 - (8.0 + (i_pkj // nx_pkj) * 32.0)
         ax = GR_AXON0 + int(dy / 10.0)
         best, min_x = -1, 1000000.0
         for _ in range(N_SYN_PER_GRPKJ):
-            f = (1.0 - rng.random()) - 0.5          # (0, 1] like curand_uniform, minus 0.5
+            u = uniform(k_draw) if uniform is not None else 1.0 - rng.random()   # (0, 1] like curand_uniform
+            k_draw += 1
+            f = u - 0.5
             d = np.abs(x - dx + 10.0 * f)
             k = int(np.argmin(d))                    # first of the smallest, as the strict < scan
             if d[k] < min_x:

@@ -1,6 +1,6 @@
 // gbrkc_main: the reference's command line over gbrkc_compat.h.
 //
-//   gbrkc_main S_gr gx gy S_go ox oy S_pkj px py S_io ix iy [TS_ms [batch]]
+//   gbrkc_main S_gr gx gy S_go ox oy S_pkj px py S_io ix iy [TS_ms [batch [network]]]
 //
 // S is the solver name per type, matched on its first three letters as the
 // reference does (main.cu:60-102); only RKC is provided.  A type with
@@ -14,7 +14,10 @@
 // voltage record and raster evaluated on the device
 // (gbrkc_compat_advance_batch), and a writer thread formats the same CSV
 // rows from the recorded columns while the GPU runs the next batch.  The
-// files are byte-identical to the per-interval path's.
+// files are byte-identical to the per-interval path's.  network = 1 runs
+// main.cu's network_sim branch: no stimulus kernels, and the synapse updates
+// after every interval (batch must then be 1).  The coupling objects are
+// created in either case, as main.cu:137-145 does.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -124,8 +127,9 @@ int main(int argc, char **argv) {
   }
   const double ts = (argc > 13) ? atof(argv[13]) : 1500.0;
   const int batch = (argc > 14) ? atoi(argv[14]) : 1;
-  if (batch < 1) {
-    printf("batch must be >= 1\n");
+  const bool network = (argc > 15) && atoi(argv[15]) != 0;
+  if (batch < 1 || (network && batch != 1)) {
+    printf("batch must be >= 1 (and 1 in network mode)\n");
     return 1;
   }
   srand(0);  // the initial-voltage jitter stream, seeded as main.cu:38 does
@@ -166,6 +170,12 @@ int main(int argc, char **argv) {
     r.raster = (double *)malloc((r.p->n > 0 ? r.p->n : 1) * sizeof(double));
     for (int j = 0; j < r.p->n; j++) r.raster[j] = 100.0;
   }
+  // the coupling objects (main.cu:137-145)
+  synapse_t *mfgr = mfgr_create(runs[0].p->n);
+  synapse_t *gogr = gogr_create(runs[1].p->nx, runs[1].p->ny, runs[0].p->nx, runs[0].p->ny);
+  synapse_t *grgo = grgo_create(runs[0].p->nx, runs[0].p->ny, runs[1].p->nx, runs[1].p->ny);
+  synapse_t *grpkj = grpkj_create(runs[0].p->nx, runs[0].p->ny, runs[2].p->nx, runs[2].p->ny);
+  synapse_t *mlipkj = mlipkj_create(runs[2].p->n, runs[0].p->n);
   gap_t *io_gap = io_gap_create(nx[3], ny[3]);
   FILE *dbg = fopen("debug_file.csv", "w");
   if (dbg) fclose(dbg);
@@ -221,7 +231,7 @@ int main(int argc, char **argv) {
     for (int k = 0; k < 4; k++) {
       TypeRun &r = runs[k];
       if (r.p->n <= 0) continue;
-      r.stim(r.d, t);
+      if (!network) r.stim(r.d, t);
       update[k](r);
       if (cudaMemcpy(r.vh, r.ps->vec[v_new], r.p->nc * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
         printf("copy of %s voltages failed\n", r.name);
@@ -232,6 +242,11 @@ int main(int argc, char **argv) {
         return 1;
       }
       r.out(r.p, r.vh, r.raster, t + H_MAX, r.fv, r.fr);
+    }
+    if (network) {  // main.cu:300-305
+      gr_synapse_update(t, H_MAX, mfgr, gogr, runs[1].d, runs[0].ps);
+      go_synapse_update(t, H_MAX, grgo, runs[0].d, runs[1].ps);
+      pkj_synapse_update(t, H_MAX, grpkj, mlipkj, runs[0].d, runs[2].ps);
     }
     t += H_MAX;
     if (t >= 500.0 && 500.0 + H_MAX > t) half = clock();
@@ -245,6 +260,11 @@ int main(int argc, char **argv) {
   else
     output_time2(n[0], runs[0].solver, n[1], runs[1].solver, n[2], runs[2].solver, n[3], runs[3].solver, comp,
                  (double)(end - half) / CLOCKS_PER_SEC, (int)ts);
+  mfgr_finalize(mfgr, n[0]);
+  gogr_finalize(gogr, n[1] * n[0]);
+  grgo_finalize(grgo, n[1] * n[0]);
+  grpkj_finalize(grpkj, n[0] * n[2]);
+  mlipkj_finalize(mlipkj, n[0] * n[2]);
   io_gap_finalize(io_gap);
   for (int k = 0; k < 4; k++) {
     TypeRun &r = runs[k];

@@ -15,6 +15,7 @@
 
 #include "../../include/gbrkc.h"
 #include "../../include/gbrkc_compat.h"
+#include "splitmix.h"
 
 namespace {
 
@@ -28,9 +29,12 @@ const int REF_NCOMP_GR = 578;
 struct Block {
   gbrkc_engine *eng = nullptr;
   int sid = -1;
-  int n = 0, ncomp = 0;
+  int n = 0, ncomp = 0, nx = 0, ny = 0;
   int stim_comp = 0;              // compartment of every cell the protocol drives
   int batch_cap = 0;              // batched output: intervals the recorder holds
+  std::vector<double> rows, jitter;  // the block's description, kept for network mode
+  std::vector<int> pairs;
+  bool shared = false;            // network mode: the block lives in the shared engine
   double t = 0.0;                 // start of the next interval
   neuron_t *d_neuron = nullptr;   // device copy of the mirror (for stimulus kernels)
   double **d_elem = nullptr;      // device table behind d_neuron->elem
@@ -138,6 +142,8 @@ neuron_t *initialize(int type, int nx, int ny, const char *solver, neuron_t *p) 
   p->ny = ny;
   p->DT = RKC_DT;
   B.n = n;
+  B.nx = nx;
+  B.ny = ny;
   B.t = 0.0;
   B.h_elem = (double **)calloc(n_elem, sizeof(double *));
   p->elem = B.h_elem;
@@ -152,6 +158,9 @@ neuron_t *initialize(int type, int nx, int ny, const char *solver, neuron_t *p) 
       if (gj.size() % 2) die("Pkj_GJ.csv has a partial pair");
       for (double x : gj) pairs.push_back((int)x);
     }
+    B.rows = rows;
+    B.jitter = jitter;
+    B.pairs = pairs;
     check(gbrkc_engine_create(GBRKC_FP64, &B.eng), "engine");
     gbrkc_system_desc d;
     memset(&d, 0, sizeof d);
@@ -200,11 +209,17 @@ neuron_solve_t *solve_initialize(int type, neuron_solve_t *ps, const char *solve
   return B.d_solve;
 }
 
+void network_advance(Block &B);
+
 void update_v(int type) {
   Block &B = g_block[type];
   if (B.n == 0) return;
   // the caller's stimulus kernel ran on the default stream
   cuda_check(cudaStreamSynchronize(0), "stimulus");
+  if (B.shared) {
+    network_advance(B);
+    return;
+  }
   const int rc = gbrkc_advance(B.eng, B.t, 1);
   if (rc != 0) {
     printf("%s: %s\n", TYPE_NAME[type], gbrkc_last_error());
@@ -251,9 +266,13 @@ void output(int type, neuron_t *p, double *vh, double *rprev, double t, FILE *fv
   }
 }
 
+void network_release();
+
 void finalize(int type, neuron_t *p, FILE *fv, FILE *fr) {
   Block &B = g_block[type];
   if (B.eng) gbrkc_engine_destroy(B.eng);
+  if (B.shared) network_release();
+  B.shared = false;
   if (B.d_neuron) cudaFree(B.d_neuron);
   if (B.d_elem) cudaFree(B.d_elem);
   free(B.h_elem);
@@ -282,6 +301,252 @@ void launch_stim(int type, neuron_t *d, double t);
 struct _gap_t {
   int nx, ny;
 };
+
+struct _synapse_t {
+  int kind;
+};
+
+namespace {
+
+// ------------------------------------------------------------ network mode
+// The reference's network path (main.cu with network_sim true): every
+// interval each type advances, then gr/go/pkj_synapse_update refresh the
+// synapses from the new voltages.  The blocks then have to share one engine
+// (synapses join systems of different types), which the per-type
+// initialisation could not know: on the first X_synapse_update the blocks
+// move into one engine wired by the reference's rules (syn.cu's *_create),
+// which replays the interval already run -- bit for bit the same, as every
+// synaptic value is still 0 in it -- and from then on the first
+// X_solve_update_v of an interval advances every block and the synapses
+// together; the other calls of that interval have nothing left to do.
+enum { SYN_K_MFGR = 0, SYN_K_GRGO = 1, SYN_K_GOGR = 2, SYN_K_GRPKJ = 3, SYN_K_MLIPKJ = 4 };
+
+struct Net {
+  bool on = false;
+  bool made[5] = {};
+  unsigned long long seed_mf = 0, seed_pk = 0;
+  gbrkc_engine *eng = nullptr;
+  int sid[NTYPES] = {-1, -1, -1, -1};
+  double t = 0.0;  // start of the shared engine's next interval
+  int refs = 0;
+} g_net;
+
+synapse_t *net_create(int kind, int) {
+  g_net.made[kind] = true;
+  // the reference seeds its cuRAND streams with rand() here (syn.cu:82, 611)
+  if (kind == SYN_K_MFGR) g_net.seed_mf = (unsigned long long)rand();
+  if (kind == SYN_K_GRPKJ) g_net.seed_pk = (unsigned long long)rand();
+  return new _synapse_t{kind};
+}
+
+// the reference's wiring (syn.cu:146-262, 295-410, 455-619) on the blocks'
+// grids: granule cell i at 16 (i mod nx, i div nx) um, Golgi and Purkinje
+// cells at 32 (i mod nx, i div nx) + 8 um
+struct Wire {
+  std::vector<int> pre_cell, pre_comp, post_cell, post_comp;
+  std::vector<double> w;
+};
+
+void wire_grgo(int gx, int gy, int ox, int oy, Wire &W) {
+  const int n_gr = gx * gy, n_go = ox * oy;
+  std::vector<int> cnt(n_go, 0);
+  for (int a = 0; a < n_gr; a++)
+    for (int b = 0; b < n_go; b++) {
+      const double xg = (a % gx) * 16.0, yg = (a / gx) * 16.0, xo = (b % ox) * 32.0 + 8.0, yo = (b / ox) * 32.0 + 8.0;
+      if (fabs(xo - xg) < 16.0 && fabs(yo - yg) < 220.0) {
+        const float diff = (float)(8.0 + (b / ox) * 32.0 - (a / gx) * 16.0);
+        W.pre_cell.push_back(a);
+        W.pre_comp.push_back(250 + 77 - (int)(diff / 10.0));
+        W.post_cell.push_back(b);
+        W.post_comp.push_back(0);
+        cnt[b]++;
+      }
+    }
+  for (int b : W.post_cell) W.w.push_back(64.0 / 4.0 / (cnt[b] * 1.0 / 4.0));  // W_GRGO / (n / 4)
+}
+
+void wire_gogr(int ox, int oy, int gx, int gy, Wire &W) {
+  const int n_gr = gx * gy, n_go = ox * oy;
+  std::vector<int> cnt(n_gr, 0);
+  for (int b = 0; b < n_go; b++)
+    for (int a = 0; a < n_gr; a++) {
+      const double xg = (a % gx) * 16.0, yg = (a / gx) * 16.0, xo = (b % ox) * 32.0 + 8.0, yo = (b / ox) * 32.0 + 8.0;
+      if (fabs(xo - xg) < 32.0 && fabs(yo - yg) < 32.0) {
+        W.pre_cell.push_back(b);
+        W.pre_comp.push_back(30);  // GO_COMP_DEND * 3
+        W.post_cell.push_back(a);
+        W.post_comp.push_back(16);
+        cnt[a]++;
+      }
+    }
+  for (int a : W.post_cell) W.w.push_back(160000.0 * 4.0 / (cnt[a] * 4.0));  // W_GOGR / (4 n)
+}
+
+void wire_grpkj(int gx, int gy, int px, int py, const std::vector<double> &x, unsigned long long seed, Wire &W) {
+  const int n_gr = gx * gy, n_pkj = px * py;
+  std::vector<std::pair<int, int>> pairs;
+  std::vector<int> cnt(n_pkj, 0);
+  for (int a = 0; a < n_gr; a++)
+    for (int b = 0; b < n_pkj; b++) {
+      const double xg = (a % gx) * 16.0, yg = (a / gx) * 16.0, xp = (b % px) * 32.0 + 8.0, yp = (b / px) * 32.0 + 8.0;
+      if (fabs(xp - xg) < 120.0 && fabs(yp - yg) < 220.0) {
+        pairs.push_back({a, b});
+        cnt[b]++;
+      }
+    }
+  long long k = 0;
+  for (const auto &pr : pairs) {
+    const int a = pr.first, b = pr.second;
+    const double dx = (a % gx) * 16.0 - (8.0 + (b % px) * 32.0);
+    const double dy = (a / gx) * 16.0 - (8.0 + (b / px) * 32.0);
+    const int ax = 250 + 77 + (int)(dy / 10.0);
+    int best = -1;
+    double min_x = 1000000.0;
+    for (int i = 0; i < 25; i++, k++) {  // N_Syn_Per_GRPKJ, the running minimum kept (syn.cu:489-499)
+      const double f = gbrkc::splitmix_uniform(seed, k, 0) - 0.5;
+      for (size_t c = 0; c < x.size(); c++) {
+        const double d = fabs(x[c] - dx + 10.0 * f);
+        if (d < min_x) {
+          min_x = d;
+          best = (int)c;
+        }
+      }
+      W.pre_cell.push_back(a);
+      W.pre_comp.push_back(ax);
+      W.post_cell.push_back(b);
+      W.post_comp.push_back(best);
+      W.w.push_back(1000000.0 * 0.3 / (512.0 * cnt[b] * 1.0 * 1 / 10.0));  // W_GRPKJ / (512 n / 10)
+    }
+  }
+}
+
+void add_wire(gbrkc_engine *E, int kind, int pre_type, int post_type, const Wire &W, unsigned long long seed) {
+  if (W.post_cell.empty()) return;
+  const Block &Pre = g_block[pre_type < 0 ? GBRKC_GR : pre_type], &Post = g_block[post_type];
+  const size_t n = W.post_cell.size();
+  std::vector<int> ps(n), pc(n), qs(n, g_net.sid[post_type]), qc(n);
+  for (size_t i = 0; i < n; i++) {
+    qc[i] = W.post_cell[i] * Post.ncomp + W.post_comp[i];
+    if (pre_type >= 0) {
+      ps[i] = g_net.sid[pre_type];
+      pc[i] = W.pre_cell[i] * Pre.ncomp + W.pre_comp[i];
+    }
+  }
+  gbrkc_synapse_desc d;
+  memset(&d, 0, sizeof d);
+  d.kind = kind;
+  d.n = (int)n;
+  d.pre_system = pre_type >= 0 ? ps.data() : nullptr;
+  d.pre_comp = pre_type >= 0 ? pc.data() : nullptr;
+  d.post_system = qs.data();
+  d.post_comp = qc.data();
+  d.weight = W.w.data();
+  d.seed = seed;
+  check(gbrkc_add_synapses(E, &d, nullptr), "synapses");
+}
+
+void network_on() {
+  if (g_net.on) return;
+  // the blocks have run 0 or 1 intervals, all the same
+  double t_done = -1.0;
+  for (int k = 0; k < NTYPES; k++) {
+    const Block &B = g_block[k];
+    if (B.n == 0) continue;
+    if (t_done < 0.0) t_done = B.t;
+    if (B.t != t_done) die("network mode: the blocks have advanced unequally");
+  }
+  if (t_done < 0.0) return;
+  if (t_done > H_MAX) die("network mode: synapse updates must start after the first interval");
+  gbrkc_engine *E = nullptr;
+  check(gbrkc_engine_create(GBRKC_FP64, &E), "engine");
+  for (int k = 0; k < NTYPES; k++) {
+    Block &B = g_block[k];
+    if (B.n == 0) continue;
+    gbrkc_system_desc d;
+    memset(&d, 0, sizeof d);
+    d.cell_type = k;
+    d.nx = B.nx;
+    d.ny = B.ny;
+    d.ncomp = B.ncomp;
+    d.rows = B.rows.data();
+    d.gj_pairs = B.pairs.empty() ? nullptr : B.pairs.data();
+    d.n_gj_pairs = (int)B.pairs.size() / 2;
+    d.gap_junctions = 1;
+    d.jitter = B.jitter.data();
+    check(gbrkc_add_system(E, &d, &g_net.sid[k]), "add system");
+  }
+  const Block &GR = g_block[GBRKC_GR], &GO = g_block[GBRKC_GO], &PK = g_block[GBRKC_PKJ];
+  const bool full_gr = GR.n == 0 || GR.ncomp >= 578;
+  if (GR.n > 0 && g_net.made[SYN_K_MFGR]) {
+    Wire W;
+    for (int a = 0; a < GR.n; a++)
+      for (int j = 0; j < 4; j++) {  // four fibres onto compartments 0-3, W_MFGR / 4 (syn.cu:43-62)
+        W.post_cell.push_back(a);
+        W.post_comp.push_back(j);
+        W.w.push_back(40000.0 / 4.0);
+      }
+    add_wire(E, GBRKC_SYN_MFGR, -1, GBRKC_GR, W, g_net.seed_mf);
+  }
+  if (GR.n > 0 && GO.n > 0 && (g_net.made[SYN_K_GRGO] || g_net.made[SYN_K_GOGR])) {
+    if (!full_gr) die("network mode: the granule -> Golgi wiring needs the 578-compartment granule cell");
+    Wire A, B;
+    if (g_net.made[SYN_K_GRGO]) wire_grgo(GR.nx, GR.ny, GO.nx, GO.ny, A);
+    if (g_net.made[SYN_K_GOGR]) wire_gogr(GO.nx, GO.ny, GR.nx, GR.ny, B);
+    add_wire(E, GBRKC_SYN_GRGO, GBRKC_GR, GBRKC_GO, A, 0);
+    add_wire(E, GBRKC_SYN_GOGR, GBRKC_GO, GBRKC_GR, B, 0);
+  }
+  if (GR.n > 0 && PK.n > 0 && g_net.made[SYN_K_GRPKJ]) {
+    if (!full_gr) die("network mode: the granule -> Purkinje wiring needs the 578-compartment granule cell");
+    // Pkj_location_info.csv: index, x, y, z, type per Purkinje compartment (syn.cu:536-553)
+    const std::vector<double> loc = read_numbers(model_path("Pkj_location_info.csv"), ',');
+    if (loc.size() < (size_t)PK.ncomp * 5) die("Pkj_location_info.csv holds fewer rows than Pkj.txt");
+    std::vector<double> x(PK.ncomp);
+    for (int c = 0; c < PK.ncomp; c++) x[c] = loc[(size_t)c * 5 + 1];
+    Wire W;
+    wire_grpkj(GR.nx, GR.ny, PK.nx, PK.ny, x, g_net.seed_pk, W);
+    add_wire(E, GBRKC_SYN_GRPKJ, GBRKC_GR, GBRKC_PKJ, W, 0);
+  }
+  check(gbrkc_build(E), "build");
+  // replay the interval the blocks ran alone (no synaptic input yet), with
+  // the synapse update that ends it
+  if (t_done > 0.0) check(gbrkc_advance(E, 0.0, 1), "network advance");
+  for (int k = 0; k < NTYPES; k++) {
+    Block &B = g_block[k];
+    if (B.n == 0) continue;
+    check(gbrkc_field_device_ptr(E, g_net.sid[k], GBRKC_F_V, &B.h_elem[v]), "elem[v]");
+    check(gbrkc_field_device_ptr(E, g_net.sid[k], GBRKC_F_CA, &B.h_elem[Ca]), "elem[Ca]");
+    check(gbrkc_field_device_ptr(E, g_net.sid[k], GBRKC_F_IEXT, &B.h_elem[i_ext]), "elem[i_ext]");
+    cuda_check(cudaMemcpy(B.d_elem, B.h_elem, n_elem * sizeof(double *), cudaMemcpyHostToDevice), "device table");
+    if (B.h_vec) check(gbrkc_field_device_ptr(E, g_net.sid[k], GBRKC_F_VNEW, &B.h_vec[v_new]), "vec[v_new]");
+    gbrkc_engine_destroy(B.eng);
+    B.eng = nullptr;
+    B.shared = true;
+    g_net.refs++;
+  }
+  g_net.eng = E;
+  g_net.t = t_done;
+  g_net.on = true;
+}
+
+void network_advance(Block &B) {
+  if (B.t >= g_net.t) {
+    const int rc = gbrkc_advance(g_net.eng, g_net.t, 1);
+    if (rc != 0) {
+      printf("network: %s\n", gbrkc_last_error());
+      exit(1);
+    }
+    g_net.t += H_MAX;
+  }
+  B.t += H_MAX;
+}
+
+void network_release() {
+  if (--g_net.refs > 0) return;
+  if (g_net.eng) gbrkc_engine_destroy(g_net.eng);
+  g_net = Net();
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -363,24 +628,31 @@ void go_solve_finalize(const int, neuron_solve_t *, neuron_solve_t *ps) { solve_
 void pkj_solve_finalize(const int, neuron_solve_t *, neuron_solve_t *ps) { solve_finalize(GBRKC_PKJ, ps); }
 void io_solve_finalize(const int, neuron_solve_t *, neuron_solve_t *ps) { solve_finalize(GBRKC_IO, ps); }
 
-synapse_t *mfgr_create(const int) { return nullptr; }
-synapse_t *gogr_create(const int, const int, const int, const int) { return nullptr; }
-synapse_t *grgo_create(const int, const int, const int, const int) { return nullptr; }
-synapse_t *grpkj_create(const int, const int, const int, const int) { return nullptr; }
-synapse_t *mlipkj_create(const int, const int) { return nullptr; }
-void mfgr_finalize(synapse_t *, const int) {}
-void gogr_finalize(synapse_t *, const int) {}
-void grgo_finalize(synapse_t *, const int) {}
-void grpkj_finalize(synapse_t *, const int) {}
-void mlipkj_finalize(synapse_t *, const int) {}
+// The coupling objects only record which synapse families the caller asked
+// for (and, like the reference, take a rand() seed for the random ones); the
+// network is wired and built on the first X_synapse_update call.
+synapse_t *mfgr_create(const int n) { return net_create(SYN_K_MFGR, n); }
+synapse_t *gogr_create(const int go_x, const int go_y, const int gr_x, const int gr_y) {
+  return net_create(SYN_K_GOGR, go_x * go_y * gr_x * gr_y);
+}
+synapse_t *grgo_create(const int gr_x, const int gr_y, const int go_x, const int go_y) {
+  return net_create(SYN_K_GRGO, go_x * go_y * gr_x * gr_y);
+}
+synapse_t *grpkj_create(const int gr_x, const int gr_y, const int pkj_x, const int pkj_y) {
+  return net_create(SYN_K_GRPKJ, gr_x * gr_y * pkj_x * pkj_y);
+}
+synapse_t *mlipkj_create(const int n_pkj, const int n_gr) { return net_create(SYN_K_MLIPKJ, n_pkj * n_gr); }
+void mfgr_finalize(synapse_t *s, const int) { delete s; }
+void gogr_finalize(synapse_t *s, const int) { delete s; }
+void grgo_finalize(synapse_t *s, const int) { delete s; }
+void grpkj_finalize(synapse_t *s, const int) { delete s; }
+void mlipkj_finalize(synapse_t *s, const int) { delete s; }
 void gr_synapse_update(const double, const double, synapse_t *, synapse_t *, neuron_t *, neuron_solve_t *) {
-  die("gr_synapse_update: network mode is not provided");
+  network_on();
 }
-void go_synapse_update(const double, const double, synapse_t *, neuron_t *, neuron_solve_t *) {
-  die("go_synapse_update: network mode is not provided");
-}
+void go_synapse_update(const double, const double, synapse_t *, neuron_t *, neuron_solve_t *) { network_on(); }
 void pkj_synapse_update(const double, const double, synapse_t *, synapse_t *, neuron_t *, neuron_solve_t *) {
-  die("pkj_synapse_update: network mode is not provided");
+  network_on();
 }
 
 gap_t *io_gap_create(const int nx, const int ny) {
@@ -442,6 +714,7 @@ extern "C" long gbrkc_compat_advance_batch(int type, int n, double *rows, long r
   if (type < 0 || type >= NTYPES || n <= 0 || !rows || spk_cap < 0) return GBRKC_EINVAL;
   Block &B = g_block[type];
   if (B.n == 0) return 0;
+  if (B.shared) return GBRKC_EINVAL;  // network mode advances all types together
   const int cols = (type == GBRKC_IO) ? 3 : 1;
   if (row_cap < (long)n * B.n * cols) return GBRKC_EINVAL;
   if (n > B.batch_cap) {

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include "engine.h"
+#include "splitmix.h"
 
 namespace gbrkc {
 
@@ -31,14 +32,8 @@ constexpr double G_GOGR_GABA = 0.028e-9;
 constexpr double G_GRPKJ_AMPA = 0.7e-9;
 constexpr double RKC_DT_MS = 0.125;
 
-__host__ __device__ __forceinline__ double syn_uniform(unsigned long long seed, long long id, long long interval) {
-  unsigned long long z = seed ^ ((unsigned long long)id * 0xD1B54A32D192ED03ull) ^
-                         ((unsigned long long)interval * 0x9E3779B97F4A7C15ull);
-  z += 0x9E3779B97F4A7C15ull;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  z ^= z >> 31;
-  return (double)((z >> 11) + 1ull) * 0x1p-53;  // (0, 1], like curand_uniform
+__device__ __forceinline__ double syn_uniform(unsigned long long seed, long long id, long long interval) {
+  return splitmix_uniform(seed, id, interval);
 }
 
 __device__ __forceinline__ int delayed(const SynView &S, int id, int f_now) {

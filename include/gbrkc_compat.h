@@ -96,9 +96,11 @@ neuron_solve_t *io_solve_initialize(neuron_solve_t *p_solve, const char *type, n
 
 /* Advance the block by one output interval (H_MAX = 0.125 ms) after any
  * stimulus kernel the caller launched on the default stream; on return
- * p_solve->vec[v_new] holds the new voltages.  The coupling objects of
- * network mode are accepted and must be NULL (network mode is not provided).
- * (gr_solve.cu:293, go_solve.cu:362, pkj_solve.cu:395, io_solve.cu:300) */
+ * p_solve->vec[v_new] holds the new voltages.  The coupling objects are the
+ * ones the constructors below return (or NULL); in network mode the first
+ * call of an interval advances every block and the synapses together, and
+ * the others of that interval return at once.  (gr_solve.cu:293,
+ * go_solve.cu:362, pkj_solve.cu:395, io_solve.cu:300) */
 void gr_solve_update_v(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron_solve_t *p_solve, synapse_t *mfgr,
                        synapse_t *gogr);
 void go_solve_update_v(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron_solve_t *p_solve, synapse_t *grgo);
@@ -149,10 +151,21 @@ void go_solve_finalize(const int n, neuron_solve_t *d_solve, neuron_solve_t *p_s
 void pkj_solve_finalize(const int n, neuron_solve_t *d_solve, neuron_solve_t *p_solve);
 void io_solve_finalize(const int n, neuron_solve_t *d_solve, neuron_solve_t *p_solve);
 
-/* Coupling objects (syn.cuh:84-104, gap.cuh:19-21).  Network mode (chemical
- * synapses) is not provided: the synapse constructors return NULL and the
- * synapse updates report an error.  The IO gap junctions are part of the IO
- * system itself (built at io_initialize with the reference's conductance);
+/* Coupling objects (syn.cuh:84-104, gap.cuh:19-21).  The constructors record
+ * the synapse families (mfgr_create and grpkj_create take a rand() seed, as
+ * the reference does).  Network mode (main.cu's network_sim) starts with the
+ * first X_synapse_update, after the first interval: the blocks then move into
+ * one engine, wired by the reference's rules (syn.cu:43-84, 146-262, 295-410,
+ * 455-619; GrC -> PC targets from Pkj_location_info.csv, drawn with a
+ * SplitMix64 stream seeded by that rand() value instead of cuRAND).  That
+ * engine replays the first interval, which is bit-identical because the
+ * synapses are still 0 in it, and from then on advances all blocks and
+ * updates the synapses in one call per interval.  The wiring needs the
+ * reference's 578-compartment granule cell (its axon compartments).  In
+ * network mode a stimulus kernel must come before the interval's first
+ * update call.  mlipkj is never updated or applied on the reference's RKC
+ * path and is accepted only.  The IO gap junctions are part of the IO system
+ * itself (built at io_initialize with the reference's conductance);
  * io_gap_create returns a handle for the caller to pass back and free. */
 synapse_t *mfgr_create(const int n);
 synapse_t *gogr_create(const int go_x, const int go_y, const int gr_x, const int gr_y);

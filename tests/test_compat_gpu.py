@@ -111,3 +111,57 @@ def test_batched_cli_writes_identical_files(tmp_path):
     for f in out[1]:
         assert out[1][f] == out[70][f], f
     assert out[1]["gr_v_by_RKC.csv"].count(b"\n") == 480
+
+
+def test_network_mode_dropin_matches_native(tmp_path, oracle):
+    """gbrkc_main with main.cu's network branch (coupling objects, synapse
+    updates after every interval) against the native ABI wired by the same
+    rules (connectivity.py, SplitMix target draws, rand() seeds in the
+    constructors' order): every written soma voltage identical."""
+    import ctypes
+    import connectivity as CN
+    import gbrkc as G
+    O = oracle
+    gr, go, pk = M.gr_synthetic(11), M.go_synthetic(3), M.pkj_synthetic(4)
+    px = np.random.default_rng(8).uniform(-150, 150, 1600)
+    loc = "".join(f"{i},{x:.6f},0.0,0.0,3\n" for i, x in enumerate(px))
+    gj = "\n".join(f"{a},{b}" for a, b in M.PKJ_GJ_PAIRS) + "\n"
+    files = {"Gr.txt": M.write_rows(gr, M.GR), "Go_131.txt": M.write_rows(go, M.GO),
+             "Pkj.txt": M.write_rows(pk, M.PKJ), "Pkj_GJ.csv": gj, "Pkj_location_info.csv": loc}
+    for name, text in files.items():
+        (tmp_path / name).write_text(text)
+    ts, n_iv = 2.0, 16
+    args = [CLI, "RKC", "2", "2", "RKC", "1", "1", "RKC", "1", "1", "RKC", "0", "0", str(ts), "1", "1"]
+    r = subprocess.run(args, cwd=tmp_path, env=dict(os.environ, GBRKC_MODEL_DIR=str(tmp_path)), capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    # the same run through the native ABI
+    O.libc_srand(0)
+    jit = {t: O.draw_jitter(t, n) for t, n in ((M.GR, 4), (M.GO, 1), (M.PKJ, 1))}
+    libc = ctypes.CDLL(None)
+    seed_mf = libc.rand()        # mfgr_create
+    seed_pk = libc.rand()        # grpkj_create
+    rows = [gr, go, pk]
+    nc = [r_.shape[0] for r_ in rows]
+    eng = G.Engine(G.FP64)
+    sid = [eng.add_system(M.GR, 2, 2, gr, jit[M.GR]), eng.add_system(M.GO, 1, 1, go, jit[M.GO]),
+           eng.add_system(M.PKJ, 1, 1, pk, jit[M.PKJ], gj_pairs=M.PKJ_GJ_PAIRS)]
+    g = CN.reference_synapses(2, 2, 1, 1, 1, 1, px, uniform=lambda k: CN.splitmix_uniform(seed_pk, k))
+    for kind, seed in ((CN.SYN_MFGR, seed_mf), (CN.SYN_GRGO, 0), (CN.SYN_GOGR, 0), (CN.SYN_GRPKJ, 0)):
+        one = {k: (g[k] if k == kind else dict(post_cell=[])) for k in g}
+        CN.add_reference_network(eng, one, lambda ty, c: (sid[ty], c * nc[ty]), seed=seed)
+    eng.build()
+    soma = {M.GR: 16, M.GO: 30, M.PKJ: 1599}
+    got = {name: (tmp_path / f"{name}_v_by_RKC.csv").read_text().splitlines() for name in ("gr", "go", "pkj")}
+    t = 0.0
+    for k in range(n_iv):
+        eng.advance(t, 1)
+        t += 0.125
+        for name, ty, s in (("gr", M.GR, sid[0]), ("go", M.GO, sid[1]), ("pkj", M.PKJ, sid[2])):
+            v = eng.vnew(s)
+            n = v.size // nc[ty]
+            line = "%f," % t + "".join("%f," % v[soma[ty] + j * nc[ty]] for j in range(n))
+            assert got[name][k] == line, (name, k)
+    syn = eng.read_synapses(G.SYNF_S0, sum(len(g[k]["post_cell"]) for k in g))
+    assert syn[:16].max() >= 0.0
+    eng.close()
