@@ -49,3 +49,19 @@ def test_reference_entry_points_present():
         for f in ("initialize", "solve_initialize", "solve_update_v", "set_current", "output_file", "finalize",
                   "solve_finalize"):
             assert f"{t}_{f}" in names
+
+
+@pytest.mark.parametrize("header", ["gbrkc.h", "gbrkc_compat.h"])
+@pytest.mark.parametrize("lang", [("gcc", "c", "-std=c99"), ("g++", "c++", "-std=c++17")])
+def test_header_compiles_alone(tmp_path, header, lang):
+    """Each public header is self-contained C99 and C++17 (a caller may be either)."""
+    import shutil
+    import subprocess
+    cc, x, std = lang
+    if shutil.which(cc) is None:
+        pytest.skip(f"no {cc}")
+    src = tmp_path / "h.c"
+    src.write_text(f'#include "{header}"\n')
+    r = subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", x, f"-I{INCLUDE}", str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
