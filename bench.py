@@ -610,6 +610,15 @@ def main():
                     {names[k]: kern_ms[k] / args.steps for k in range(4)}}
     if persistent:
         roofline["role_ctas"] = {names[k]: role_ctas[k] for k in range(4)}
+    # what bounds the kernel instead: the FP64 pipe, as ncu reported it for the
+    # same kernel (profiles/), beside the HBM fraction above
+    if os.path.exists(tfile):
+        try:
+            tr = json.load(open(tfile))
+            if "fp64_pipe_active" in tr:
+                roofline["fp64_pipe_active_ncu"] = tr["fp64_pipe_active"]
+        except Exception:
+            pass
 
     # end to end through the C ABI with host buffers: per step, upload every
     # cell's stimulus table -- the workload's own protocol, so the dynamics
