@@ -250,3 +250,32 @@ def test_reset_then_noalloc_advance(precision):
     np.testing.assert_array_equal(np.concatenate([b.vnew(2), b.vnew(3)]), ref[G.F_VNEW])
     for eng in engines:
         eng.close()
+
+
+def test_failed_request_is_reported_and_its_slots_reused():
+    """A request whose cells blow up (a 1000x stimulus: non-finite voltages,
+    a solver stop on the device) ends FAILED with the stop status; the
+    request beside it completes, and the freed slots serve the next one."""
+    rng = np.random.default_rng(31)
+    srv = G.Server(G.MIXED, hbm_budget=0, quantum=8)
+    c = srv.add_class(M.GR, 1, 1, rows("gr"), slots=8, gap=False)
+    srv.start()
+    good = srv.submit(c, 4, 12, rng.uniform(-0.5, 0.5, 4), stim=(1, 0.02e-3, 0.0, 1e9))
+    bad = srv.submit(c, 2, 12, rng.uniform(-0.5, 0.5, 2), stim=(1, 1.0, 0.0, 1e9))
+    for _ in range(10):
+        srv.advance()
+        if srv.stats()["resident"] == 0:
+            break
+    st_bad, _, status = srv.state(bad)
+    assert st_bad == G.REQ_FAILED and status != 0
+    assert srv.state(good)[0] == G.REQ_DONE
+    st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == 1 and st["free_slots"] == st["slots"]
+    inp = inputs("gr", 8, rng)
+    nxt = srv.submit(c, 8, 10, inp["jitter"], stim=inp["stim"], cond_scale=inp["cond_scale"])
+    while srv.state(nxt)[0] in (G.REQ_QUEUED, G.REQ_RESIDENT):
+        srv.advance()
+    assert srv.state(nxt)[0] == G.REQ_DONE
+    ref = fresh(G.MIXED, "gr", 8, 10, inp)
+    np.testing.assert_array_equal(srv.read(nxt, 8 * 4), ref[G.F_VNEW])
+    srv.close()
