@@ -40,6 +40,19 @@ H_MAX = 0.125
 ALG_BYTES = {"mixed": 56, "fp64": 68}   # algorithmic bytes per compartment-update
 
 
+def cpu_model():
+    """The host CPU's model name (for the CPU baseline's record)."""
+    try:
+        for line in open("/proc/cpuinfo"):
+            k, _, v = line.partition(":")
+            if k.strip() in ("model name", "Model", "CPU part") and v.strip():
+                return v.strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -436,6 +449,7 @@ def run_reference(args):
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded morphologies and stimuli)",
            "config": {"workload": wl, "precision": "fp64 (reference arithmetic)"},
            "cpu_baseline": {"value": v, "unit": "compartment-updates/s", "cores": cores, "kind": "port",
+                            "cpu": cpu_model(),
                             "sample": sample},
            "e2e": {"value": v, "unit": "compartment-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -708,6 +722,7 @@ def main():
         n_cpu = int(max(4, min(4000, args.cpu_seconds / per_iv)))
         units_c, wall_c, sample = cpu_sample(args.config, frac, n_cpu, 0, 1)
         cpu = {"value": units_c / wall_c, "unit": "compartment-updates/s", "cores": 1, "kind": "port",
+               "cpu": cpu_model(), "nproc": os.cpu_count(),
                "sample": sample + " (oracle, reference arithmetic, FP64, one thread)"}
 
     if rank == 0:
