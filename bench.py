@@ -43,11 +43,12 @@ ALG_BYTES = {"mixed": 56, "fp64": 68}   # algorithmic bytes per compartment-upda
 def cpu_model():
     """The host CPU's model name (for the CPU baseline's record)."""
     try:
-        for line in open("/proc/cpuinfo"):
-            k, _, v = line.partition(":")
-            if k.strip() in ("model name", "Model", "CPU part") and v.strip():
-                return v.strip()
-    except OSError:
+        with open("/proc/cpuinfo", errors="replace") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                if k.strip() in ("model name", "Model", "CPU part") and v.strip():
+                    return v.strip()
+    except Exception:
         pass
     import platform
     return platform.machine()
