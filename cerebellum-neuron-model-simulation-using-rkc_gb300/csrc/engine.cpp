@@ -8,6 +8,7 @@
 // capacitances, conductances, axial conductances) are computed in the same
 // operation order as the reference, so they are bit-identical on every host.
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdlib.h>
@@ -499,6 +500,9 @@ extern "C" int gbrkc_add_system(gbrkc_engine *E, const gbrkc_system_desc *d, int
   if (E->built) return fail(GBRKC_ESTATE, "engine already built");
   if (d->cell_type < 0 || d->cell_type >= NTYPES || d->nx <= 0 || d->ny <= 0 || d->ncomp <= 0)
     return fail(GBRKC_EINVAL, "bad system shape");
+  // compartment indices are 32-bit on the device
+  if ((long long)d->nx * d->ny * d->ncomp > (long long)INT_MAX / 2)
+    return fail(GBRKC_EINVAL, "system too large (%lld compartments)", (long long)d->nx * d->ny * d->ncomp);
   HostSystem S;
   S.type = d->cell_type; S.nx = d->nx; S.ny = d->ny; S.n = d->nx * d->ny; S.ncomp = d->ncomp;
   S.nc = S.n * S.ncomp;

@@ -1,0 +1,157 @@
+"""Edge cases of the native ABI on the GPU.
+
+* Arguments the host rejects before anything is launched: an empty engine, a
+  bad cell type or shape, out-of-range stimulus and gap-junction
+  compartments, broken morphology rows, negative conductance scales, bad
+  synapse kinds, targets and delays, calls out of order, bad ids and fields.
+* A zero-interval advance leaves every state bit as it was, and advancing in
+  pieces (with empty pieces between) equals one call.
+* The largest systems: a Purkinje network that just fits a 16-CTA cluster
+  (14 rows of 256 compartments per CTA) and one that does not (its workspace
+  stays in HBM, one CTA), both bit-exact with the oracle.
+"""
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+import gbrkc as G
+import morph as M
+from gpu_cases import add_to_engine, jitter_for
+
+pytestmark = pytest.mark.gpu
+
+EINVAL, ESTATE = -1, -3
+
+
+def expect(code, fn, *a, **k):
+    with pytest.raises(G.GbrkcError) as ei:
+        fn(*a, **k)
+    got = int(re.search(r"gbrkc error (-?\d+)", str(ei.value)).group(1))
+    assert got == code, str(ei.value)
+
+
+def test_rejected_arguments(oracle):
+    eng = G.Engine(G.FP64)
+    expect(EINVAL, eng.build)                                   # no systems
+    go = M.go_synthetic(2)
+    one = np.zeros(1)
+    expect(EINVAL, eng.add_system, 7, 1, 1, go, one)            # no such cell type
+    expect(EINVAL, eng.add_system, M.GO, 0, 1, go, np.zeros(0))
+    expect(EINVAL, eng.add_system, M.GO, 1, 1, go, one, stim=(go.shape[0], 1e-3, 0.0, 1.0))
+    expect(EINVAL, eng.add_system, M.GO, 1, 1, go, one, cond_scale=-1.0)
+    expect(EINVAL, eng.add_system, M.GO, 1, 1, go, one, cond_scale=np.nan)
+    bad = go.copy()
+    bad[3, 0] = 7                                               # row index != position
+    expect(EINVAL, eng.add_system, M.GO, 1, 1, bad, one)
+    pk = M.pkj_synthetic(2)
+    expect(EINVAL, eng.add_system, M.PKJ, 2, 1, pk, np.zeros(2), gj_pairs=[[0, pk.shape[0]]])
+    d = G.SystemDesc()                                          # 2^32 cells: rejected before
+    d.cell_type, d.nx, d.ny, d.ncomp = M.GO, 1 << 16, 1 << 16, go.shape[0]   # the jitter is read
+    d.rows, d.jitter = G._dp(np.ascontiguousarray(go)), G._dp(one)
+    sid = C.c_int()
+    assert G.lib().gbrkc_add_system(eng.h, C.byref(d), C.byref(sid)) == EINVAL
+
+    gr = add_to_engine(G, oracle, eng, "gr_reduced")
+    gsys = add_to_engine(G, oracle, eng, "go_cell")
+    expect(EINVAL, eng.add_synapses, 9, [gr], [0], 1.0)                      # no such kind
+    expect(EINVAL, eng.add_synapses, 0, [gsys], [0], 1.0)                    # MF onto a Golgi cell
+    expect(EINVAL, eng.add_synapses, 0, [gr], [4], 1.0)                      # compartment past the cell
+    expect(EINVAL, eng.add_synapses, 1, [gsys], [0], 1.0, pre_system=[gsys], pre_comp=[0])  # GR->GO from a GO
+    expect(EINVAL, eng.add_synapses, 0, [gr], [0], 1.0, delay=64)            # ring holds 0..63
+    expect(EINVAL, eng.add_synapses, 0, [gr], [0], 1.0, delay=-1)
+    eng.add_synapses(0, [gr], [0], 1.0, delay=63)
+
+    eng.build()
+    expect(ESTATE, eng.build)
+    expect(ESTATE, eng.add_system, M.GO, 1, 1, go, one)
+    expect(ESTATE, eng.add_synapses, 0, [gr], [0], 1.0)
+    expect(EINVAL, eng.advance, 0.0, -1)
+    L = G.lib()
+    buf = np.zeros(8)
+    assert L.gbrkc_read(eng.h, 99, G.F_VNEW, 0, buf.ctypes.data_as(C.POINTER(C.c_double)), 1) == EINVAL
+    assert L.gbrkc_read(eng.h, gr, 99, 0, buf.ctypes.data_as(C.POINTER(C.c_double)), 1) == EINVAL
+    assert L.gbrkc_read(eng.h, gr, G.F_VNEW, 0, buf.ctypes.data_as(C.POINTER(C.c_double)), 5) == EINVAL
+    assert L.gbrkc_read(eng.h, gr, G.F_ION, 99, buf.ctypes.data_as(C.POINTER(C.c_double)), 1) == EINVAL
+    # the engine is still usable after every rejected call
+    eng.advance(0.0, 2)
+    assert np.all(np.isfinite(eng.vnew(gr)))
+    eng.close()
+
+
+def _snapshot(eng, ids):
+    out = []
+    for sid in ids:
+        out += [eng.read(sid, f) for f in (G.F_VNEW, G.F_V, G.F_CA, G.F_B)]
+        ctl, stats, status = eng.ctl(sid)
+        out += [np.array(list(ctl.values())), np.array(list(stats.values())), np.array([status])]
+    return out
+
+
+@pytest.mark.parametrize("precision", [G.FP64, G.MIXED])
+def test_zero_interval_advance_and_pieces(oracle, precision):
+    names = ("gr_reduced", "go_cell", "pkj_cell", "io_net4x4")
+    engs = []
+    for _ in range(2):
+        eng = G.Engine(precision)
+        ids = [add_to_engine(G, oracle, eng, nm) for nm in names]
+        eng.build()
+        engs.append((eng, ids))
+    (a, ia), (b, ib) = engs
+    before = _snapshot(a, ia)
+    a.advance(0.0, 0)
+    for x, y in zip(before, _snapshot(a, ia)):
+        np.testing.assert_array_equal(x, y)
+    t = 0.0
+    for n in (3, 0, 5, 0, 0, 8):
+        a.advance(t, n)
+        t += n * G.H_MAX
+    b.advance(0.0, 16)
+    for x, y in zip(_snapshot(a, ia), _snapshot(b, ib)):
+        np.testing.assert_array_equal(x, y)
+    a.close()
+    b.close()
+
+
+def _pkj_grid(O, nx, ny, ncomp, n_iv):
+    """A Purkinje nx x ny network (x-neighbour gap junctions), FP64 GPU vs oracle."""
+    rows = M.pkj_synthetic(4, ncomp)
+    stim = (ncomp - 1, 0.5e-3, 0.0, 1e9)
+    jit = jitter_for(O, M.PKJ, nx * ny)
+    s = O.System(M.PKJ, nx, ny, rows, jit, stim=stim, gj_pairs=M.PKJ_GJ_PAIRS, pkj_gj=True, canon=True)
+    assert s.init() == 0
+    eng = G.Engine(G.FP64)
+    sid = eng.add_system(M.PKJ, nx, ny, rows, jit, stim=stim, gj_pairs=M.PKJ_GJ_PAIRS, gap=True)
+    eng.build()
+    layout = eng.launch_layout()
+    t = 0.0
+    for chunk in (1, n_iv - 1):
+        eng.advance(t, chunk)
+        for _ in range(chunk):
+            assert s.advance(t) == 0
+            t += G.H_MAX
+        np.testing.assert_array_equal(eng.vnew(sid), s.vnew())
+        np.testing.assert_array_equal(eng.read(sid, G.F_CA), s.ca())
+        ctl_g, st_g, status = eng.ctl(sid)
+        assert status == 0
+        for k, v in s.stats().items():
+            assert st_g[k] == v, (k, st_g[k], v)
+    eng.close()
+    return layout
+
+
+def test_largest_cluster_system(oracle):
+    # 6 x 6 cells of 1592 compartments = 57 312 <= 16 CTAs x 14 rows x 256
+    persistent, ctas = _pkj_grid(oracle, 6, 6, 1592, 4)
+    print("layout", persistent, ctas)
+    # the 16-CTA cluster; where the device cannot co-schedule 16 CTAs of
+    # 197 KB, one CTA of the persistent launch with the workspace in HBM
+    assert persistent or ctas[M.PKJ] == 16, (persistent, ctas)
+
+
+def test_system_beyond_cluster_capacity(oracle):
+    # 6 x 6 cells of 1600 compartments = 57 600: no cluster holds the
+    # workspace, so one CTA integrates it with the workspace in HBM
+    persistent, ctas = _pkj_grid(oracle, 6, 6, 1600, 3)
+    assert persistent and ctas[M.PKJ] >= 1, (persistent, ctas)
