@@ -51,10 +51,16 @@ struct TypeRun {
   double *vh = nullptr, *raster = nullptr;
 };
 
-void gr_update(TypeRun &r) { gr_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr, nullptr); }
-void go_update(TypeRun &r) { go_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr); }
-void pkj_update(TypeRun &r) { pkj_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr, nullptr); }
-void io_update(TypeRun &r) { io_solve_update_v(r.d, r.ds, r.p, r.ps, nullptr); }
+// the coupling objects, passed to every update call as main.cu:201-285 does
+struct Coupling {
+  synapse_t *mfgr = nullptr, *gogr = nullptr, *grgo = nullptr, *grpkj = nullptr, *mlipkj = nullptr;
+  gap_t *io_gap = nullptr;
+} g_cpl;
+
+void gr_update(TypeRun &r) { gr_solve_update_v(r.d, r.ds, r.p, r.ps, g_cpl.mfgr, g_cpl.gogr); }
+void go_update(TypeRun &r) { go_solve_update_v(r.d, r.ds, r.p, r.ps, g_cpl.grgo); }
+void pkj_update(TypeRun &r) { pkj_solve_update_v(r.d, r.ds, r.p, r.ps, g_cpl.grpkj, g_cpl.mlipkj); }
+void io_update(TypeRun &r) { io_solve_update_v(r.d, r.ds, r.p, r.ps, g_cpl.io_gap); }
 
 // One batch of recorded output of one type, written by the writer thread in
 // the order the batches were queued.
@@ -177,6 +183,7 @@ int main(int argc, char **argv) {
   synapse_t *grpkj = grpkj_create(runs[0].p->nx, runs[0].p->ny, runs[2].p->nx, runs[2].p->ny);
   synapse_t *mlipkj = mlipkj_create(runs[2].p->n, runs[0].p->n);
   gap_t *io_gap = io_gap_create(nx[3], ny[3]);
+  g_cpl = Coupling{mfgr, gogr, grgo, grpkj, mlipkj, io_gap};
   FILE *dbg = fopen("debug_file.csv", "w");
   if (dbg) fclose(dbg);
 

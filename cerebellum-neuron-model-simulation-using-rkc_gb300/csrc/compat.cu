@@ -586,17 +586,14 @@ neuron_solve_t *io_solve_initialize(neuron_solve_t *ps, const char *type, neuron
   return solve_initialize(GBRKC_IO, ps, type, p);
 }
 
-void gr_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *mfgr, synapse_t *gogr) {
-  if (mfgr || gogr) die("gr: network mode is not provided");
+// main.cu passes its coupling objects on every call, network_sim or not
+// (main.cu:201, 227, 259, 285).  Their synaptic values stay 0 -- and the
+// blocks independent -- until the first X_synapse_update starts network mode.
+void gr_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *, synapse_t *) {
   update_v(GBRKC_GR);
 }
-void go_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *grgo) {
-  if (grgo) die("go: network mode is not provided");
-  update_v(GBRKC_GO);
-}
-void pkj_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *grpkj,
-                        synapse_t *mlipkj) {
-  if (grpkj || mlipkj) die("pkj: network mode is not provided");
+void go_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *) { update_v(GBRKC_GO); }
+void pkj_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *, synapse_t *) {
   update_v(GBRKC_PKJ);
 }
 void io_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, gap_t *) { update_v(GBRKC_IO); }
