@@ -40,17 +40,25 @@ H_MAX = 0.125
 ALG_BYTES = {"mixed": 56, "fp64": 68}   # algorithmic bytes per compartment-update
 
 
+# Arm CPU part numbers (/proc/cpuinfo "CPU part", implementer 0x41)
+_ARM_PARTS = {"0xd40": "Neoverse-V1", "0xd49": "Neoverse-N2", "0xd4f": "Neoverse-V2", "0xd84": "Neoverse-V3",
+              "0xd0c": "Neoverse-N1"}
+
+
 def cpu_model():
     """The host CPU's model name (for the CPU baseline's record)."""
+    import platform
     try:
         with open("/proc/cpuinfo", errors="replace") as f:
             for line in f:
                 k, _, v = line.partition(":")
-                if k.strip() in ("model name", "Model", "CPU part") and v.strip():
-                    return v.strip()
+                k, v = k.strip(), v.strip()
+                if k in ("model name", "Model") and v:
+                    return v
+                if k == "CPU part" and v:
+                    return f"{_ARM_PARTS.get(v.lower(), 'Arm part ' + v)} ({platform.machine()})"
     except Exception:
         pass
-    import platform
     return platform.machine()
 
 
