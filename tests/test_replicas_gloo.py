@@ -59,3 +59,11 @@ def test_reference_arm_runs_on_rank_zero_only():
                   "--config", "pkj3x3"])
     assert '"impl": "reference"' in out[0]
     assert out[1].strip() == ""
+    import json
+    line = json.loads(out[0].strip().splitlines()[-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["n_gpus"] == 2 and line["steps"] == 1 and line["warmup"] == 3 and line["value"] > 0
+    assert line["config"]["workload"] and line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
