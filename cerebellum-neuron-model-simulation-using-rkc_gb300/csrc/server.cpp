@@ -250,6 +250,40 @@ extern "C" int gbrkc_server_add_class(gbrkc_server *S, const gbrkc_slot_class *c
   return 0;
 }
 
+namespace {
+
+// The arenas' systems in the server's engine (idle until a request fills
+// them), the engine built, and the raster log sized for `cells` cells.
+int fill_arenas(gbrkc_server *S, long long cells) {
+  int rc = 0;
+  for (auto &C : S->classes) {
+    std::vector<double> jit(C->cells, 0.0);
+    gbrkc_system_desc d = C->shape;
+    d.jitter = jit.data();
+    for (int k = 0; k < C->slots; k++) {
+      int id = -1;
+      rc = gbrkc_add_system(S->e, &d, &id);
+      if (rc) return srv_fail(rc, "arena: %s", gbrkc_last_error());
+      if (k == 0) C->first_id = id;
+    }
+    C->arena = gbrkc::serve::SlotArena(C->slots);
+    C->owner.assign(C->slots, -1);
+    C->rank.assign(C->slots, -1);
+  }
+  rc = gbrkc_build(S->e);
+  if (rc) return srv_fail(rc, "build: %s", gbrkc_last_error());
+  // a cell crosses upward at most every other interval
+  S->spike_cap = (long)std::min<long long>(cells * ((S->quantum + 1) / 2 + 1), 1 << 24);
+  rc = gbrkc_record_spikes(S->e, S->spike_cap);
+  if (rc) return srv_fail(rc, "raster: %s", gbrkc_last_error());
+  S->spk_t.resize(S->spike_cap);
+  S->spk_sys.resize(S->spike_cap);
+  S->spk_cell.resize(S->spike_cap);
+  return 0;
+}
+
+}  // namespace
+
 extern "C" int gbrkc_server_start(gbrkc_server *S) {
   if (!S) return srv_fail(GBRKC_EINVAL, "null server");
   if (S->started) return srv_fail(GBRKC_ESTATE, "server already started");
@@ -281,29 +315,14 @@ extern "C" int gbrkc_server_start(gbrkc_server *S) {
   S->reserved = total;
   int rc = gbrkc_engine_create(S->precision, &S->e);
   if (rc) return srv_fail(rc, "engine: %s", gbrkc_last_error());
-  for (auto &C : S->classes) {
-    std::vector<double> jit(C->cells, 0.0);
-    C->shape.jitter = jit.data();
-    for (int k = 0; k < C->slots; k++) {
-      int id = -1;
-      rc = gbrkc_add_system(S->e, &C->shape, &id);
-      if (rc) return srv_fail(rc, "arena: %s", gbrkc_last_error());
-      if (k == 0) C->first_id = id;
-    }
-    C->shape.jitter = nullptr;
-    C->arena = gbrkc::serve::SlotArena(C->slots);
-    C->owner.assign(C->slots, -1);
-    C->rank.assign(C->slots, -1);
+  rc = fill_arenas(S, cells);
+  if (rc) {
+    // back to the state before the call, so that start can be retried
+    gbrkc_engine_destroy(S->e);
+    S->e = nullptr;
+    S->reserved = 0;
+    return rc;
   }
-  rc = gbrkc_build(S->e);
-  if (rc) return srv_fail(rc, "build: %s", gbrkc_last_error());
-  // a cell crosses upward at most every other interval
-  S->spike_cap = (long)std::min<long long>(cells * ((S->quantum + 1) / 2 + 1), 1 << 24);
-  rc = gbrkc_record_spikes(S->e, S->spike_cap);
-  if (rc) return srv_fail(rc, "raster: %s", gbrkc_last_error());
-  S->spk_t.resize(S->spike_cap);
-  S->spk_sys.resize(S->spike_cap);
-  S->spk_cell.resize(S->spike_cap);
   S->started = true;
   return 0;
 }
