@@ -2,9 +2,9 @@
 //
 //   gbrkc_main S_gr gx gy S_go ox oy S_pkj px py S_io ix iy [TS_ms [batch [network]]]
 //
-// S is the solver name per type, matched on its first three letters as the
-// reference does (main.cu:60-102); only RKC is provided.  A type with
-// nx * ny == 0 is skipped.  Each 0.125 ms interval: the type's stimulus
+// S is the solver name per type, matched on its first letters as the
+// reference does (main.cu:60-102); only RKC is provided, and BE or CN is
+// accepted for a type with nx * ny == 0, which is skipped.  Each 0.125 ms interval: the type's stimulus
 // protocol, one advance, the voltages copied back, one CSV row written; the
 // files are the reference's: <type>_v_by_RKC.csv, <type>_raster_by_RKC.csv,
 // comptime.csv (appended) and an empty debug_file.csv.  The jitter stream is
@@ -152,14 +152,24 @@ int main(int argc, char **argv) {
     runs[k].solver[GBRKC_MAX_BUF - 1] = 0;
     nx[k] = atoi(argv[2 + 3 * k]);
     ny[k] = atoi(argv[3 + 3 * k]);
-    if (strncmp(runs[k].solver, "RKC", 3) != 0) {
-      printf("Error!! -> set solver name in argv [ %d ] (only RKC is provided)\n", 1 + 3 * k);
+    // BE, CN or RKC, matched on the first letters (main.cu:60-102); the
+    // reference's scripts name BE or CN for the types they leave empty
+    const char *tag = !strncmp(runs[k].solver, "BE", 2)    ? "BE"
+                      : !strncmp(runs[k].solver, "CN", 2)  ? "CN"
+                      : !strncmp(runs[k].solver, "RKC", 3) ? "RKC"
+                                                           : nullptr;
+    if (!tag) {
+      printf("Error!! -> set solver name in argv [ %d ]\n", 1 + 3 * k);
       return 0;
     }
+    if (strcmp(tag, "RKC") != 0 && nx[k] * ny[k] > 0) {
+      printf("%s: solver %s is not provided (only RKC)\n", runs[k].name, runs[k].solver);
+      return 1;
+    }
     char name[64];
-    snprintf(name, sizeof name, "%s_v_by_RKC.csv", runs[k].name);
+    snprintf(name, sizeof name, "%s_v_by_%s.csv", runs[k].name, tag);
     runs[k].fv = fopen(name, "w");
-    snprintf(name, sizeof name, "%s_raster_by_RKC.csv", runs[k].name);
+    snprintf(name, sizeof name, "%s_raster_by_%s.csv", runs[k].name, tag);
     runs[k].fr = fopen(name, "w");
     if (!runs[k].fv || !runs[k].fr) {
       printf("cannot open the output files of %s\n", runs[k].name);

@@ -126,16 +126,32 @@ std::vector<double> draw_jitter(int type, int n) {
 
 __device__ int d_stim_comp[NTYPES];
 
+// kBE, kCN or kRKC from a solver name, matched on its first letters as
+// main.cu:60-102 does; -1 for anything else
+int solver_kind(const char *solver) {
+  if (!strncmp(solver, "BE", 2)) return kBE;
+  if (!strncmp(solver, "CN", 2)) return kCN;
+  if (!strncmp(solver, "RKC", 3)) return kRKC;
+  return -1;
+}
+
+// Only RKC is provided.  A block without cells runs no solver, so BE and CN
+// are accepted there (the reference's run scripts name them for the types
+// they leave empty).
+void check_solver(int type, const char *solver, int n) {
+  const int kind = solver_kind(solver);
+  if (kind == kRKC || (kind >= 0 && n <= 0)) return;
+  printf("%s: solver %s is not provided (only RKC)\n", TYPE_NAME[type], solver);
+  exit(1);
+}
+
 neuron_t *initialize(int type, int nx, int ny, const char *solver, neuron_t *p) {
-  if (strncmp(solver, "RKC", 3) != 0) {
-    printf("%s: solver %s is not provided (only RKC)\n", TYPE_NAME[type], solver);
-    exit(1);
-  }
+  const int n = nx * ny;
+  check_solver(type, solver, n);
   Block &B = g_block[type];
   if (B.eng) die("block initialised twice");
-  const int n = nx * ny;
   memset(p, 0, sizeof *p);
-  p->n_solver = kRKC;
+  p->n_solver = solver_kind(solver);
   p->neuron_type = type;
   p->n = n;
   p->nx = nx;
@@ -195,10 +211,7 @@ neuron_t *initialize(int type, int nx, int ny, const char *solver, neuron_t *p) 
 
 neuron_solve_t *solve_initialize(int type, neuron_solve_t *ps, const char *solver, neuron_t *p) {
   Block &B = g_block[type];
-  if (strncmp(solver, "RKC", 3) != 0) {
-    printf("%s: solver %s is not provided (only RKC)\n", TYPE_NAME[type], solver);
-    exit(1);
-  }
+  check_solver(type, solver, p->n);
   memset(ps, 0, sizeof *ps);
   strncpy(ps->type, solver, GBRKC_MAX_BUF - 1);
   B.h_vec = (double **)calloc(n_vec_RKC, sizeof(double *));

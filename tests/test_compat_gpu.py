@@ -84,6 +84,32 @@ def test_go_pkj_blocks_match_oracle(tmp_path, oracle):
             np.testing.assert_allclose(v[k, 1:], ref, atol=1.5e-6, rtol=0, err_msg=f"{name} interval {k}")
 
 
+def test_reference_script_solver_names(tmp_path):
+    """The reference's run scripts name CN or BE for the types they leave
+    empty (`./main CN 0 0 RKC 1 1 CN 0 0 CN 0 0`): accepted, their files are
+    opened under those names and stay empty, and the RKC block writes the
+    same bytes as with RKC everywhere."""
+    files = {"Go_131.txt": M.write_rows(M.go_synthetic(3), M.GO)}
+    out = {}
+    for tag, names in (("mixed", ("CN", "RKC", "CN", "BE")), ("rkc", ("RKC",) * 4)):
+        d = tmp_path / tag
+        d.mkdir()
+        for name, text in files.items():
+            (d / name).write_text(text)
+        args = [CLI]
+        for s, (nx, ny) in zip(names, [(0, 0), (1, 1), (0, 0), (0, 0)]):
+            args += [s, str(nx), str(ny)]
+        args.append("2.0")
+        r = subprocess.run(args, cwd=d, env=dict(os.environ, GBRKC_MODEL_DIR=str(d)), capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0, r.stdout + r.stderr
+        out[tag] = (d / "go_v_by_RKC.csv").read_bytes()
+        if tag == "mixed":
+            for f in ("gr_v_by_CN.csv", "pkj_raster_by_CN.csv", "io_v_by_BE.csv"):
+                assert (d / f).exists() and (d / f).stat().st_size == 0, f
+    assert out["mixed"] == out["rkc"] and out["rkc"].count(b"\n") == 16
+
+
 def test_batched_cli_writes_identical_files(tmp_path):
     """gbrkc_main with batch > 1 (several intervals per launch, voltage
     record and raster on the device, CSV from a writer thread) writes the
