@@ -317,6 +317,8 @@ struct _gap_t {
 
 struct _synapse_t {
   int kind;
+  int n;        // synapses of the family where the constructor knows them (mfgr, mlipkj), else its pair count
+  FILE *f_out;  // MF_RASTER.csv / MLI_RASTER.csv (syn.cu:76, 726), or NULL
 };
 
 namespace {
@@ -342,14 +344,47 @@ struct Net {
   int sid[NTYPES] = {-1, -1, -1, -1};
   double t = 0.0;  // start of the shared engine's next interval
   int refs = 0;
+  // mossy-fibre states as of the last synapse update before the current
+  // interval, for mf_output_file (the engine's own states are one update
+  // ahead once the interval has run); kept while MF_RASTER.csv is open
+  int mf_watch = 0;  // synapses of the open MF_RASTER.csv
+  std::vector<double> mf_ampa, mf_nmda;
 } g_net;
 
-synapse_t *net_create(int kind, int) {
+synapse_t *net_create(int kind, int n, const char *raster) {
   g_net.made[kind] = true;
-  // the reference seeds its cuRAND streams with rand() here (syn.cu:82, 611)
-  if (kind == SYN_K_MFGR) g_net.seed_mf = (unsigned long long)rand();
-  if (kind == SYN_K_GRPKJ) g_net.seed_pk = (unsigned long long)rand();
-  return new _synapse_t{kind};
+  _synapse_t *s = new _synapse_t{kind, n, nullptr};
+  if (n > 0 && raster) {
+    s->f_out = fopen(raster, "w");
+    if (!s->f_out) die("cannot open a synapse raster file");
+    if (kind == SYN_K_MFGR) g_net.mf_watch = n;
+  }
+  // a non-empty random family seeds its cuRAND states with rand() here
+  // (syn.cu:82, 623, 755)
+  if (n > 0 && (kind == SYN_K_MFGR || kind == SYN_K_GRPKJ || kind == SYN_K_MLIPKJ)) {
+    const unsigned long long r = (unsigned long long)rand();
+    if (kind == SYN_K_MFGR) g_net.seed_mf = r;
+    if (kind == SYN_K_GRPKJ) g_net.seed_pk = r;
+  }
+  return s;
+}
+
+void syn_free(synapse_t *s) {
+  if (!s) return;
+  if (s->f_out) fclose(s->f_out);
+  if (s->kind == SYN_K_MFGR && s->f_out) g_net.mf_watch = 0;
+  delete s;
+}
+
+// the mossy-fibre synapses are the shared engine's first (network_on adds
+// them first): copy their states before the next update
+void snapshot_mf() {
+  const int n = g_net.mf_watch;
+  if (n <= 0 || !g_net.made[SYN_K_MFGR] || g_block[GBRKC_GR].n * 4 != n) return;
+  g_net.mf_ampa.resize(n);
+  g_net.mf_nmda.resize(n);
+  check(gbrkc_read_synapses(g_net.eng, GBRKC_SYNF_S0, g_net.mf_ampa.data(), n), "mossy-fibre states");
+  check(gbrkc_read_synapses(g_net.eng, GBRKC_SYNF_S1, g_net.mf_nmda.data(), n), "mossy-fibre states");
 }
 
 // the reference's wiring (syn.cu:146-262, 295-410, 455-619) on the blocks'
@@ -543,6 +578,7 @@ void network_on() {
 
 void network_advance(Block &B) {
   if (B.t >= g_net.t) {
+    snapshot_mf();
     const int rc = gbrkc_advance(g_net.eng, g_net.t, 1);
     if (rc != 0) {
       printf("network: %s\n", gbrkc_last_error());
@@ -641,22 +677,55 @@ void io_solve_finalize(const int, neuron_solve_t *, neuron_solve_t *ps) { solve_
 // The coupling objects only record which synapse families the caller asked
 // for (and, like the reference, take a rand() seed for the random ones); the
 // network is wired and built on the first X_synapse_update call.
-synapse_t *mfgr_create(const int n) { return net_create(SYN_K_MFGR, n); }
+// Four mossy fibres per granule cell and N_Syn_Per_MLIPKJ = 1 MLI synapse
+// per Purkinje cell (syn.cu:66, 709; syn.cuh:52); those two families open
+// their raster files when they have synapses (syn.cu:76, 726).
+synapse_t *mfgr_create(const int n) { return net_create(SYN_K_MFGR, 4 * n, "MF_RASTER.csv"); }
 synapse_t *gogr_create(const int go_x, const int go_y, const int gr_x, const int gr_y) {
-  return net_create(SYN_K_GOGR, go_x * go_y * gr_x * gr_y);
+  return net_create(SYN_K_GOGR, go_x * go_y * gr_x * gr_y, nullptr);
 }
 synapse_t *grgo_create(const int gr_x, const int gr_y, const int go_x, const int go_y) {
-  return net_create(SYN_K_GRGO, go_x * go_y * gr_x * gr_y);
+  return net_create(SYN_K_GRGO, go_x * go_y * gr_x * gr_y, nullptr);
 }
 synapse_t *grpkj_create(const int gr_x, const int gr_y, const int pkj_x, const int pkj_y) {
-  return net_create(SYN_K_GRPKJ, gr_x * gr_y * pkj_x * pkj_y);
+  return net_create(SYN_K_GRPKJ, gr_x * gr_y * pkj_x * pkj_y, nullptr);
 }
-synapse_t *mlipkj_create(const int n_pkj, const int n_gr) { return net_create(SYN_K_MLIPKJ, n_pkj * n_gr); }
-void mfgr_finalize(synapse_t *s, const int) { delete s; }
-void gogr_finalize(synapse_t *s, const int) { delete s; }
-void grgo_finalize(synapse_t *s, const int) { delete s; }
-void grpkj_finalize(synapse_t *s, const int) { delete s; }
-void mlipkj_finalize(synapse_t *s, const int) { delete s; }
+synapse_t *mlipkj_create(const int n_pkj, const int n_gr) {
+  return net_create(SYN_K_MLIPKJ, (n_pkj == 0 || n_gr == 0) ? 0 : n_pkj, "MLI_RASTER.csv");
+}
+void mfgr_finalize(synapse_t *s, const int) { syn_free(s); }
+void gogr_finalize(synapse_t *s, const int) { syn_free(s); }
+void grgo_finalize(synapse_t *s, const int) { syn_free(s); }
+void grpkj_finalize(synapse_t *s, const int) { syn_free(s); }
+void mlipkj_finalize(synapse_t *s, const int) { syn_free(s); }
+
+// syn.cu:114-127: the time, then each mossy fibre's conductance
+// (G_MFGR_AMPA 0.88 ampa + G_MFGR_NMDA 0.12 nmda) x weight x 1e6, in the
+// reference's synapse order (granule cell i, fibre j at 4 i + j).  Before
+// network mode the states are 0, as the reference's are without updates.
+void mf_output_file(synapse_t *s, const double t, neuron_t *) {
+  if (!s || !s->f_out) return;
+  constexpr double G_MFGR_AMPA = 0.18e-9, G_MFGR_NMDA = 0.025e-9, W_MFGR = 40000.0;  // syn.cuh:13-14, 54
+  const bool live = g_net.on && (int)g_net.mf_ampa.size() == s->n;
+  fprintf(s->f_out, "%lf,", t);
+  for (int j = 0; j < s->n; j++) {
+    const double ampa = live ? g_net.mf_ampa[j] : 0.0, nmda = live ? g_net.mf_nmda[j] : 0.0;
+    double val = G_MFGR_AMPA * 0.88 * ampa + G_MFGR_NMDA * 0.12 * nmda;
+    val *= W_MFGR / 4.0 * 1000000;
+    fprintf(s->f_out, "%lf,", val);
+  }
+  fprintf(s->f_out, "\n");
+}
+
+// syn.cu:804-817: the time, then each MLI synapse's G_MLIPKJ_GABA x gaba x
+// weight x 1e6.  On the RKC path these synapses are never updated
+// (syn.cu:912-916) and W_MLIPKJ is 0 (syn.cuh:59): every value is 0.
+void mli_output_file(synapse_t *s, const double t, neuron_t *) {
+  if (!s || !s->f_out) return;
+  fprintf(s->f_out, "%lf,", t);
+  for (int j = 0; j < s->n; j++) fprintf(s->f_out, "%lf,", 0.0);
+  fprintf(s->f_out, "\n");
+}
 void gr_synapse_update(const double, const double, synapse_t *, synapse_t *, neuron_t *, neuron_solve_t *) {
   network_on();
 }

@@ -177,6 +177,16 @@ void gogr_finalize(synapse_t *s, const int n);
 void grgo_finalize(synapse_t *s, const int n);
 void grpkj_finalize(synapse_t *s, const int n);
 void mlipkj_finalize(synapse_t *s, const int n);
+/* mfgr_create (with granule cells) and mlipkj_create (with granule and
+ * Purkinje cells) open MF_RASTER.csv and MLI_RASTER.csv, as syn.cu:76, 726
+ * do.  These append one row to them: the time, then one "%lf," conductance
+ * per synapse in the reference's order (syn.cu:114, 804; main.cu:215 has
+ * the first call, commented out).  Mossy-fibre values are 0 until network
+ * mode starts, then the states of the last synapse update before the
+ * current interval.  MLI synapses are never updated on the RKC path, so
+ * their values are 0. */
+void mf_output_file(synapse_t *mfgr, const double t, neuron_t *p_gr);
+void mli_output_file(synapse_t *mlipkj, const double t, neuron_t *p_pkj);
 void gr_synapse_update(const double t, const double DT, synapse_t *mfgr, synapse_t *gogr, neuron_t *d_go,
                        neuron_solve_t *p_gr_solve);
 void go_synapse_update(const double t, const double DT, synapse_t *grgo, neuron_t *d_gr, neuron_solve_t *p_go_solve);

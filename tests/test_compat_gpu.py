@@ -161,6 +161,8 @@ def test_network_mode_dropin_matches_native(tmp_path, oracle):
     r = subprocess.run(args, cwd=tmp_path, env=dict(os.environ, GBRKC_MODEL_DIR=str(tmp_path)), capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
+    # the constructors open the synapse rasters (syn.cu:76, 726); main.cu writes no rows to them
+    assert (tmp_path / "MF_RASTER.csv").read_text() == "" and (tmp_path / "MLI_RASTER.csv").read_text() == ""
     # the same run through the native ABI
     O.libc_srand(0)
     jit = {t: O.draw_jitter(t, n) for t, n in ((M.GR, 4), (M.GO, 1), (M.PKJ, 1))}

@@ -1,0 +1,75 @@
+"""The drop-in's coupling-object constructors and synapse raster writers on
+the CPU (they make no device call before network mode starts): the files
+syn.cu's constructors open, the rows mf_output_file / mli_output_file write
+(all values 0 without network mode), and rand() drawn only by non-empty
+random families, as the reference's constructors draw their cuRAND seeds."""
+import ctypes as C
+import os
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "cerebellum-neuron-model-simulation-using-rkc_gb300")
+LIB = os.path.join(PKG, "libgbrkc.so")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(LIB):
+        import build as B
+        B.build()
+    L = C.CDLL(LIB)
+    P = C.c_void_p
+    L.mfgr_create.restype = P
+    L.mfgr_create.argtypes = [C.c_int]
+    L.mlipkj_create.restype = P
+    L.mlipkj_create.argtypes = [C.c_int, C.c_int]
+    L.grpkj_create.restype = P
+    L.grpkj_create.argtypes = [C.c_int] * 4
+    for f in ("mfgr_finalize", "mlipkj_finalize", "grpkj_finalize"):
+        getattr(L, f).argtypes = [P, C.c_int]
+    for f in ("mf_output_file", "mli_output_file"):
+        getattr(L, f).argtypes = [P, C.c_double, P]
+    return L
+
+
+def test_raster_files_and_rows(lib, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    mf = lib.mfgr_create(3)                      # 3 granule cells: 12 fibres
+    mli = lib.mlipkj_create(2, 3)                # 2 Purkinje cells: 2 MLI synapses
+    assert (tmp_path / "MF_RASTER.csv").exists() and (tmp_path / "MLI_RASTER.csv").exists()
+    for t in (0.125, 0.25):
+        lib.mf_output_file(mf, t, None)
+        lib.mli_output_file(mli, t, None)
+    lib.mfgr_finalize(mf, 3)
+    lib.mlipkj_finalize(mli, 6)
+    mf_rows = (tmp_path / "MF_RASTER.csv").read_text().splitlines()
+    assert mf_rows == ["0.125000," + "0.000000," * 12, "0.250000," + "0.000000," * 12]
+    mli_rows = (tmp_path / "MLI_RASTER.csv").read_text().splitlines()
+    assert mli_rows == ["0.125000," + "0.000000," * 2, "0.250000," + "0.000000," * 2]
+
+
+def test_empty_families_open_no_file(lib, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    mf = lib.mfgr_create(0)
+    mli = lib.mlipkj_create(4, 0)                # no granule cells: no MLI synapses
+    lib.mf_output_file(mf, 0.125, None)          # nothing to write to
+    lib.mfgr_finalize(mf, 0)
+    lib.mlipkj_finalize(mli, 0)
+    assert not (tmp_path / "MF_RASTER.csv").exists() and not (tmp_path / "MLI_RASTER.csv").exists()
+
+
+def test_rand_drawn_by_non_empty_random_families(lib, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    libc = C.CDLL(None)
+    libc.srand(7)
+    seq = [libc.rand() for _ in range(5)]
+    libc.srand(7)
+    objs = [(lib.mfgr_create(0), lib.mfgr_finalize), (lib.grpkj_create(2, 2, 0, 0), lib.grpkj_finalize),
+            (lib.mlipkj_create(0, 4), lib.mlipkj_finalize)]
+    assert libc.rand() == seq[0]                 # empty families draw nothing
+    objs += [(lib.mfgr_create(2), lib.mfgr_finalize), (lib.grpkj_create(2, 2, 1, 1), lib.grpkj_finalize),
+             (lib.mlipkj_create(1, 4), lib.mlipkj_finalize)]
+    assert libc.rand() == seq[4]                 # one draw each (syn.cu:82, 623, 755)
+    for o, fin in objs:
+        fin(o, 0)
