@@ -646,6 +646,14 @@ void pkj_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t
   update_v(GBRKC_PKJ);
 }
 void io_solve_update_v(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, gap_t *) { update_v(GBRKC_IO); }
+void gr_solve_by_rkc(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *, synapse_t *) {
+  update_v(GBRKC_GR);
+}
+void go_solve_by_rkc(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *) { update_v(GBRKC_GO); }
+void pkj_solve_by_rkc(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, synapse_t *, synapse_t *) {
+  update_v(GBRKC_PKJ);
+}
+void io_solve_by_rkc(neuron_t *, neuron_solve_t *, neuron_t *, neuron_solve_t *, gap_t *) { update_v(GBRKC_IO); }
 
 void gr_set_current_launch(neuron_t *d, const double t) { launch_stim(GBRKC_GR, d, t); }
 void go_set_current_launch(neuron_t *d, const double t) { launch_stim(GBRKC_GO, d, t); }
@@ -765,6 +773,56 @@ void output_time2(const int n_gr, const char *type1, const int n_go, const char 
   fprintf(f, "Gr,%d,%s,Go,%d,%s,Pkj,%d,%s,Io,%d,%s,AllCompTime,%lf,0.5s-endCompTime,%lf,SimTime,%d\n", n_gr, type1,
           n_go, type2, n_pkj, type3, n_io, type4, comp_time, comp_time_half, sim_time);
   fclose(f);
+}
+
+void raster_plot(const int n_go, const char *type) {
+  if (n_go <= 0) return;
+  // the reference's solver names and file names (output.cu:40-45)
+  static const struct {
+    const char *name;
+    size_t len;
+    const char *in, *out;
+  } kFiles[] = {{"BACKWARD_EULER", 14, "go_v_by_BEm.csv", "go_raster_by_BEm.csv"},
+                {"CRANK_NICOLSON", 14, "go_v_by_CNm.csv", "go_raster_by_CNm.csv"},
+                {"FORWARD_EULER", 13, "go_v_by_FEm.csv", "go_raster_by_FEm.csv"},
+                {"RUNGE_KUTTA_4", 13, "go_v_by_RK4m.csv", "go_raster_by_RK4.csv"},
+                {"RKC", 3, "go_v_by_RKC.csv", "go_raster_by_RKC.csv"}};
+  const char *in = nullptr, *out = nullptr;
+  for (const auto &f : kFiles)
+    if (!strncmp(type, f.name, f.len)) {
+      in = f.in;
+      out = f.out;
+      break;
+    }
+  if (!in) {
+    printf("go_initialization_error \n");
+    exit(1);
+  }
+  FILE *fp = fopen(in, "r");
+  FILE *fw = fopen(out, "w");
+  if (!fp || !fw) die("raster_plot: cannot open the Golgi voltage or raster file");
+  std::vector<double> v(n_go, -70.0), old_v(n_go, -70.0);
+  printf("Debug for output \n");
+  double t;
+  while (fscanf(fp, "%lf,", &t) == 1) {
+    fprintf(fw, "%lf,", t);
+    for (int i = 0; i < n_go; i++) {
+      if (fscanf(fp, "%lf,", &v[i]) != 1) {
+        printf("raster_FILE_ERROR2\n");
+        exit(1);
+      }
+      if (v[i] > 0.0 && old_v[i] < 0.0) {
+        fprintf(fw, "%d,", i);
+        printf("%d,", i);
+      } else {
+        fprintf(fw, ",");
+      }
+      old_v[i] = v[i];
+    }
+    fprintf(fw, "\n");
+  }
+  fclose(fp);
+  fclose(fw);
 }
 
 }  // extern "C"

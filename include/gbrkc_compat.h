@@ -108,6 +108,15 @@ void pkj_solve_update_v(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuro
                         synapse_t *grpkj, synapse_t *mlipkj);
 void io_solve_update_v(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron_solve_t *p_solve, gap_t *io_gap);
 
+/* The RKC drivers X_solve_update_v runs for an RKC block (solve_rkc.cuh:23-26,
+ * solve_rkc.cu:1122-1362): the same one-interval advance. */
+void gr_solve_by_rkc(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron_solve_t *p_solve, synapse_t *mfgr,
+                     synapse_t *gogr);
+void go_solve_by_rkc(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron_solve_t *p_solve, synapse_t *grgo);
+void pkj_solve_by_rkc(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron_solve_t *p_solve, synapse_t *grpkj,
+                      synapse_t *mlipkj);
+void io_solve_by_rkc(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron_solve_t *p_solve, gap_t *io_gap);
+
 /* The reference's stimulus protocols, as kernels over the device neuron_t
  * (launch <<<n / 128 + 1, 128>>> on the default stream, as main.cu does) and
  * as host launchers for callers without a CUDA compiler.  GrC: 0.01 nA at the
@@ -216,6 +225,17 @@ void output_time(const int n_gr, const char *type1, const int n_go, const char *
 void output_time2(const int n_gr, const char *type1, const int n_go, const char *type2, const int n_pkj,
                   const char *type3, const int n_io, const char *type4, const double comp_time,
                   const double comp_time_half, const int sim_time);
+
+/* Golgi raster from the voltage file after a run (output.cu:38-81; its call
+ * in main.cu is commented out): reads go_v_by_<S>.csv and writes
+ * go_raster_by_<S>.csv as one row per interval, "t," then for each cell
+ * "i," where its voltage crossed 0 mV upward (from -70 mV before the first
+ * row) and "," otherwise.  S is picked from type by the reference's names
+ * (BACKWARD_EULER, CRANK_NICOLSON, FORWARD_EULER, RUNGE_KUTTA_4 or RKC);
+ * another name stops with the reference's message.  The reference's read
+ * loop ends every file with "raster_FILE_ERROR1" and exit(1); this one
+ * returns at the end of the file. */
+void raster_plot(const int n_go, const char *type);
 
 #ifdef __cplusplus
 }
