@@ -43,6 +43,19 @@ static int fail(int code, const char *fmt, ...) {
   return code;
 }
 
+// A C entry point lets no C++ exception out: host allocations sized by the
+// caller (dense templates, recorders, logs) report GBRKC_ENOMEM instead.
+template <class F>
+static int no_throw(F &&f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc &) {
+    return fail(GBRKC_ENOMEM, "host memory exhausted");
+  } catch (const std::exception &x) {
+    return fail(GBRKC_EINVAL, "%s", x.what());
+  }
+}
+
 #define CUDA_TRY(x)                                                                     \
   do {                                                                                  \
     cudaError_t e_ = (x);                                                               \
@@ -495,7 +508,7 @@ extern "C" int gbrkc_engine_create(int precision, gbrkc_engine **out) {
 
 extern "C" void gbrkc_engine_destroy(gbrkc_engine *e) { delete e; }
 
-extern "C" int gbrkc_add_system(gbrkc_engine *E, const gbrkc_system_desc *d, int *sys_id) {
+static int add_system_impl(gbrkc_engine *E, const gbrkc_system_desc *d, int *sys_id) {
   if (!E || !d || !d->rows || !d->jitter) return fail(GBRKC_EINVAL, "null argument");
   if (E->built) return fail(GBRKC_ESTATE, "engine already built");
   if (d->cell_type < 0 || d->cell_type >= NTYPES || d->nx <= 0 || d->ny <= 0 || d->ncomp <= 0)
@@ -577,6 +590,10 @@ extern "C" int gbrkc_add_system(gbrkc_engine *E, const gbrkc_system_desc *d, int
   E->systems.push_back(std::move(S));
   if (sys_id) *sys_id = (int)E->systems.size() - 1;
   return 0;
+}
+
+extern "C" int gbrkc_add_system(gbrkc_engine *E, const gbrkc_system_desc *d, int *sys_id) {
+  return no_throw([&] { return add_system_impl(E, d, sys_id); });
 }
 
 namespace {
@@ -1300,7 +1317,7 @@ int build_synapses(gbrkc_engine *E) {
 
 }  // namespace
 
-extern "C" int gbrkc_add_synapses(gbrkc_engine *E, const gbrkc_synapse_desc *d, int *first_id) {
+static int add_synapses_impl(gbrkc_engine *E, const gbrkc_synapse_desc *d, int *first_id) {
   if (!E || !d) return fail(GBRKC_EINVAL, "null argument");
   if (E->built) return fail(GBRKC_ESTATE, "synapses must be added before gbrkc_build");
   if (d->kind < 0 || d->kind >= SYN_KINDS) return fail(GBRKC_EINVAL, "bad synapse kind %d", d->kind);
@@ -1348,6 +1365,10 @@ extern "C" int gbrkc_add_synapses(gbrkc_engine *E, const gbrkc_synapse_desc *d, 
   return 0;
 }
 
+extern "C" int gbrkc_add_synapses(gbrkc_engine *E, const gbrkc_synapse_desc *d, int *first_id) {
+  return no_throw([&] { return add_synapses_impl(E, d, first_id); });
+}
+
 extern "C" int gbrkc_read_synapses(gbrkc_engine *E, int field, double *host, long n) {
   if (!E || !host) return fail(GBRKC_EINVAL, "null argument");
   if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
@@ -1366,7 +1387,7 @@ extern "C" int gbrkc_read_synapses(gbrkc_engine *E, int field, double *host, lon
   return 0;
 }
 
-extern "C" int gbrkc_build(gbrkc_engine *E) {
+static int build_impl(gbrkc_engine *E) {
   if (!E) return fail(GBRKC_EINVAL, "null engine");
   if (E->built) return fail(GBRKC_ESTATE, "already built");
   if (E->systems.empty()) return fail(GBRKC_EINVAL, "no systems");
@@ -1413,6 +1434,8 @@ extern "C" int gbrkc_build(gbrkc_engine *E) {
   if (rc) { E->built = false; return rc; }
   return 0;
 }
+
+extern "C" int gbrkc_build(gbrkc_engine *E) { return no_throw([&] { return build_impl(E); }); }
 
 extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
   if (!E || n_iv < 0) return fail(GBRKC_EINVAL, "bad arguments");
@@ -1621,7 +1644,7 @@ extern "C" int gbrkc_read_soma_type(gbrkc_engine *E, int type, int n_iv, double 
   if (!E || type < 0 || type >= NTYPES || !host) return fail(GBRKC_EINVAL, "bad arguments");
   PoolHost &P = E->pools[type];
   if (P.systems.empty()) return 0;
-  if (!P.d_soma || n_iv > E->soma_iv) return fail(GBRKC_EINVAL, "no such recording");
+  if (!P.d_soma || n_iv < 0 || n_iv > E->soma_iv) return fail(GBRKC_EINVAL, "no such recording");
   CUDA_TRY(cudaMemcpyAsync(host, P.d_soma, (size_t)n_iv * P.ncell * P.rec_w * sizeof(double), cudaMemcpyDeviceToHost,
                            E->streams[type]));
   CUDA_TRY(cudaStreamSynchronize(E->streams[type]));
@@ -1675,7 +1698,7 @@ extern "C" long gbrkc_total_compartments(gbrkc_engine *E) {
   return n;
 }
 
-extern "C" int gbrkc_record_soma(gbrkc_engine *E, int n_max) {
+static int record_soma_impl(gbrkc_engine *E, int n_max) {
   if (!E || n_max < 0) return fail(GBRKC_EINVAL, "bad arguments");
   if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
   E->soma_cap = n_max;
@@ -1688,6 +1711,10 @@ extern "C" int gbrkc_record_soma(gbrkc_engine *E, int n_max) {
     if (rc) return rc;
   }
   return 0;
+}
+
+extern "C" int gbrkc_record_soma(gbrkc_engine *E, int n_max) {
+  return no_throw([&] { return record_soma_impl(E, n_max); });
 }
 
 extern "C" int gbrkc_record_width(gbrkc_engine *E, int type, int width) {
@@ -1712,12 +1739,12 @@ extern "C" int gbrkc_record_width(gbrkc_engine *E, int type, int width) {
   return 0;
 }
 
-extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) {
+static int read_soma_impl(gbrkc_engine *E, int id, int n_iv, double *host) {
   PoolHost *P = nullptr;
   HostSystem *S = nullptr;
   int rc = system_loc(E, id, &P, &S);
   if (rc) return rc;
-  if (!P->d_soma || n_iv > E->soma_iv || !host) return fail(GBRKC_EINVAL, "no such recording");
+  if (!P->d_soma || n_iv < 0 || n_iv > E->soma_iv || !host) return fail(GBRKC_EINVAL, "no such recording");
   const int c0 = P->sys_cell0[S->pool_index], w = P->rec_w;
   std::vector<double> all((size_t)n_iv * P->ncell * w);
   CUDA_TRY(cudaMemcpy(all.data(), P->d_soma, all.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -1725,6 +1752,10 @@ extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) 
     for (int c = 0; c < S->n * w; c++)
       host[(size_t)k * S->n * w + c] = all[((size_t)k * P->ncell + c0) * w + c];
   return 0;
+}
+
+extern "C" int gbrkc_read_soma(gbrkc_engine *E, int id, int n_iv, double *host) {
+  return no_throw([&] { return read_soma_impl(E, id, n_iv, host); });
 }
 
 // ------------------------------------------------------- slots and raster
@@ -1807,7 +1838,7 @@ int upload_run(gbrkc_engine *E, PoolHost &P, int pi0, int pi1) {
 
 }  // namespace
 
-extern "C" int gbrkc_systems_reset(gbrkc_engine *E, int first_id, int n, const gbrkc_reset_desc *d) {
+static int systems_reset_impl(gbrkc_engine *E, int first_id, int n, const gbrkc_reset_desc *d) {
   PoolHost *P = nullptr;
   int pi0 = 0;
   int rc = system_run(E, first_id, n, &P, &pi0);
@@ -1872,6 +1903,10 @@ extern "C" int gbrkc_systems_reset(gbrkc_engine *E, int first_id, int n, const g
   return 0;
 }
 
+extern "C" int gbrkc_systems_reset(gbrkc_engine *E, int first_id, int n, const gbrkc_reset_desc *d) {
+  return no_throw([&] { return systems_reset_impl(E, first_id, n, d); });
+}
+
 extern "C" int gbrkc_read_run(gbrkc_engine *E, int first_id, int n, int field, double *host, long cap) {
   PoolHost *P = nullptr;
   int pi0 = 0;
@@ -1918,7 +1953,7 @@ extern "C" int gbrkc_set_budget(gbrkc_engine *E, int first_id, int n, int n_inte
   return 0;
 }
 
-extern "C" int gbrkc_record_spikes(gbrkc_engine *E, long capacity) {
+static int record_spikes_impl(gbrkc_engine *E, long capacity) {
   if (!E || capacity < 0 || capacity > (1L << 30)) return fail(GBRKC_EINVAL, "bad arguments");
   if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
   for (int t = 0; t < NTYPES; t++) {
@@ -1939,7 +1974,11 @@ extern "C" int gbrkc_record_spikes(gbrkc_engine *E, long capacity) {
   return 0;
 }
 
-extern "C" int gbrkc_read_spikes(gbrkc_engine *E, int type, long cap, double *t, int *sys, int *cell, long *n) {
+extern "C" int gbrkc_record_spikes(gbrkc_engine *E, long capacity) {
+  return no_throw([&] { return record_spikes_impl(E, capacity); });
+}
+
+static int read_spikes_impl(gbrkc_engine *E, int type, long cap, double *t, int *sys, int *cell, long *n) {
   if (!E || type < 0 || type >= NTYPES || cap < 0 || !n || (cap > 0 && (!t || !sys || !cell)))
     return fail(GBRKC_EINVAL, "bad arguments");
   if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
@@ -1967,6 +2006,10 @@ extern "C" int gbrkc_read_spikes(gbrkc_engine *E, int type, long cap, double *t,
     return fail(GBRKC_EOVERFLOW, "%ld spike(s) lost (logged %d, log capacity %d, read capacity %ld)",
                 (long)cnt - m, cnt, P.spk_cap, cap);
   return 0;
+}
+
+extern "C" int gbrkc_read_spikes(gbrkc_engine *E, int type, long cap, double *t, int *sys, int *cell, long *n) {
+  return no_throw([&] { return read_spikes_impl(E, type, cap, t, sys, cell, n); });
 }
 
 extern "C" long long gbrkc_system_bytes(int precision, int cell_type, int ncomp, int ncell) {

@@ -27,7 +27,9 @@
 #include <string.h>
 
 #include <chrono>
+#include <exception>
 #include <map>
+#include <new>
 #include <memory>
 #include <string>
 #include <vector>
@@ -51,6 +53,19 @@ int srv_fail(int code, const char *fmt, ...) {
   va_end(ap);
   g_srv_error = buf;
   return code;
+}
+
+// A C entry point lets no C++ exception out (host allocations sized by the
+// caller report GBRKC_ENOMEM).
+template <class F>
+int srv_no_throw(F &&f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc &) {
+    return srv_fail(GBRKC_ENOMEM, "host memory exhausted");
+  } catch (const std::exception &x) {
+    return srv_fail(GBRKC_EINVAL, "%s", x.what());
+  }
 }
 
 double now_s() {
@@ -212,7 +227,7 @@ extern "C" int gbrkc_server_create(int precision, long long hbm_budget, int quan
 
 extern "C" void gbrkc_server_destroy(gbrkc_server *S) { delete S; }
 
-extern "C" int gbrkc_server_add_class(gbrkc_server *S, const gbrkc_slot_class *c, int *class_id) {
+static int server_add_class_impl(gbrkc_server *S, const gbrkc_slot_class *c, int *class_id) {
   if (!S || !c || !c->shape.rows) return srv_fail(GBRKC_EINVAL, "null argument");
   if (S->started) return srv_fail(GBRKC_ESTATE, "server already started");
   const gbrkc_system_desc &d = c->shape;
@@ -250,6 +265,10 @@ extern "C" int gbrkc_server_add_class(gbrkc_server *S, const gbrkc_slot_class *c
   return 0;
 }
 
+extern "C" int gbrkc_server_add_class(gbrkc_server *S, const gbrkc_slot_class *c, int *class_id) {
+  return srv_no_throw([&] { return server_add_class_impl(S, c, class_id); });
+}
+
 namespace {
 
 // The arenas' systems in the server's engine (idle until a request fills
@@ -284,7 +303,7 @@ int fill_arenas(gbrkc_server *S, long long cells) {
 
 }  // namespace
 
-extern "C" int gbrkc_server_start(gbrkc_server *S) {
+static int server_start_impl(gbrkc_server *S) {
   if (!S) return srv_fail(GBRKC_EINVAL, "null server");
   if (S->started) return srv_fail(GBRKC_ESTATE, "server already started");
   if (S->classes.empty()) return srv_fail(GBRKC_EINVAL, "no classes");
@@ -327,7 +346,9 @@ extern "C" int gbrkc_server_start(gbrkc_server *S) {
   return 0;
 }
 
-extern "C" int gbrkc_request_create(gbrkc_server *S, const gbrkc_request_desc *d, int *req_id) {
+extern "C" int gbrkc_server_start(gbrkc_server *S) { return srv_no_throw([&] { return server_start_impl(S); }); }
+
+static int request_create_impl(gbrkc_server *S, const gbrkc_request_desc *d, int *req_id) {
   if (!S || !d || !d->jitter) return srv_fail(GBRKC_EINVAL, "null argument");
   if (!S->started) return srv_fail(GBRKC_ESTATE, "server not started");
   if (d->class_id < 0 || d->class_id >= (int)S->classes.size()) return srv_fail(GBRKC_EINVAL, "bad class");
@@ -361,7 +382,11 @@ extern "C" int gbrkc_request_create(gbrkc_server *S, const gbrkc_request_desc *d
   return 0;
 }
 
-extern "C" int gbrkc_request_advance(gbrkc_server *S, int *n_done) {
+extern "C" int gbrkc_request_create(gbrkc_server *S, const gbrkc_request_desc *d, int *req_id) {
+  return srv_no_throw([&] { return request_create_impl(S, d, req_id); });
+}
+
+static int request_advance_impl(gbrkc_server *S, int *n_done) {
   if (!S) return srv_fail(GBRKC_EINVAL, "null server");
   if (!S->started) return srv_fail(GBRKC_ESTATE, "server not started");
   const double t_round = now_s();
@@ -433,6 +458,10 @@ extern "C" int gbrkc_request_advance(gbrkc_server *S, int *n_done) {
   S->busy_s += now_s() - t_round;
   if (n_done) *n_done = done;
   return 0;
+}
+
+extern "C" int gbrkc_request_advance(gbrkc_server *S, int *n_done) {
+  return srv_no_throw([&] { return request_advance_impl(S, n_done); });
 }
 
 extern "C" int gbrkc_request_state(gbrkc_server *S, int rid, int *state, double *latency_ms, int *status) {

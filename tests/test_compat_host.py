@@ -75,7 +75,7 @@ def test_rand_drawn_by_non_empty_random_families(lib, tmp_path, monkeypatch):
         fin(o, 0)
 
 
-def test_raster_plot(lib, tmp_path, monkeypatch):
+def test_raster_plot(lib, tmp_path, monkeypatch, capfd):
     """output.cu's post-run Golgi raster: a row per interval, the index of
     each cell whose voltage crossed 0 mV upward, "," for the others."""
     monkeypatch.chdir(tmp_path)
@@ -84,6 +84,8 @@ def test_raster_plot(lib, tmp_path, monkeypatch):
     (tmp_path / "go_v_by_RKC.csv").write_text("".join(",".join("%lf" % x for x in r) + ",\n" for r in rows))
     lib.raster_plot.argtypes = [C.c_int, C.c_char_p]
     lib.raster_plot(3, b"RKC")
+    C.CDLL(None).fflush(None)
+    assert capfd.readouterr().out == "Debug for output \n2,0,1,0,2,"
     got = (tmp_path / "go_raster_by_RKC.csv").read_text().splitlines()
     # cell 2 crosses in the first row (from -70 mV); 0 in the second; 1 in the third; 0 and 2 in the fourth
     assert got == ["0.125000,,,2,", "0.250000,0,,,", "0.375000,,1,,", "0.500000,0,,2,"]
