@@ -124,8 +124,6 @@ std::vector<double> draw_jitter(int type, int n) {
   return j;
 }
 
-__device__ int d_stim_comp[NTYPES];
-
 // kBE, kCN or kRKC from a solver name, matched on its first letters as
 // main.cu:60-102 does; -1 for anything else
 int solver_kind(const char *solver) {
@@ -195,9 +193,8 @@ neuron_t *initialize(int type, int nx, int ny, const char *solver, neuron_t *p) 
     check(gbrkc_field_device_ptr(B.eng, B.sid, GBRKC_F_V, &B.h_elem[v]), "elem[v]");
     check(gbrkc_field_device_ptr(B.eng, B.sid, GBRKC_F_CA, &B.h_elem[Ca]), "elem[Ca]");
     check(gbrkc_field_device_ptr(B.eng, B.sid, GBRKC_F_IEXT, &B.h_elem[i_ext]), "elem[i_ext]");
-    const int sc = (type == GBRKC_IO) ? 0 : (type == GBRKC_GO) ? 30 : soma_comp(type, B.ncomp);
-    cuda_check(cudaMemcpyToSymbol(d_stim_comp, &sc, sizeof(int), type * sizeof(int)), "stimulus site");
-    B.stim_comp = sc;
+    // the compartment the X_set_current kernels drive
+    B.stim_comp = (type == GBRKC_IO) ? 0 : (type == GBRKC_GO) ? 30 : soma_comp(type, B.ncomp);
   }
   // device mirror for the stimulus kernels
   cuda_check(cudaMalloc(&B.d_elem, n_elem * sizeof(double *)), "device table");
@@ -241,22 +238,12 @@ void update_v(int type) {
   B.t += H_MAX;
 }
 
-// stimulus protocols of the reference's *_set_current kernels
+// stimulus protocols of the reference's *_set_current kernels (the
+// kernels themselves are defined in gbrkc_compat.h)
 struct Protocol {
   double t0, t1, amp;
 };
-__device__ __forceinline__ void set_current(neuron_t *d, int type, double t, Protocol pr) {
-  const int id = threadIdx.x + blockIdx.x * blockDim.x;
-  if (id < d->n) {
-    const int ncomp = d->nc / d->n;
-    double *iv = &d->elem[i_ext][d_stim_comp[type] + id * ncomp];
-    *iv = 0.0;
-    if (pr.t0 <= t && t < pr.t1) *iv = pr.amp;
-  }
-}
-
-constexpr Protocol PR_GR{50.0, 100.0, 0.01e-3}, PR_GO{800.0, 1100.0, 0.2e-3}, PR_PKJ{550.0, 1300.0, 0.1e-3},
-    PR_IO{800.0, 820.0, 5.5};
+constexpr Protocol PR_GR{GBRKC_STIM_GR}, PR_GO{GBRKC_STIM_GO}, PR_PKJ{GBRKC_STIM_PKJ}, PR_IO{GBRKC_STIM_IO};
 
 void output(int type, neuron_t *p, double *vh, double *rprev, double t, FILE *fv, FILE *fr) {
   const Block &B = g_block[type];
@@ -599,15 +586,6 @@ void network_release() {
 
 extern "C" {
 
-// exported (nvcc gives kernel stubs hidden visibility by default): a caller
-// launches these with <<<>>> from its own translation unit, as main.cu does
-#define GBRKC_EXPORT __attribute__((visibility("default")))
-GBRKC_EXPORT __global__ void gr_set_current(neuron_t *d_gr, const double t) { set_current(d_gr, GBRKC_GR, t, PR_GR); }
-GBRKC_EXPORT __global__ void go_set_current(neuron_t *d_go, const double t) { set_current(d_go, GBRKC_GO, t, PR_GO); }
-GBRKC_EXPORT __global__ void pkj_set_current(neuron_t *d_pkj, const double t) {
-  set_current(d_pkj, GBRKC_PKJ, t, PR_PKJ);
-}
-GBRKC_EXPORT __global__ void io_set_current(neuron_t *d_io, const double t) { set_current(d_io, GBRKC_IO, t, PR_IO); }
 
 neuron_t *gr_initialize(const int nx, const int ny, const char *type, neuron_t *p) {
   return initialize(GBRKC_GR, nx, ny, type, p);

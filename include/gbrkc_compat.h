@@ -120,17 +120,45 @@ void io_solve_by_rkc(neuron_t *d, neuron_solve_t *d_solve, neuron_t *p, neuron_s
 /* The reference's stimulus protocols, as kernels over the device neuron_t
  * (launch <<<n / 128 + 1, 128>>> on the default stream, as main.cu does) and
  * as host launchers for callers without a CUDA compiler.  GrC: 0.01 nA at the
- * soma for 50 <= t < 100 ms (gr.cu:245); GoC: 0.2 nA at compartment 30 for
- * 800 <= t < 1100 (go.cu:258); PC: 0.1 nA at the soma for 550 <= t < 1300
- * (pkj.cu:333); IO: 5.5 uA/cm^2 at the dendrite for 800 <= t < 820
- * (io.cu:247). */
+ * soma for 50 <= t < 100 ms (gr.cu:244-253); GoC: 0.2 nA at compartment 30
+ * for 800 <= t < 1100 (go.cu:257-267); PC: 0.1 nA at the soma for
+ * 550 <= t < 1300 (pkj.cu:332-343); IO: 5.5 uA/cm^2 at the dendrite for
+ * 800 <= t < 820 (io.cu:246-256).  Each is (t0, t1, amplitude). */
+#define GBRKC_STIM_GR 50.0, 100.0, 0.01e-3
+#define GBRKC_STIM_GO 800.0, 1100.0, 0.2e-3
+#define GBRKC_STIM_PKJ 550.0, 1300.0, 0.1e-3
+#define GBRKC_STIM_IO 800.0, 820.0, 5.5
 #ifdef __CUDACC__
-/* default visibility: nvcc hides kernel stubs by default, which would keep a
- * caller's <<<>>> launch from binding to the library's kernels */
-__attribute__((visibility("default"))) __global__ void gr_set_current(neuron_t *d_gr, const double t);
-__attribute__((visibility("default"))) __global__ void go_set_current(neuron_t *d_go, const double t);
-__attribute__((visibility("default"))) __global__ void pkj_set_current(neuron_t *d_pkj, const double t);
-__attribute__((visibility("default"))) __global__ void io_set_current(neuron_t *d_io, const double t);
+/* The kernels are defined here, not in the library: a caller's <<<>>>
+ * launch then runs the caller's own copy through the caller's own CUDA
+ * runtime, however each side links the runtime (a launch through another
+ * module's kernel stub pairs the launch configuration across two runtimes
+ * when they are linked statically). */
+static __device__ __forceinline__ void gbrkc_set_current(neuron_t *d, int type, double t, double t0, double t1,
+                                                         double amp) {
+  const int id = threadIdx.x + blockIdx.x * blockDim.x;
+  if (id < d->n) {
+    const int ncomp = d->nc / d->n;
+    /* GrC soma (16 in the reference's 578-compartment cell, else 1), GoC 30, PC soma (the last), IO 0 */
+    const int comp = type == N_TYPE_IO ? 0 : type == N_TYPE_GO ? 30 : type == N_TYPE_PKJ ? ncomp - 1
+                                                                                        : (ncomp == 578 ? 16 : 1);
+    double *iv = &d->elem[i_ext][comp + id * ncomp];
+    *iv = 0.0;
+    if (t0 <= t && t < t1) *iv = amp;
+  }
+}
+static __global__ void gr_set_current(neuron_t *d_gr, const double t) {
+  gbrkc_set_current(d_gr, N_TYPE_GR, t, GBRKC_STIM_GR);
+}
+static __global__ void go_set_current(neuron_t *d_go, const double t) {
+  gbrkc_set_current(d_go, N_TYPE_GO, t, GBRKC_STIM_GO);
+}
+static __global__ void pkj_set_current(neuron_t *d_pkj, const double t) {
+  gbrkc_set_current(d_pkj, N_TYPE_PKJ, t, GBRKC_STIM_PKJ);
+}
+static __global__ void io_set_current(neuron_t *d_io, const double t) {
+  gbrkc_set_current(d_io, N_TYPE_IO, t, GBRKC_STIM_IO);
+}
 #endif
 void gr_set_current_launch(neuron_t *d_gr, const double t);
 void go_set_current_launch(neuron_t *d_go, const double t);
