@@ -139,6 +139,12 @@ int main(int argc, char **argv) {
     return 1;
   }
   srand(0);  // the initial-voltage jitter stream, seeded as main.cu:38 does
+  // the reference's console echo (main.cu:40-55)
+  printf("argc = %d\n", argc);
+  for (int i = 0; i < argc; i++) printf("argv[%d] = %s\n", i, argv[i]);
+  static const char *const kEcho[4] = {"GR  solver -> ", "GO  solver -> ", "PKJ solver -> ", "IO  solver -> "};
+  for (int k = 0; k < 4; k++) printf("%s%s\n", kEcho[k], argv[1 + 3 * k]);
+  printf("\n");
   TypeRun runs[4] = {
       {"gr", gr_initialize, gr_solve_initialize, gr_set_current_launch, gr_output_file, gr_finalize, gr_solve_finalize},
       {"go", go_initialize, go_solve_initialize, go_set_current_launch, go_output_file, go_finalize, go_solve_finalize},
@@ -244,7 +250,12 @@ int main(int argc, char **argv) {
     }
     w.finish();
   }
+  long t_count = 0;
   while (t < ts - 0.0001) {
+    if (t_count++ % 400 == 0) {  // progress every 50 ms (main.cu:185-190)
+      printf("time:%f\n", t);
+      printf("Now compute time = %.2f \n", (double)(clock() - start) / CLOCKS_PER_SEC);
+    }
     for (int k = 0; k < 4; k++) {
       TypeRun &r = runs[k];
       if (r.p->n <= 0) continue;

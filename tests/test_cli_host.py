@@ -28,6 +28,9 @@ def test_unknown_solver_name(cli, tmp_path):
     r = run(cli, tmp_path, "RKC", "0", "0", "XX", "0", "0", "RKC", "0", "0", "RKC", "0", "0")
     assert r.returncode == 0
     assert "Error!! -> set solver name in argv [ 4 ]" in r.stdout
+    # main.cu:40-55's echo comes first
+    assert r.stdout.startswith("argc = 14\nargv[0] = ")
+    assert "argv[4] = XX\n" in r.stdout and "GO  solver -> XX\n" in r.stdout
 
 
 def test_be_cn_refused_for_a_type_with_cells(cli, tmp_path):
