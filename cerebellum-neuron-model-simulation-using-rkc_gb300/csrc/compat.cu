@@ -245,6 +245,16 @@ struct Protocol {
 };
 constexpr Protocol PR_GR{GBRKC_STIM_GR}, PR_GO{GBRKC_STIM_GO}, PR_PKJ{GBRKC_STIM_PKJ}, PR_IO{GBRKC_STIM_IO};
 
+// pkj.cu:346-354: every Purkinje soma (the last compartment) gets 0.1 nA
+// times the filtered Poisson train
+__global__ void set_current_poisson(neuron_t *d_pkj, const double val_current) {
+  const int id = threadIdx.x + blockIdx.x * blockDim.x;
+  if (id < d_pkj->n) {
+    const int ncomp = d_pkj->nc / d_pkj->n;
+    d_pkj->elem[i_ext][ncomp - 1 + id * ncomp] = 0.1e-3 * val_current;
+  }
+}
+
 void output(int type, neuron_t *p, double *vh, double *rprev, double t, FILE *fv, FILE *fr) {
   const Block &B = g_block[type];
   const int nc = B.ncomp;
@@ -637,6 +647,16 @@ void gr_set_current_launch(neuron_t *d, const double t) { launch_stim(GBRKC_GR, 
 void go_set_current_launch(neuron_t *d, const double t) { launch_stim(GBRKC_GO, d, t); }
 void pkj_set_current_launch(neuron_t *d, const double t) { launch_stim(GBRKC_PKJ, d, t); }
 void io_set_current_launch(neuron_t *d, const double t) { launch_stim(GBRKC_IO, d, t); }
+void pkj_set_current_Poisson(const int num, neuron_t *d_pkj, const double t) {
+  static double val_current = 0.0;
+  const double fr = (350 <= t && t < 1000) ? 25.0 : 0.0;
+  const double f = ((double)rand() + 1.0) / ((double)RAND_MAX + 2.0);
+  const int firing_flag = (fr * 0.125 * 0.001 > f) ? 1 : 0;
+  val_current = val_current * 0.81193634615 + firing_flag;  // exp(-0.125 / 0.6)
+  if (num <= 0) return;
+  set_current_poisson<<<(num + 127) / 128, 128>>>(d_pkj, val_current);
+  cuda_check(cudaGetLastError(), "Poisson stimulus launch");
+}
 
 void gr_output_file(neuron_t *p, double *vh, double *rp, const double t, FILE *fv, FILE *fr) {
   output(GBRKC_GR, p, vh, rp, t, fv, fr);

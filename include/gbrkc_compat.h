@@ -164,6 +164,12 @@ void gr_set_current_launch(neuron_t *d_gr, const double t);
 void go_set_current_launch(neuron_t *d_go, const double t);
 void pkj_set_current_launch(neuron_t *d_pkj, const double t);
 void io_set_current_launch(neuron_t *d_io, const double t);
+/* The reference's alternative Purkinje stimulus (pkj.cu:346-368; its call
+ * in main.cu, once per interval, is commented out): a 25 Hz Poisson train
+ * for 350 <= t < 1000 ms, one rand() draw per call, filtered by
+ * exp(-0.125 / 0.6 ms); every cell's soma gets 0.1 nA times the filtered
+ * train.  The train's state is kept across calls, as the reference's. */
+void pkj_set_current_Poisson(const int num, neuron_t *d_pkj, const double t);
 
 /* One CSV row of soma voltages ("%lf," per value, t first; IO: its three
  * compartments per cell) and the raster lines "%lf,%d\n" of cells whose

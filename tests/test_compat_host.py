@@ -89,3 +89,16 @@ def test_raster_plot(lib, tmp_path, monkeypatch, capfd):
     got = (tmp_path / "go_raster_by_RKC.csv").read_text().splitlines()
     # cell 2 crosses in the first row (from -70 mV); 0 in the second; 1 in the third; 0 and 2 in the fourth
     assert got == ["0.125000,,,2,", "0.250000,0,,,", "0.375000,,1,,", "0.500000,0,,2,"]
+
+
+def test_pkj_poisson_draws_one_rand_per_call(lib):
+    """pkj_set_current_Poisson draws one rand() per call, as pkj.cu:364 does
+    (no cells: nothing is launched)."""
+    lib.pkj_set_current_Poisson.argtypes = [C.c_int, C.c_void_p, C.c_double]
+    libc = C.CDLL(None)
+    libc.srand(11)
+    seq = [libc.rand() for _ in range(4)]
+    libc.srand(11)
+    for t in (0.0, 400.0, 400.125):
+        lib.pkj_set_current_Poisson(0, None, t)
+    assert libc.rand() == seq[3]
