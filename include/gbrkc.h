@@ -29,7 +29,7 @@ enum {
   GBRKC_EINVAL = -1,   /* bad argument */
   GBRKC_ECUDA = -2,    /* CUDA error (no device, launch failure, ...) */
   GBRKC_ESTATE = -3,   /* call out of order (e.g. add after build) */
-  GBRKC_ENOMEM = -4,   /* device allocation failed */
+  GBRKC_ENOMEM = -4,   /* device or host allocation failed */
   GBRKC_ESOLVER = -5,  /* a system stopped: see gbrkc_system_ctl status */
   GBRKC_EOVERFLOW = -6 /* a fixed-size log or queue was full: entries were lost */
 };
