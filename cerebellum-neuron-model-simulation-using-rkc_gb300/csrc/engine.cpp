@@ -1849,6 +1849,7 @@ static int systems_reset_impl(gbrkc_engine *E, int first_id, int n, const gbrkc_
   if (d->stim_comp && (!d->stim_amp || !d->stim_t0 || !d->stim_t1)) return fail(GBRKC_EINVAL, "incomplete stimulus");
   // validate everything before changing anything
   long cells = 0, edges = 0;
+  std::vector<std::vector<double>> new_gap_g(n);  // the olive systems' new edge conductances
   for (int k = 0; k < n; k++) {
     const HostSystem &S = E->systems[first_id + k];
     for (int c = 0; c < S.n; c++) {
@@ -1859,8 +1860,18 @@ static int systems_reset_impl(gbrkc_engine *E, int first_id, int n, const gbrkc_
         if (!(x >= 0.0) || !std::isfinite(x)) return fail(GBRKC_EINVAL, "conductance scale must be finite and >= 0");
       }
     }
+    if (d->io_gap_g && S.type == IO && !S.gap_pre.empty()) {
+      // same edges, new conductances (gap.cu:4-120)
+      HostSystem G = S;
+      G.io_gap_g.assign(d->io_gap_g + 4 * cells, d->io_gap_g + 4 * (cells + S.n));
+      G.gap_pre.clear(); G.gap_post.clear(); G.gap_g.clear();
+      if ((rc = build_io_gap(G))) return rc;
+      if (G.gap_pre != S.gap_pre || G.gap_post != S.gap_post)
+        return fail(GBRKC_EINVAL, "io_gap_g changes the edge set of system %d (a conductance of 0?)", first_id + k);
+      new_gap_g[k] = std::move(G.gap_g);
+      edges += 4L * S.n;
+    }
     cells += S.n;
-    if (d->io_gap_g && S.type == IO && !S.gap_pre.empty()) edges += 4L * S.n;
   }
   if (d->io_gap_g && edges == 0) return fail(GBRKC_EINVAL, "io_gap_g given for systems without IO gap junctions");
   cells = 0;
@@ -1879,15 +1890,8 @@ static int systems_reset_impl(gbrkc_engine *E, int first_id, int n, const gbrkc_
     if (d->cond_scale) S.cond_scale.assign(d->cond_scale + cells, d->cond_scale + cells + S.n);
     else S.cond_scale.clear();
     if (d->io_gap_g && S.type == IO && !S.gap_pre.empty()) {
-      // same edges, new conductances (gap.cu:4-120)
-      HostSystem G = S;
-      G.io_gap_g.assign(d->io_gap_g + 4 * cells, d->io_gap_g + 4 * (cells + S.n));
-      G.gap_pre.clear(); G.gap_post.clear(); G.gap_g.clear();
-      if ((rc = build_io_gap(G))) return rc;
-      if (G.gap_pre != S.gap_pre || G.gap_post != S.gap_post)
-        return fail(GBRKC_EINVAL, "io_gap_g changes the edge set of system %d (a conductance of 0?)", first_id + k);
-      S.io_gap_g = G.io_gap_g;
-      S.gap_g = G.gap_g;
+      S.io_gap_g.assign(d->io_gap_g + 4 * cells, d->io_gap_g + 4 * (cells + S.n));
+      S.gap_g = std::move(new_gap_g[k]);
       std::copy(S.gap_g.begin(), S.gap_g.end(), P->gap_g.begin() + P->sys_gap0[pi]);
     }
     fill_state(E, *P, S, P->sys_off[pi], P->sys_cell0[pi]);
