@@ -2016,6 +2016,17 @@ extern "C" int gbrkc_read_spikes(gbrkc_engine *E, int type, long cap, double *t,
   return no_throw([&] { return read_spikes_impl(E, type, cap, t, sys, cell, n); });
 }
 
+extern "C" long gbrkc_rkc_coefficients(int m, double *out, long cap) {
+  if (m < 1 || m > 1024 || cap < 0 || (!out && cap > 0)) return fail(GBRKC_EINVAL, "bad arguments");
+  std::vector<double> coef;
+  std::vector<long> off;
+  coef_table(m, coef, off);
+  const long n = off[m + 1] - off[m];
+  if (cap < n) return fail(GBRKC_EINVAL, "buffer holds %ld of %ld values", cap, n);
+  std::copy(coef.begin() + off[m], coef.begin() + off[m + 1], out);
+  return n;
+}
+
 extern "C" long long gbrkc_system_bytes(int precision, int cell_type, int ncomp, int ncell) {
   if (cell_type < 0 || cell_type >= NTYPES || ncomp <= 0 || ncell <= 0) return fail(GBRKC_EINVAL, "bad shape");
   const long long nc = (long long)ncomp * ncell;

@@ -264,6 +264,12 @@ int gbrkc_set_budget(gbrkc_engine *e, int first_id, int n, int n_intervals);
 /* Device bytes one system of this shape takes in an engine (an upper
  * estimate for admission control), or a negative error code. */
 long long gbrkc_system_bytes(int precision, int cell_type, int ncomp, int ncell);
+/* The RKC stage coefficients the kernels use for m stages (1 <= m <= 1024),
+ * tabulated on the host by the recurrences of solve_rkc.cu:816-906: mu~_1,
+ * then for each stage j = 2..m the five values mu_j, nu_j, 1 - mu_j - nu_j,
+ * mu~_j and a_{j-1}.  Returns the count, 1 + 5 (m - 1), or a negative error
+ * code.  Needs no device. */
+long gbrkc_rkc_coefficients(int m, double *out, long cap);
 
 /* ---- device raster ----
  * At the end of every interval each cell's spike compartment is compared

@@ -37,3 +37,17 @@ def test_no_row_swaps(oracle):
     assert s.stats()["ion_updates"] > 20
     assert sp_gr + sp_go > 0, "the runs should cross spike threshold"
     assert O.pivot_swaps() == before
+
+
+def test_markov_states_conserved(oracle):
+    """The Markov schemes keep their occupancies summing to 1 through the
+    same spiking runs (the reference's own check: gr_ion.cu:204, within
+    0.99..1.01; go_ion.cu:208, within 1e-4); here to 1e-9."""
+    O = oracle
+    for cell_type, rows, comp, amp, ms, slots in ((M.GR, M.gr_reduced4(), 1, 0.05e-3, 30.0, range(8, 20)),
+                                                   (M.GO, M.go_synthetic(2), 30, 0.4e-3, 15.0, range(18, 24))):
+        s, _ = run(O, cell_type, rows, comp, amp, ms)
+        total = sum(s.ion(k) for k in slots)
+        used = total > 0.5                       # compartments that carry the scheme
+        assert used.any()
+        assert np.max(np.abs(total[used] - 1.0)) < 1e-9, (cell_type, np.max(np.abs(total[used] - 1.0)))
