@@ -455,6 +455,9 @@ struct gbrkc_engine {
   double role_work[NTYPES] = {};  // smoothed CTA-ms per role
   int *d_queue = nullptr;
   unsigned long long *d_tstart = nullptr, *d_tend = nullptr;
+  // device address of noalloc.cu's static launch scratch, looked up at build
+  // on the engine's device (persistent engines only)
+  unsigned long long *d_static_scratch = nullptr;
   // chemical synapses (network mode), as added
   struct {
     std::vector<int> kind, grp, pre_sys, pre_comp, post_sys, post_comp;
@@ -1424,6 +1427,11 @@ static int build_impl(gbrkc_engine *E) {
     if (!rc) rc = E->mem.upload(z, &E->d_tstart);
     if (!rc) rc = E->mem.upload(z, &E->d_tend);
     if (rc) return rc;
+    // gbrkc_advance_noalloc's scratch: its address is taken here, while the
+    // engine's device is current, so that the advance itself only reads it
+    // (and an engine built after a device reset gets the new module's address)
+    rc = noalloc_scratch(&E->d_static_scratch);
+    if (rc) return fail(GBRKC_ECUDA, "static scratch: %s", cudaGetErrorString((cudaError_t)rc));
   }
   {
     int rc = build_synapses(E);
@@ -2124,9 +2132,8 @@ extern "C" int gbrkc_advance_noalloc(gbrkc_engine *E, double t0, int n_iv) {
     // systems reset since the last call are initialised (only they) first
     const int n = init ? 0 : n_iv;
     if (E->mega) {
-      unsigned long long *scratch = nullptr;
-      rc = noalloc_scratch(&scratch);
-      if (rc) return fail(GBRKC_ECUDA, "static scratch: %s", cudaGetErrorString((cudaError_t)rc));
+      unsigned long long *scratch = E->d_static_scratch;
+      if (!scratch) return fail(GBRKC_ESTATE, "static scratch address not set up");
       rc = (E->precision == GBRKC_FP64) ? launch_mega_static<double>(E, t0, n, iv0, init, scratch)
                                         : launch_mega_static<float>(E, t0, n, iv0, init, scratch);
     } else {
@@ -2137,22 +2144,31 @@ extern "C" int gbrkc_advance_noalloc(gbrkc_engine *E, double t0, int n_iv) {
     if (init) E->pending_init = false;
   }
   if (E->soma_cap > 0) E->soma_iv += n_iv;
-  // stopped systems: their status words, read in chunks with a strided copy
+  // stopped systems: their status words and interval budgets (adjacent in
+  // Ctl), read in chunks with a strided copy; the granule systems with work
+  // left are counted as gbrkc_advance counts them, for the next launch's
+  // granule warps
+  static_assert(offsetof(Ctl, iv_left) == offsetof(Ctl, status) + sizeof(int), "status and iv_left adjacent");
   int stopped = 0, first_id = -1, first_status = 0;
   constexpr int CHUNK = 512;
-  int status[CHUNK];
+  int word[2 * CHUNK];
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
     const int nsys = (int)P.systems.size();
+    long active = 0;
     for (int i0 = 0; i0 < nsys; i0 += CHUNK) {
       const int cnt = std::min(CHUNK, nsys - i0);
-      CUDA_TRY(cudaMemcpy2D(status, sizeof(int), (const char *)(P.d_ctl + i0) + offsetof(Ctl, status), sizeof(Ctl),
-                            sizeof(int), cnt, cudaMemcpyDeviceToHost));
-      for (int i = 0; i < cnt; i++)
-        if (status[i]) {
-          if (!stopped++) { first_id = P.systems[i0 + i]; first_status = status[i]; }
+      CUDA_TRY(cudaMemcpy2D(word, 2 * sizeof(int), (const char *)(P.d_ctl + i0) + offsetof(Ctl, status),
+                            sizeof(Ctl), 2 * sizeof(int), cnt, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < cnt; i++) {
+        const int status = word[2 * i], iv_left = word[2 * i + 1];
+        active += (status == 0 && iv_left != 0);
+        if (status) {
+          if (!stopped++) { first_id = P.systems[i0 + i]; first_status = status; }
         }
+      }
     }
+    if (t == GR && nsys > 0) E->gr_active = active;
   }
   if (stopped)
     return fail(GBRKC_ESOLVER, "%d system(s) are stopped (first: system %d, status %d); the others advanced", stopped,

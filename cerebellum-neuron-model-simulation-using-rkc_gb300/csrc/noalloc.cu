@@ -5,8 +5,11 @@
 // (NOALLOC_SCRATCH_WORDS * 8 bytes = 16.6 KB) until the process exits.
 //
 // Host code may not use the array's name as a device address (on the host it
-// names a host-side stand-in): the address is looked up here, once per
-// device, with cudaGetSymbolAddress while that device is current.
+// names a host-side stand-in): the address is looked up here with
+// cudaGetSymbolAddress while the engine's device is current.  gbrkc_build
+// calls this once per persistent engine and keeps the result in the engine,
+// so an engine built after a device reset (which reloads this module) gets
+// the reloaded array's address, and the advance itself looks nothing up.
 #include <cuda_runtime.h>
 
 #include "noalloc.h"
@@ -17,23 +20,13 @@ namespace {
 
 static __device__ __align__(256) unsigned long long g_scratch[NOALLOC_SCRATCH_WORDS];
 
-constexpr int MAX_DEVICES = 64;
-unsigned long long *g_addr[MAX_DEVICES] = {};
-
 }  // namespace
 
 int noalloc_scratch(unsigned long long **ptr) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
   if (e != cudaSuccess) return (int)e;
-  if (dev < 0 || dev >= MAX_DEVICES) return (int)cudaErrorInvalidDevice;
-  if (!g_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) return (int)e;
-    g_addr[dev] = (unsigned long long *)p;
-  }
-  *ptr = g_addr[dev];
+  *ptr = (unsigned long long *)p;
   return 0;
 }
 

@@ -10,8 +10,9 @@ constexpr int NOALLOC_MAX_CTAS = 1024;
 constexpr int NOALLOC_QUEUE_WORDS = 32;
 constexpr int NOALLOC_SCRATCH_WORDS = NOALLOC_QUEUE_WORDS + 2 * NOALLOC_MAX_CTAS;
 
-// Device address of the scratch on the current device (looked up on the
-// first call per device).  Returns 0 or a cudaError_t code.
+// Device address of the scratch on the current device (a fresh lookup on
+// every call; gbrkc_build makes it once per persistent engine).  Returns 0 or
+// a cudaError_t code.
 int noalloc_scratch(unsigned long long **ptr);
 
 }  // namespace gbrkc

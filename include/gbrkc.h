@@ -201,8 +201,11 @@ int gbrkc_read_synapses(gbrkc_engine *e, int field, double *host, long n);
  * library until the process exits); a larger launch is rejected with
  * GBRKC_EINVAL.  Engines advanced one pool per launch need no scratch and
  * take the same path as gbrkc_advance.
- *   - The first call on a device looks the array's address up; make that
- *     first call before any stream capture.
+ *   - gbrkc_build looks the array's address up on the engine's device and
+ *     keeps it in the engine; this call only reads it.  An engine built
+ *     after a device reset gets the reloaded array's address.
+ *   - The call waits for its launch to finish and reads the status words
+ *     back (device synchronisation, no allocation).
  *   - Every call shares the one array: calls whose work overlaps on the GPU
  *     (e.g. two host threads advancing two engines at once) race on it and
  *     corrupt each other's scheduling.  Serialise them.
