@@ -82,27 +82,34 @@ def pkj_grid(nx=3, ny=3, seed=2, amp=0.5e-3, tree_seed=None, gap=True):
 AMP_MAX = {M.GR: 0.05e-3, M.GO: 0.4e-3, M.PKJ: 0.4e-3, M.IO: 6.0}
 
 
-def mixed_batch(seed=2, n_gr=4096, n_go=1024, n_pkj=256, io_side=16):
+def mixed_batch(seed=2, n_gr=4096, n_go=1024, n_pkj=256, io_side=16, amp_max=None, go_variants=GO_STABLE_VARIANTS,
+                pkj_seeds=PKJ_STABLE_SEEDS, pkj_taper=True):
+    """The mixed-type batch.  amp_max (per type) bounds the step currents;
+    go_variants / pkj_seeds pick the tree shapes, cycled over the cells;
+    pkj_taper=False gives untapered Purkinje trees.  Each spec's tag names
+    its type and shape ("pkj7", "go3", ...)."""
+    amp = dict(AMP_MAX if amp_max is None else amp_max)
     rng = np.random.default_rng(seed)
     specs = []
     gr_rows = M.gr_reduced4()
     for i in range(n_gr):
         specs.append(Spec(M.GR, 1, 1, gr_rows, _jitter(rng, 1),
-                          stim=(1, rng.uniform(0, AMP_MAX[M.GR]), rng.uniform(0, 20.0), 1e9), tag="gr"))
-    go_rows = [M.go_synthetic(seed * 1000 + k) for k in GO_STABLE_VARIANTS]
+                          stim=(1, rng.uniform(0, amp[M.GR]), rng.uniform(0, 20.0), 1e9), tag="gr"))
+    go_rows = [M.go_synthetic(seed * 1000 + k) for k in go_variants]
     for i in range(n_go):
         specs.append(Spec(M.GO, 1, 1, go_rows[i % len(go_rows)], _jitter(rng, 1),
-                          stim=(30, rng.uniform(0, AMP_MAX[M.GO]), rng.uniform(0, 20.0), 1e9), tag="go"))
-    pk_rows = [M.pkj_synthetic(s) for s in PKJ_STABLE_SEEDS]
+                          stim=(30, rng.uniform(0, amp[M.GO]), rng.uniform(0, 20.0), 1e9),
+                          tag=f"go{go_variants[i % len(go_rows)]}"))
+    pk_rows = [M.pkj_synthetic(s, taper=pkj_taper) for s in pkj_seeds]
     for i in range(n_pkj):
         r = pk_rows[i % len(pk_rows)]
         specs.append(Spec(M.PKJ, 1, 1, r, _jitter(rng, 1),
-                          stim=(r.shape[0] - 1, rng.uniform(0, AMP_MAX[M.PKJ]), rng.uniform(0, 20.0), 1e9),
-                          tag="pkj"))
+                          stim=(r.shape[0] - 1, rng.uniform(0, amp[M.PKJ]), rng.uniform(0, 20.0), 1e9),
+                          tag=f"pkj{pkj_seeds[i % len(pk_rows)]}"))
     if io_side > 0:
         n = io_side * io_side
         specs.append(Spec(M.IO, io_side, io_side, M.io_rows(), _jitter(rng, n),
-                          stim=(np.zeros(n, np.int32), rng.uniform(0, AMP_MAX[M.IO], n), rng.uniform(0, 20.0, n),
+                          stim=(np.zeros(n, np.int32), rng.uniform(0, amp[M.IO], n), rng.uniform(0, 20.0, n),
                                 np.full(n, 1e9)),
                           gap=True, io_gap_g=G_C_IO * rng.uniform(0.5, 1.5, 4 * n), tag="io"))
     return specs

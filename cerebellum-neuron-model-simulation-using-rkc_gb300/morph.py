@@ -129,7 +129,7 @@ def _random_binary_tree(rng, n_nodes: int, root_children: int):
     return parent, depth
 
 
-def pkj_synthetic(seed: int, ncomp: int = 1600) -> np.ndarray:
+def pkj_synthetic(seed: int, ncomp: int = 1600, taper: bool = True) -> np.ndarray:
     """Seeded synthetic Purkinje cell in ``Pkj.txt`` layout.
 
     Soma at index ncomp-1 (diameter 29.8 um, type 0) and a binary-branching
@@ -141,7 +141,8 @@ def pkj_synthetic(seed: int, ncomp: int = 1600) -> np.ndarray:
     diameters 8.4 / 4.6 / 1.5 um in Pkj.txt); without the thick trunk the soma
     is too weakly loaded for the frozen-current RKC splitting at 0.5 nA.
     Parents always carry a higher index than their children, as in the
-    reference file."""
+    reference file.  taper=False draws every diameter from the untapered
+    lognormal (median 1.5 um)."""
     rng = np.random.default_rng(seed)
     nd = ncomp - 1
     parent, depth = _random_binary_tree(rng, nd, root_children=1)
@@ -158,7 +159,7 @@ def pkj_synthetic(seed: int, ncomp: int = 1600) -> np.ndarray:
         x, y, z = (L * u).tolist()
         dep = depth[old]
         ctype = 1 if dep <= 3 else (2 if dep <= 8 else 3)
-        dd = _lognormal_diam(rng, median=1.5 * {1: 5.5, 2: 3.0, 3: 1.0}[ctype])
+        dd = _lognormal_diam(rng, median=1.5 * ({1: 5.5, 2: 3.0, 3: 1.0}[ctype] if taper else 1.0))
         rows[i] = [i, pi, x, y, z, dd, ctype]
     rows[ncomp - 1] = [ncomp - 1, -1, 0.0, 0.0, 0.0, 29.8, 0]
     return rows

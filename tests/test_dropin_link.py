@@ -11,9 +11,11 @@ import subprocess
 
 import pytest
 
+import refsrc
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "cerebellum-neuron-model-simulation-using-rkc_gb300")
-REF = "/root/reference"
+REF = refsrc.reference_dir() or ""
 HEADERS = ["param.h", "go.cuh", "go_solve.cuh", "go_ion.cuh", "gr.cuh", "gr_solve.cuh", "gr_ion.cuh", "pkj.cuh",
            "pkj_solve.cuh", "pkj_ion.cuh", "io.cuh", "io_solve.cuh", "io_ion.cuh", "solve_bem.cuh",
            "solve_rkc.cuh", "syn.cuh", "gap.cuh", "output.cuh"]

@@ -9,10 +9,12 @@ import os
 import numpy as np
 import pytest
 
+import refsrc
+
 import connectivity as CN
 import morph as M
 
-REF = "/root/reference"
+REF = refsrc.reference_dir() or ""
 needs_ref = pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "Gr.txt")), reason="reference checkout not mounted")
 FILES = {"Gr.txt": (M.GR, 578), "Go_131.txt": (M.GO, 131), "Go_5.txt": (M.GO, 5), "Pkj.txt": (M.PKJ, 1600),
          "IO.txt": (M.IO, 3)}
