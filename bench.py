@@ -38,6 +38,10 @@ import numpy as np  # noqa: E402
 
 H_MAX = 0.125
 ALG_BYTES = {"mixed": 56, "fp64": 68}   # algorithmic bytes per compartment-update
+# the simulated window each workload's timed steps cover from t = 0: the
+# workloads' own durations (the sweep's systems run 100-1000 ms each; its
+# default window is their first 50 ms, when every system is still running)
+WINDOW_MS = {"mixed": 500.0, "screened": 500.0, "pkj3x3": 200.0, "sweep": 50.0}
 
 
 # Arm CPU part numbers (/proc/cpuinfo "CPU part", implementer 0x41)
@@ -122,17 +126,38 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ workloads
+STATED_DESC = ("mixed-type batch: 4096 GrC x4 + 1024 GoC x131 + 256 PC x1600 + IO 16x16 net x3, "
+               "step currents U[0,0.6] nA (olive: 0.6 nA over its dendrite, U[0,60] uA/cm^2) switched on at "
+               "U[0,20] ms, a distinct seeded tree per GoC and per PC, g_gap U[0.5,1.5] x nominal; one stated "
+               "deviation: PC dendrite diameters tapered by depth (main x5.5, smooth x3) -- untapered trees go "
+               "non-finite within ms in the reference's own frozen-current scheme")
+
+
 def workload(name, scale=1.0):
     import configs
-    if name == "mixed" and scale < 1.0:
+    if name == "mixed":
+        if scale < 1.0:
+            specs = configs.scaled_stated_batch(scale)
+            return specs, f"{STATED_DESC}; populations scaled x{scale:g} (small profiling case)"
+        return configs.stated_mixed_batch(), STATED_DESC
+    if name == "screened" and scale < 1.0:
         specs = configs.scaled_mixed_batch(scale)
         c = configs.type_counts(specs)
         return specs, (f"mixed-type batch scaled x{scale:g}: {c['gr'][0]} GrC x4 + {c['go'][0]} GoC x131 + "
                        f"{c['pkj'][0]} PC x1600 + IO 16x16 net x3 (small profiling case)")
-    if name == "mixed":
-        return configs.mixed_batch(), "mixed-type batch: 4096 GrC x4 + 1024 GoC x131 + 256 PC x1600 + IO 16x16 net x3"
+    if name == "screened":
+        return configs.mixed_batch(), ("mixed-type batch, screened: 4096 GrC x4 + 1024 GoC x131 (6 tree variants) + "
+                                       "256 PC x1600 (5 tapered trees) + IO 16x16 net x3; currents U[0,0.05] nA GrC, "
+                                       "U[0,0.4] nA GoC/PC, U[0,6] uA/cm^2 IO")
+    if name == "sweep":
+        return configs.sweep_batch(), ("parameter sweep: 32768 GrC x4 + 32768 GoC x131 (one seeded tree) independent "
+                                       "systems, every channel density x U[0.8,1.2] per instance, step current "
+                                       "U[0,0.4] nA from t = 0, durations U[100,1000] ms as per-system interval "
+                                       "budgets, no gap junctions")
     if name == "pkj3x3":
-        return configs.pkj_grid(3, 3), "Purkinje 3x3 grid, one RKC system, x-neighbour gap junctions, 0.5 nA"
+        return configs.pkj_grid(3, 3), ("Purkinje 3x3 grid, one RKC system of 14400 compartments (one seeded tapered "
+                                        "tree), x-neighbour gap junctions, constant 0.5 nA at every soma, the "
+                                        "reference's own initial jitter (srand(0)), plain FP64")
     raise SystemExit(f"unknown config {name}")
 
 
@@ -196,63 +221,187 @@ def run_network(args, G, configs, torch, precision, rank, world, dist):
         dist.destroy_process_group()
 
 
-# ------------------------------------------------------------ FP64 comparison
-def fp64_compare(G, configs, specs, n_iv, warmup, k, step_ms, step_units, flush, torch):
-    """Plain FP64 on the same systems and time window as the first k timed
-    mixed steps (throughput ratio), then the mixed precision's accuracy on
-    a 1/16 sample of the workload: max |V_mixed - V_fp64| over every
-    compartment after 1 ms and after 5 ms, and the device raster's spike
-    counts over 20 ms."""
-    eng = G.Engine(G.FP64)
-    configs.add_to(eng, specs)
-    eng.build()
-    t = 0.0
-    for _ in range(warmup):
-        eng.advance(t, n_iv, tolerate_retire=True)
-        t += n_iv * H_MAX
-    ms, units = 0.0, 0
-    for _ in range(k):
-        flush.zero_()
-        torch.cuda.synchronize()
-        u0 = eng.compartment_updates(-1)
-        eng.advance(t, n_iv, tolerate_retire=True)
-        t += n_iv * H_MAX
-        ms += eng.last_advance_ms()
-        units += eng.compartment_updates(-1) - u0
-    eng.close()
-    fp64 = units / (ms * 1e-3)
-    mixed = sum(step_units[:k]) / (sum(step_ms[:k]) * 1e-3)
-    sample = configs.scaled_mixed_batch(1.0 / 16)
+# ------------------------------------------------------------ helpers
+def type_runs(specs, ids):
+    """{cell type: (first system id, count, spec indices)}: every type's systems
+    are one consecutive run of ids (configs.add_to registers them in order)."""
+    runs = {}
+    for k, sp in enumerate(specs):
+        runs.setdefault(sp.cell_type, []).append(k)
+    out = {}
+    for ty, ks in runs.items():
+        first = ids[ks[0]]
+        if [ids[k] for k in ks] != list(range(first, first + len(ks))):
+            raise RuntimeError("systems of one type are not consecutive")
+        out[ty] = (first, len(ks), ks)
+    return out
+
+
+def cell_stim(specs, ks):
+    """Per-cell (comp, amp, t0, t1) arrays of the given specs, concatenated."""
+    cols = [[], [], [], []]
+    for k in ks:
+        sp = specs[k]
+        for j, dt in enumerate((np.int32, np.float64, np.float64, np.float64)):
+            cols[j].append(np.broadcast_to(np.asarray(sp.stim[j], dtype=dt), sp.n))
+    return tuple(np.ascontiguousarray(np.concatenate(c)) for c in cols)
+
+
+def apply_budgets(eng, specs, ids):
+    """Per-system interval budgets (spec.extra["n_intervals"]), where given."""
+    for sp, sid in zip(specs, ids):
+        n = sp.extra.get("n_intervals")
+        if n is not None:
+            eng.set_budget(sid, 1, int(n))
+
+
+def reset_to_start(eng, specs, ids):
+    """Refill every system with its own initial cell (same jitter, stimulus and
+    edge conductances): the state of a freshly built engine at t = 0, while
+    the engine keeps its launch tuning.  The initialisation launch runs here,
+    outside any timed region."""
+    for ty, (first, n, ks) in type_runs(specs, ids).items():
+        jit = np.concatenate([np.asarray(specs[k].jitter, dtype=np.float64) for k in ks])
+        gg = None
+        if all(specs[k].io_gap_g is not None for k in ks):
+            gg = np.concatenate([np.asarray(specs[k].io_gap_g, dtype=np.float64) for k in ks])
+        cc = None
+        if all(specs[k].cond_scale_ch is not None for k in ks):
+            cc = np.concatenate([np.asarray(specs[k].cond_scale_ch, dtype=np.float64).reshape(-1) for k in ks])
+        eng.reset_systems(first, n, jit, stim=cell_stim(specs, ks), io_gap_g=gg, cond_scale_ch=cc)
+    apply_budgets(eng, specs, ids)
+    eng.advance(0.0, 0, tolerate_retire=True)
+
+
+def stopped_systems(G, eng, specs, ids):
+    """The systems that stopped: spec index, shape tag, cell type, status bits."""
+    out = []
+    for ty, (first, n, ks) in type_runs(specs, ids).items():
+        st, _ = eng.run_status(first, n)
+        for j in np.nonzero(st)[0]:
+            k = ks[int(j)]
+            out.append({"index": k, "tag": specs[k].tag, "type": int(ty), "status": int(st[j]),
+                        "why": G.STATUS_BITS.get(int(st[j]) & 15, str(int(st[j])))})
+    return out
+
+
+RASTER_W = {0: 4, 3: 3}          # recorded compartments 0..w-1 per cell (granule, olive)
+RASTER_AT = {0: 3, 1: 0, 2: 0, 3: 2}   # raster compartment within the record
+
+
+def raster_traces(eng, n_iv):
+    """Per cell type, [interval][cell] values of each cell's raster compartment
+    at the interval ends (the soma record, widened for granule and olive)."""
+    out = {}
+    for ty in range(4):
+        nc = eng.type_cells(ty)
+        if nc == 0:
+            continue
+        w = RASTER_W.get(ty, 1)
+        buf = np.empty((n_iv, nc, w), np.float64)
+        eng.read_soma_type(ty, n_iv, buf)
+        out[ty] = buf[:, :, RASTER_AT[ty]]
+    return out
+
+
+def spike_times(trace, t0=0.0, thresh=None, ty=0):
+    """Threshold crossings of output_file's rule (value > threshold, previous
+    <= threshold; GrC/GoC/IO 10 mV, PC -10 mV; the first previous value is 100,
+    as main.cu:163-169), each timed by linear interpolation between the two
+    interval-end samples: per cell, the list of times."""
+    th = (-10.0 if ty == 2 else 10.0) if thresh is None else thresh
+    n_iv, nc = trace.shape
+    prev = np.concatenate([np.full((1, nc), 100.0), trace[:-1]])
+    up = (trace > th) & (prev <= th)
+    out = [[] for _ in range(nc)]
+    for k, c in zip(*np.nonzero(up)):
+        t1 = t0 + (k + 1) * H_MAX
+        if k == 0:
+            out[c].append(t1)          # crossing from the initial 100 mV sentinel: no interpolation
+            continue
+        a, b = prev[k, c], trace[k, c]
+        out[c].append(t1 - H_MAX + H_MAX * (th - a) / (b - a))
+    return out
+
+
+def compare_spikes(a, b):
+    """Spike counts and times of two runs (lists per cell)."""
+    equal = sum(1 for x, y in zip(a, b) if len(x) == len(y))
+    spiking = sum(1 for x, y in zip(a, b) if x or y)
+    dts = [abs(p - q) for x, y in zip(a, b) if len(x) == len(y) for p, q in zip(x, y)]
+    return {"spikes": [sum(len(x) for x in a), sum(len(y) for y in b)], "cells_spiking": spiking,
+            "cells_with_equal_counts": equal, "cells": len(a),
+            "max_spike_time_err_ms": max(dts) if dts else 0.0,
+            "spikes_within_0.05ms": (sum(1 for d in dts if d <= 0.05), len(dts))}
+
+
+# ------------------------------------------------------------ accuracy against FP64
+def accuracy_vs_fp64(G, configs, sample, horizon_ms=100.0, checkpoints=(1.0, 5.0, 20.0, 100.0)):
+    """Mixed precision against plain FP64 on a sample of the workload, from
+    t = 0, next to the FP64 sensitivity floor: the same FP64 run with every
+    cell's initial jitter moved by 1e-14 (its initial voltage by a few units in
+    the last place: V0 = V_init + 2..10 x jitter).  Both FP64 runs
+    share one engine (the perturbed copy is a second set of systems).  Reports
+    max |V - V_fp64| over every compartment at the checkpoints, and the
+    interpolated spike times of every cell (device raster rule) over the
+    horizon."""
+    import copy
+    pert = []
+    for sp in sample:
+        q = copy.copy(sp)
+        q.jitter = np.asarray(sp.jitter, dtype=np.float64) + 1e-14
+        pert.append(q)
+    n_iv = int(round(horizon_ms / H_MAX))
+    nsys = len(sample)
+    # FP64 engine: both copies, ordered by cell type (each type one run of
+    # ids), the unperturbed copy first within a type
+    combo = sorted([(sp.cell_type, 0, k) for k, sp in enumerate(sample)] +
+                   [(sp.cell_type, 1, k) for k, sp in enumerate(pert)])
     res = {}
-    for prec in (G.FP64, G.MIXED):
+    for name, prec in (("fp64", G.FP64), ("mixed", G.MIXED)):
+        keys = combo if name == "fp64" else [(sp.cell_type, 0, k) for k, sp in enumerate(sample)]
+        specs = [(sample if c == 0 else pert)[k] for _, c, k in keys]
         e = G.Engine(prec)
-        ids = configs.add_to(e, sample)
+        ids = configs.add_to(e, specs)
         e.build()
-        e.record_spikes(1 << 20)
-        v = []
-        tt = 0.0
-        for n in (8, 32, 120):          # to 1 ms, 5 ms, 20 ms
-            e.advance(tt, n, tolerate_retire=True)
-            tt += n * H_MAX
-            v.append(np.concatenate([e.read(i, G.F_VNEW) for i in ids]))
-        counts = {}
-        for ty in range(4):
-            _, sy, ce = e.read_spikes(ty)
-            for a, b in zip(sy.tolist(), ce.tolist()):
-                counts[(a, b)] = counts.get((a, b), 0) + 1
-        res[prec] = (v, counts, e.retired())
+        for ty, w in RASTER_W.items():
+            if e.type_cells(ty):
+                e.record_width(ty, w)
+        e.record_soma(n_iv)
+        v, t, done = [], 0.0, 0
+        for cp in checkpoints:
+            k = int(round(cp / H_MAX)) - done
+            e.advance(t, k, tolerate_retire=True)
+            t += k * H_MAX
+            done += k
+            by = {(c, kk): e.read(i, G.F_VNEW) for (_, c, kk), i in zip(keys, ids)}
+            v.append({c: np.concatenate([by[(c, kk)] for kk in range(nsys)]) for c in {c for _, c, _ in keys}})
+        tr = raster_traces(e, n_iv)
+        stop = [dict(x, copy=keys[x["index"]][1], index=keys[x["index"]][2]) for x in stopped_systems(G, e, specs, ids)]
+        res[name] = (v, tr, stop)
         e.close()
-    (v64, s64, r64), (v32, s32, r32) = res[G.FP64], res[G.MIXED]
-    return {"fp64_value": fp64, "mixed_value": mixed, "ratio": mixed / fp64, "steps": k,
-            "unit": "compartment-updates/s (same systems, same window)",
-            "accuracy_sample": "mixed batch x1/16 (256 GrC, 64 GoC, 16 PC, IO 16x16), from t = 0",
-            "max_abs_err_mv": {"1ms": float(np.max(np.abs(v32[0] - v64[0]))),
-                               "5ms": float(np.max(np.abs(v32[1] - v64[1]))),
-                               "20ms": float(np.max(np.abs(v32[2] - v64[2])))},
-            "spikes_20ms": {"fp64": sum(s64.values()), "mixed": sum(s32.values()),
-                            "cells_with_equal_counts": sum(1 for c in set(s64) | set(s32) if s64.get(c) == s32.get(c)),
-                            "cells_spiking": len(set(s64) | set(s32))},
-            "stopped_systems": {"fp64": r64, "mixed": r32}}
+    ncomp = sum(sp.nc for sp in sample)
+    v64 = [x[0] for x in res["fp64"][0]]
+    vpert = [x[1] for x in res["fp64"][0]]
+    v32 = [x[0] for x in res["mixed"][0]]
+    tr64, tr32 = res["fp64"][1], res["mixed"][1]
+    sp64, sppert, sp32 = [], [], []
+    for ty in sorted(tr64):
+        h = tr64[ty].shape[1] // 2
+        sp64 += spike_times(tr64[ty][:, :h], ty=ty)
+        sppert += spike_times(tr64[ty][:, h:], ty=ty)
+        sp32 += spike_times(tr32[ty], ty=ty)
+    out = {"sample": f"{nsys} systems, {ncomp} compartments, from t = 0 to {horizon_ms:g} ms",
+           "max_abs_err_mv": {f"{cp:g}ms": float(np.max(np.abs(a - b))) for cp, a, b in zip(checkpoints, v32, v64)},
+           "sensitivity_floor_mv": {f"{cp:g}ms": float(np.max(np.abs(a - b)))
+                                    for cp, a, b in zip(checkpoints, vpert, v64)},
+           "spikes_mixed_vs_fp64": compare_spikes(sp64, sp32),
+           "spikes_fp64_floor": compare_spikes(sp64, sppert),
+           "stopped": {"fp64": [x for x in res["fp64"][2] if x["copy"] == 0],
+                       "fp64_perturbed": [x for x in res["fp64"][2] if x["copy"] == 1],
+                       "mixed": res["mixed"][2]},
+           "floor": "the same FP64 run with every initial jitter + 1e-14 (V0 moved by a few units in the last place)"}
+    return out
 
 
 # ------------------------------------------------------------ serving
@@ -386,80 +535,159 @@ def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_sc
 
 
 # ------------------------------------------------------------ CPU side
-def _oracle_worker(args):
-    """Run a slice of a sampled workload in the oracle (reference arithmetic)."""
-    cfg, fraction, idx, t_begin, n_iv, warm_iv = args
+def _cpu_specs(cfg, fraction):
+    import configs
+    if cfg == "sweep":
+        return configs.sweep_batch(n_gr=max(1, int(32768 * fraction)), n_go=max(1, int(32768 * fraction)))
+    if cfg == "mixed":
+        return configs.scaled_stated_batch(fraction)
+    if cfg == "screened":
+        return configs.scaled_mixed_batch(fraction)
+    return workload(cfg)[0]
+
+
+def _oracle_worker(conn, cfg, fraction, idx):
+    """A process holding a slice of a workload sample in the oracle (reference
+    arithmetic, FP64) and advancing it on command: ("advance", t0, n) ->
+    (compartment-updates, seconds, systems stopped so far); ("reset",) rebuilds
+    the slice at t = 0; ("stop",).  A system whose step fails is stopped and
+    skipped from then on, as the GPU engine retires it."""
     sys.path.insert(0, PKG)
     sys.path.insert(0, ORACLE)
     import configs
     import oracle_py as O
-    specs = configs.scaled_mixed_batch(fraction) if cfg == "mixed" else configs.pkj_grid(3, 3)
-    systems = [(specs[i], configs.add_to_oracle(O, specs[i], canon=False)) for i in idx]
-    t = 0.0
-    for _ in range(warm_iv):
-        for sp, s in systems:
-            s.advance(t)
-        t += H_MAX
-    before = sum((s.stats()["stages"] + s.stats()["steps"]) * sp.nc for sp, s in systems)
-    t0 = time.perf_counter()
-    for _ in range(n_iv):
-        for sp, s in systems:
-            if s.advance(t) != 0:
-                raise RuntimeError("oracle step failed")
-        t += H_MAX
-    dt = time.perf_counter() - t0
-    after = sum((s.stats()["stages"] + s.stats()["steps"]) * sp.nc for sp, s in systems)
-    return after - before, dt
+    specs = _cpu_specs(cfg, fraction)
+
+    def build():
+        return [[specs[i], configs.add_to_oracle(O, specs[i], canon=False), True] for i in idx]
+
+    systems = build()
+    while True:
+        cmd = conn.recv()
+        if cmd[0] == "stop":
+            break
+        if cmd[0] == "reset":
+            systems = build()
+            conn.send(0)
+            continue
+        _, t, n = cmd
+        before = sum((s.stats()["stages"] + s.stats()["steps"]) * sp.nc for sp, s, _ in systems)
+        w0 = time.perf_counter()
+        for _ in range(n):
+            for rec in systems:
+                if rec[2] and rec[1].advance(t) != 0:
+                    rec[2] = False
+            t += H_MAX
+        dt = time.perf_counter() - w0
+        after = sum((s.stats()["stages"] + s.stats()["steps"]) * sp.nc for sp, s, _ in systems)
+        conn.send((after - before, dt, sum(1 for r in systems if not r[2])))
 
 
-def cpu_sample(cfg, fraction, n_iv, warm_iv, workers):
-    """Time the oracle on a bounded, proportional sample of the workload."""
-    import configs
-    specs = configs.scaled_mixed_batch(fraction) if cfg == "mixed" else configs.pkj_grid(3, 3)
-    order = sorted(range(len(specs)), key=lambda i: -specs[i].nc)
-    slices = [order[k::workers] for k in range(workers)]
-    jobs = [(cfg, fraction, sl, 0.0, n_iv, warm_iv) for sl in slices if sl]
-    if workers == 1:
-        res = [_oracle_worker(j) for j in jobs]
-    else:
+class OraclePool:
+    """Worker processes (spawned) over a proportional sample of a workload;
+    systems dealt out largest first."""
+
+    def __init__(self, cfg, fraction, workers):
         import multiprocessing as mp
-        with mp.get_context("spawn").Pool(len(jobs)) as pool:
-            res = pool.map(_oracle_worker, jobs)
-    units = sum(r[0] for r in res)
-    wall = max(r[1] for r in res)
-    counts = configs.type_counts(specs)
-    desc = ", ".join(f"{v[0]} {k}" for k, v in counts.items())
-    return units, wall, f"{desc}; {n_iv} intervals ({n_iv * H_MAX:g} ms) after {warm_iv} warm-up intervals"
+        specs = _cpu_specs(cfg, fraction)
+        order = sorted(range(len(specs)), key=lambda i: -specs[i].nc)
+        slices = [order[k::workers] for k in range(workers)]
+        ctx = mp.get_context("spawn")
+        self.conns, self.procs = [], []
+        for sl in slices:
+            if not sl:
+                continue
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_oracle_worker, args=(b, cfg, fraction, sl), daemon=True)
+            p.start()
+            self.conns.append(a)
+            self.procs.append(p)
+        self.specs = specs
+
+    def advance(self, t, n):
+        """Advance every slice n intervals from t in parallel: (units, wall s, stopped)."""
+        w0 = time.perf_counter()
+        for c in self.conns:
+            c.send(("advance", t, n))
+        res = [c.recv() for c in self.conns]
+        return sum(r[0] for r in res), time.perf_counter() - w0, sum(r[2] for r in res)
+
+    def reset(self):
+        for c in self.conns:
+            c.send(("reset",))
+        for c in self.conns:
+            c.recv()
+
+    def close(self):
+        for c in self.conns:
+            c.send(("stop",))
+        for p in self.procs:
+            p.join(timeout=10)
+
+    def describe(self):
+        import configs
+        counts = configs.type_counts(self.specs)
+        return ", ".join(f"{v[0]} {k}" for k, v in counts.items())
+
+
+def cpu_baseline_single(args):
+    """The oracle on one host thread, on a small sample of the same workload
+    from t = 0, for about --cpu-seconds."""
+    frac = {"mixed": 1.0 / 256, "screened": 1.0 / 256, "sweep": 1.0 / 4096}.get(args.config, 1.0)
+    pool = OraclePool(args.config, frac, 1)
+    try:
+        units, wall, n_iv = 0, 0.0, 0
+        probe_u, probe_w, _ = pool.advance(0.0, 2)
+        per_iv = max(probe_w / 2, 1e-4)
+        n = int(max(4, min(4000, args.cpu_seconds / per_iv)))
+        pool.reset()
+        units, wall, stopped = pool.advance(0.0, n)
+    finally:
+        pool.close()
+    return {"value": units / wall, "unit": "compartment-updates/s", "cores": 1, "kind": "port",
+            "cpu": cpu_model(), "nproc": os.cpu_count(),
+            "sample": f"{pool.describe()}; [0, {n * H_MAX:g}] ms (oracle, reference arithmetic, FP64, one thread)"}
 
 
 def run_reference(args):
-    """The reference arm: the CPU restatement of the reference's RKC path (the
-    reference's own CUDA code cannot travel: its sources are not part of this
-    repository), on all host cores, over a bounded sample of the workload."""
+    """The reference arm: the reference's RKC path restated on the CPU (the
+    oracle, reference arithmetic, FP64) on all host cores, over a
+    proportional sample of the same workload and the same window [0, window]
+    split into the same K steps.  Warm-up steps advance one interval each;
+    the sample is then rebuilt at t = 0.  Rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     cores = os.cpu_count() or 1
     cfg = args.config
-    fraction = 1.0 / 16 if cfg == "mixed" else 1.0
-    n_iv = 8 if cfg == "mixed" else 4
-    vals = []
-    for k in range(args.warmup + args.steps):
-        units, wall, sample = cpu_sample(cfg, fraction, n_iv, 0, cores)
-        if k >= args.warmup:
-            vals.append((units, wall))
-    units = sum(u for u, _ in vals)
-    wall = sum(w for _, w in vals)
+    window = args.window_ms
+    n_iv = int(round(window / args.steps / H_MAX))
+    frac = {"mixed": 1.0 / 16, "screened": 1.0 / 16, "sweep": 1.0 / 256}.get(cfg, 1.0)
+    pool = OraclePool(cfg, frac, cores)
+    try:
+        for k in range(args.warmup):
+            pool.advance(k * H_MAX, 1)
+        pool.reset()
+        units, wall, stopped = 0, 0.0, 0
+        for k in range(args.steps):
+            u, w, stopped = pool.advance(k * n_iv * H_MAX, n_iv)
+            units += u
+            wall += w
+        desc = pool.describe()
+    finally:
+        pool.close()
     v = units / wall
     _, wl = workload(cfg)
     out = {"impl": "reference", "metric": "compartment-updates/s", "value": v, "unit": "compartment-updates/s",
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1e3 * wall / max(1, len(vals)), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded morphologies and stimuli)",
-           "config": {"workload": wl, "precision": "fp64 (reference arithmetic)"},
+           "ms_per_step": 1e3 * wall / max(1, args.steps), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded morphologies, jitter and step currents)",
+           "config": config_key(args, wl),
            "cpu_baseline": {"value": v, "unit": "compartment-updates/s", "cores": cores, "kind": "port",
                             "cpu": cpu_model(),
-                            "sample": sample},
+                            "sample": f"{desc} (x{frac:g} of every population); the same window in the same "
+                                      f"{args.steps} steps; {stopped} systems stopped; oracle, reference "
+                                      "arithmetic, FP64"},
            "e2e": {"value": v, "unit": "compartment-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -508,11 +736,16 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbrkc", choices=["gbrkc", "reference"])
-    ap.add_argument("--config", default="mixed", choices=["mixed", "pkj3x3", "serve", "network"])
+    ap.add_argument("--config", default="mixed",
+                    choices=["mixed", "screened", "pkj3x3", "sweep", "serve", "network"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"])
-    ap.add_argument("--step-ms", type=float, default=5.0)
+    ap.add_argument("--window-ms", type=float, default=None,
+                    help="simulated window timed from t = 0, split into the steps (default: the workload's own, "
+                         "500 ms mixed, 200 ms pkj3x3)")
+    ap.add_argument("--step-ms", type=float, default=5.0, help="network workload: simulated ms per step")
+    ap.add_argument("--accuracy-ms", type=float, default=100.0, help="horizon of the mixed-vs-FP64 accuracy sample")
+    ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population fraction of the mixed batch (small profiling cases; 1 = the benchmark)")
@@ -524,6 +757,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.window_ms is None:
+        args.window_ms = WINDOW_MS.get(args.config, 500.0)
     if args.impl == "reference":
         run_reference(args)
         return
@@ -551,41 +786,100 @@ def main():
             dist.destroy_process_group()
         return
     specs, wl = workload(args.config, args.scale)
-    eng = G.Engine(G.MIXED if precision == "mixed" else G.FP64)
-    configs.add_to(eng, specs)
+    out = run_batch(args, G, configs, torch, specs, wl, precision, rank, world, dist)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_batch(args, G, configs, torch, specs, wl, precision, rank, world, dist):
+    """The batch workloads (mixed, pkj3x3): a fixed simulated window from t = 0,
+    split into the timed steps.
+
+    Warm-up: W steps of the same length from t = 0 (kernel loading, clocks, the
+    engine's CTA split between cell types settles); then every system is
+    refilled with its own initial cell (reset_to_start), so the K timed steps
+    cover exactly [0, window] whatever K is.  Each timed step, end to end
+    through the C ABI: upload every cell's stimulus table from pinned host
+    memory, advance one launch (device time from CUDA events on its stream:
+    `value`), read back every cell's recorded compartments of every interval
+    into pinned host memory (`e2e` = host wall time of the whole step).  L2 is
+    flushed (a 256 MB write) before each step, outside both timings."""
+    window = args.window_ms
+    n_iv = int(round(window / args.steps / H_MAX))
+    if n_iv < 1 or abs(n_iv * args.steps * H_MAX - window) > 1e-9:
+        raise SystemExit(f"--window-ms {window} is not {args.steps} steps of whole 0.125 ms intervals")
+    step_ms = n_iv * H_MAX
+    prec = G.MIXED if precision == "mixed" else G.FP64
+    eng = G.Engine(prec)
+    ids = configs.add_to(eng, specs)
     t_setup = time.perf_counter()
     eng.build()
+    apply_budgets(eng, specs, ids)
     setup_s = time.perf_counter() - t_setup
-    n_iv = int(round(args.step_ms / H_MAX))
+    eng.record_soma(n_iv)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+    # pinned host buffers: per type the stimulus table (inputs) and the soma record (outputs)
+    bufs = {}
+    for ty, (first, n, ks) in type_runs(specs, ids).items():
+        nc = eng.type_cells(ty)
+        stim = cell_stim(specs, ks)
+        pins = [torch.empty(nc, dtype=torch.int32 if j == 0 else torch.float64, pin_memory=True) for j in range(4)]
+        for p, a in zip(pins, stim):
+            p.numpy()[:] = a
+        soma = torch.empty((n_iv, nc), dtype=torch.float64, pin_memory=True)
+        bufs[ty] = (pins, soma)
+    h2d = sum(p[0].numel() * 4 + 3 * p[1].numel() * 8 for p, _ in bufs.values())
+    d2h = sum(sm.numel() * 8 for _, sm in bufs.values())
+
+    def step(t):
+        for ty, (pins, soma) in bufs.items():
+            eng.set_stim_type(ty, *(p.numpy() for p in pins))
+        eng.rewind_soma()
+        eng.advance(t, n_iv, tolerate_retire=True)
+        for ty, (pins, soma) in bufs.items():
+            eng.read_soma_type(ty, n_iv, soma.numpy())
+
     t = 0.0
     for _ in range(args.warmup):
-        eng.advance(t, n_iv, tolerate_retire=True)
-        t += n_iv * H_MAX
+        step(t)
+        t += step_ms
+    # granule systems per warp, measured on a replay of the next 1 ms
+    tune_s = time.perf_counter()
+    lanes = eng.autotune(t, 8)
+    tune_s = time.perf_counter() - tune_s
+    reset_to_start(eng, specs, ids)
     torch.cuda.synchronize()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
-    dev_ms, kern_ms = 0.0, {k: 0.0 for k in range(4)}
-    step_ms, step_units = [], []
+    dev_ms, e2e_s, kern_ms = 0.0, 0.0, {k: 0.0 for k in range(4)}
+    step_ms_dev, step_units, retired_at = [], [], []
+    stop_ms = {}             # spec index -> end of the timed step after which it was found stopped
     units0 = eng.compartment_updates(-1)
     units_t0 = {k: eng.compartment_updates(k) for k in range(4)}
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
-    wall0 = time.perf_counter()
-    for _ in range(args.steps):
+    t = 0.0
+    for k in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         u0 = eng.compartment_updates(-1)
-        eng.advance(t, n_iv, tolerate_retire=True)
-        t += n_iv * H_MAX
+        w0 = time.perf_counter()
+        step(t)
+        e2e_s += time.perf_counter() - w0
+        t += step_ms
         dev_ms += eng.last_advance_ms()
-        step_ms.append(eng.last_advance_ms())
+        step_ms_dev.append(eng.last_advance_ms())
         step_units.append(eng.compartment_updates(-1) - u0)
-        for k in range(4):
-            kern_ms[k] += eng.last_kernel_ms(k)
+        if eng.retired() > (retired_at[-1] if retired_at else 0):
+            for x in stopped_systems(G, eng, specs, ids):
+                stop_ms.setdefault(x["index"], t)
+        retired_at.append(eng.retired())
+        for ty in range(4):
+            kern_ms[ty] += eng.last_kernel_ms(ty)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
     if dist is not None:
         dist.barrier()
     clk = clocks.stop()
@@ -594,174 +888,111 @@ def main():
     t_max_ms = barrier_max(dist, dev_ms)
     units_all = barrier_sum(dist, units)
     value = units_all / (t_max_ms * 1e-3)
+    e2e_value = units_all / barrier_max(dist, e2e_s)
     persistent, role_ctas = eng.launch_layout()
-    if persistent:
-        launches = args.steps
-    else:
-        launches = args.steps * sum(1 for k in range(4) if eng.type_cells(k) > 0)
-
-    # roofline of the dominant kernel: the one persistent launch, or the
-    # longest per-type launch
+    launches = args.steps if persistent else args.steps * sum(1 for k in range(4) if eng.type_cells(k) > 0)
+    stopped = stopped_systems(G, eng, specs, ids)
+    for x in stopped:
+        x["stopped_by_ms"] = stop_ms.get(x["index"])
+    n_compartments = eng.total_compartments()
     names = {0: "gr", 1: "go", 2: "pkj", 3: "io"}
     peak, peak_kind = peaks()
     bpu = ALG_BYTES[precision]
     if persistent:
         kname, key = "k_mega", "mega"
-        per_launch_units = units / args.steps
-        per_launch_ms = dev_ms / args.steps
+        per_launch_units, per_launch_ms = units / args.steps, dev_ms / args.steps
     else:
         dom = max(range(4), key=lambda k: kern_ms[k])
         kname, key = f"k_advance<{names[dom]}>", names[dom]
-        per_launch_units = units_t[dom] / args.steps
-        per_launch_ms = kern_ms[dom] / args.steps
-    per_launch_bytes = bpu * per_launch_units
-    achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
-    traffic = None
+        per_launch_units, per_launch_ms = units_t[dom] / args.steps, kern_ms[dom] / args.steps
+    achieved = bpu * per_launch_units / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
+    traffic, fp64_ncu = None, None
     tfile = os.path.join(ROOT, "profiles", f"traffic_{args.config}_{precision}.json")
     if os.path.exists(tfile):
         try:
             tr = json.load(open(tfile))
-            # bytes per compartment-update from one capture, scaled to this launch
             if key in tr:
-                traffic = tr[key] * per_launch_units
+                traffic = tr[key] * per_launch_units     # DRAM bytes per update from one capture, scaled
+            fp64_ncu = tr.get("fp64_pipe_active")
         except Exception:
-            traffic = None
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "kernel": kname,
-                "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_update": bpu,
+            pass
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": kname, "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_update": bpu,
                 "role_ms_per_step" if persistent else "kernel_ms_per_step":
                     {names[k]: kern_ms[k] / args.steps for k in range(4)}}
     if persistent:
         roofline["role_ctas"] = {names[k]: role_ctas[k] for k in range(4)}
-    # what bounds the kernel instead: the FP64 pipe, as ncu reported it for the
-    # same kernel (profiles/), beside the HBM fraction above
-    if os.path.exists(tfile):
-        try:
-            tr = json.load(open(tfile))
-            if "fp64_pipe_active" in tr:
-                roofline["fp64_pipe_active_ncu"] = tr["fp64_pipe_active"]
-        except Exception:
-            pass
+    if fp64_ncu is not None:
+        roofline["fp64_pipe_active_ncu"] = fp64_ncu
+    eng.close()
+    del flush
 
-    # end to end through the C ABI with host buffers: per step, upload every
-    # cell's stimulus table -- the workload's own protocol, so the dynamics
-    # match the device-timed steps -- (pinned host -> device) and read back
-    # every cell's soma voltage at every interval (device -> pinned host)
-    e2e = None
-    if not args.no_e2e:
-        # a second engine with the same systems runs the same warm-up and
-        # steps, so e2e covers exactly the device-timed work plus the copies
-        eng.close()
-        eng = G.Engine(G.MIXED if precision == "mixed" else G.FP64)
-        configs.add_to(eng, specs)
-        eng.build()
-        ncell = {k: eng.type_cells(k) for k in range(4)}
-        eng.record_soma(n_iv)
-        bufs = {}
-        cell_specs = {k: [] for k in range(4)}
-        for s in specs:
-            cell_specs[s.cell_type].append(s)
-        for k in range(4):
-            if ncell[k] == 0:
-                continue
-            comp = torch.empty(ncell[k], dtype=torch.int32, pin_memory=True)
-            amp, t0v, t1v = (torch.empty(ncell[k], dtype=torch.float64, pin_memory=True) for _ in range(3))
-            cs, am, a0, a1 = [], [], [], []
-            for s in cell_specs[k]:
-                cs.append(np.broadcast_to(np.asarray(s.stim[0]), s.n))
-                am.append(np.broadcast_to(np.asarray(s.stim[1], dtype=np.float64), s.n))
-                a0.append(np.broadcast_to(np.asarray(s.stim[2], dtype=np.float64), s.n))
-                a1.append(np.broadcast_to(np.asarray(s.stim[3], dtype=np.float64), s.n))
-            comp.numpy()[:] = np.concatenate(cs)
-            amp.numpy()[:] = np.concatenate(am)
-            t0v.numpy()[:] = np.concatenate(a0)
-            t1v.numpy()[:] = np.concatenate(a1)
-            soma = torch.empty((n_iv, ncell[k]), dtype=torch.float64, pin_memory=True)
-            bufs[k] = (comp, amp, t0v, t1v, soma)
-        h2d = sum(b[0].numel() * 4 + 3 * b[1].numel() * 8 for b in bufs.values())
-        d2h = sum(b[4].numel() * 8 for b in bufs.values())
-        t = 0.0
-
-        def e2e_step(t):
-            for k, (comp, amp, t0v, t1v, soma) in bufs.items():
-                eng.set_stim_type(k, comp.numpy(), amp.numpy(), t0v.numpy(), t1v.numpy())
-            eng.rewind_soma()
-            eng.advance(t, n_iv, tolerate_retire=True)
-            for k, (comp, amp, t0v, t1v, soma) in bufs.items():
-                eng.read_soma_type(k, n_iv, soma.numpy())
-
-        for _ in range(args.warmup):
-            e2e_step(t)
-            t += n_iv * H_MAX
-        e_units0 = eng.compartment_updates(-1)
-        torch.cuda.synchronize()
-        w0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step(t)
-            t += n_iv * H_MAX
-        torch.cuda.synchronize()
-        e_wall = time.perf_counter() - w0
-        e_units = eng.compartment_updates(-1) - e_units0
-        e_wall = barrier_max(dist, e_wall)
-        e_units = barrier_sum(dist, e_units)
-        e2e = {"value": e_units / e_wall, "unit": "compartment-updates/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "timing": "host wall clock incl. pinned copies"}
-
-    n_compartments, n_retired = eng.total_compartments(), eng.retired()
-
-    # the same systems in plain FP64 over the first timed steps (same warm-up),
-    # and the mixed precision's voltage error and spike counts against FP64
+    # plain FP64 on the same systems over the first steps of the same window
     vs_fp64 = None
-    if precision == "mixed" and rank == 0 and not args.no_fp64_compare and args.config == "mixed":
-        eng.close()
-        vs_fp64 = fp64_compare(G, configs, specs, n_iv, args.warmup, min(3, args.steps), step_ms, step_units,
-                               flush, torch)
+    if precision == "mixed" and rank == 0 and not args.no_fp64_compare:
+        k = max(1, args.steps // 5)
+        e = G.Engine(G.FP64)
+        ids64 = configs.add_to(e, specs)
+        e.build()
+        apply_budgets(e, specs, ids64)
+        for _ in range(args.warmup):
+            e.advance(0.0, min(n_iv, 40), tolerate_retire=True)
+        reset_to_start(e, specs, ids64)
+        ms64, u64 = 0.0, 0
+        for j in range(k):
+            u0 = e.compartment_updates(-1)
+            e.advance(j * step_ms, n_iv, tolerate_retire=True)
+            ms64 += e.last_advance_ms()
+            u64 += e.compartment_updates(-1) - u0
+        e.close()
+        mixed_v = sum(step_units[:k]) / (sum(step_ms_dev[:k]) * 1e-3)
+        vs_fp64 = {"fp64_value": u64 / (ms64 * 1e-3), "mixed_value": mixed_v, "ratio": mixed_v / (u64 / (ms64 * 1e-3)),
+                   "window_ms": [0.0, k * step_ms], "unit": "compartment-updates/s (same systems, same window)"}
+        if args.config in ("mixed", "screened", "sweep") and not args.no_accuracy:
+            sample = {"mixed": lambda: configs.scaled_stated_batch(1.0 / 16),
+                      "screened": lambda: configs.scaled_mixed_batch(1.0 / 16),
+                      "sweep": lambda: configs.sweep_batch(n_gr=512, n_go=512)}[args.config]()
+            vs_fp64["accuracy"] = accuracy_vs_fp64(G, configs, sample, horizon_ms=args.accuracy_ms)
     serving = None
     n_serve = 48 if args.serve_requests is None else args.serve_requests
-    if n_serve > 0 and rank == 0 and args.config == "mixed":
-        eng.close()
+    if n_serve > 0 and rank == 0 and args.config in ("mixed", "screened"):
         serving = run_serve(G, precision, n_serve, slots_scale=args.serve_slots)
-
     cpu = None
     if not args.no_cpu and rank == 0:
-        # bounded single-thread sample of the same workload in the oracle
-        frac = 1.0 / 256 if args.config == "mixed" else 1.0
-        probe_units, probe_wall, _ = cpu_sample(args.config, frac, 2, 0, 1)
-        per_iv = max(probe_wall / 2, 1e-3)
-        n_cpu = int(max(4, min(4000, args.cpu_seconds / per_iv)))
-        units_c, wall_c, sample = cpu_sample(args.config, frac, n_cpu, 0, 1)
-        cpu = {"value": units_c / wall_c, "unit": "compartment-updates/s", "cores": 1, "kind": "port",
-               "cpu": cpu_model(), "nproc": os.cpu_count(),
-               "sample": sample + " (oracle, reference arithmetic, FP64, one thread)"}
+        cpu = cpu_baseline_single(args)
+    counts = configs.type_counts(specs)
+    cfg = config_key(args, wl)
+    res = {"metric": "compartment-updates/s", "value": value, "unit": "compartment-updates/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": t_max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64 state+stages, f32 gating" if precision == "mixed" else "f64",
+           "data": "synthetic (seeded morphologies, jitter and step currents)",
+           "config": cfg,
+           "run": {"precision": precision, "cells": {k: v[0] for k, v in counts.items()},
+                   "compartments": n_compartments, "l2": "flushed (256 MB write) before each timed step",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU", "setup_s": round(setup_s, 2),
+                   "sim_ms_per_wall_s": window / (t_max_ms * 1e-3), "units_per_step": units / args.steps,
+                   "units_per_step_list": step_units, "stopped_systems": len(stopped),
+                   "autotune": {"granule_systems_per_warp": lanes, "seconds": round(tune_s, 2),
+                                "how": "the launch after the warm-up replayed for 1 ms with 32, 16 and 8 "
+                                       "granule systems per warp from a device snapshot; fastest kept"},
+                   "stopped": stopped[:64]},
+           "roofline": roofline, "gpu_launches": launches, "clocks": clk,
+           "e2e": {"value": e2e_value, "unit": "compartment-updates/s", "h2d_bytes_per_step": h2d,
+                   "d2h_bytes_per_step": d2h,
+                   "timing": "host wall clock of each timed step: stimulus upload (pinned), launch, soma read-back"}}
+    if serving:
+        res["serving"] = serving
+    if vs_fp64:
+        res["vs_plain_fp64"] = vs_fp64
+    if cpu:
+        res["cpu_baseline"] = cpu
+    return res
 
-    if rank == 0:
-        counts = configs.type_counts(specs)
-        out = {"metric": "compartment-updates/s", "value": value, "unit": "compartment-updates/s",
-               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-               "ms_per_step": t_max_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f64 state+stages, f32 gating" if precision == "mixed" else "f64",
-               "data": "synthetic (seeded morphologies, jitter and step currents)",
-               "config": {"workload": wl, "precision": precision, "step_sim_ms": args.step_ms,
-                          "cells": {k: v[0] for k, v in counts.items()},
-                          "compartments": n_compartments,
-                          "l2": "flushed (256 MB write) between timed steps",
-                          "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                          "setup_s": round(setup_s, 2), "wall_s": round(wall, 3),
-                          "retired_systems": n_retired,
-                          "sim_ms_per_wall_s": args.steps * args.step_ms / (t_max_ms * 1e-3),
-                          "units_per_step": units / args.steps},
-               "roofline": roofline, "gpu_launches": launches, "clocks": clk}
-        if e2e:
-            out["e2e"] = e2e
-        if serving:
-            out["serving"] = serving
-        if vs_fp64:
-            out["vs_plain_fp64"] = vs_fp64
-        if cpu:
-            out["cpu_baseline"] = cpu
-        print(json.dumps(out))
-    if dist is not None:
-        dist.destroy_process_group()
+
+def config_key(args, wl):
+    """The workload description shared by this arm's line and the reference arm's."""
+    return {"workload": wl, "window_ms": [0.0, args.window_ms], "step_sim_ms": args.window_ms / args.steps}
 
 
 if __name__ == "__main__":

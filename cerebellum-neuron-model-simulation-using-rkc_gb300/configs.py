@@ -45,6 +45,7 @@ class Spec:
     gj_pairs: Optional[np.ndarray] = None
     io_gap_g: Optional[np.ndarray] = None
     tol: float = 0.0
+    cond_scale_ch: Optional[np.ndarray] = None   # per cell and channel density factors
     tag: str = ""
     extra: dict = field(default_factory=dict)
 
@@ -62,6 +63,22 @@ def _jitter(rng, n):
     return rng.uniform(-0.5, 0.5, n)
 
 
+def reference_jitter(cell_type: int, n: int, seed: int = 0) -> np.ndarray:
+    """The reference's own initial jitter of n cells of one type: libc srand
+    (seed) then one rand() per cell, (rand() + 1) / (RAND_MAX + 2) - 0.5 for
+    GrC and PC (gr_ion.cu:642, pkj_ion.cu:367), rand() / RAND_MAX - 0.5 for
+    GoC and IO (go_ion.cu:598, io_ion.cu:172), as a run of main.cu (srand(0)
+    at main.cu:38) with only this type draws it."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.srand(ctypes.c_uint(seed))
+    rand_max = 2147483647.0   # glibc RAND_MAX
+    r = np.array([libc.rand() for _ in range(n)], dtype=np.float64)
+    if cell_type in (M.GR, M.PKJ):
+        return ((r + 1.0) / (rand_max + 2.0)) - 0.5
+    return (r / rand_max) - 0.5
+
+
 # Purkinje trees whose cells stay finite for 500 ms at 0.1-0.4 nA under the
 # reference's frozen-current splitting, in FP64 and in mixed precision
 # (screened on the GPU); Golgi tree variants likewise.
@@ -69,13 +86,16 @@ PKJ_STABLE_SEEDS = (7, 8, 9, 12, 13)
 GO_STABLE_VARIANTS = (0, 1, 3, 5, 6, 7)
 
 
-def pkj_grid(nx=3, ny=3, seed=2, amp=0.5e-3, tree_seed=None, gap=True):
-    """Reference-style Purkinje grid (one RKC system); the tree is the first
-    screened-stable one unless given."""
-    rng = np.random.default_rng(seed)
+def pkj_grid(nx=3, ny=3, seed=2, amp=0.5e-3, tree_seed=None, gap=True, jitter="reference"):
+    """Reference-style Purkinje grid (one RKC system) of one seeded synthetic
+    tree (PKJ_STABLE_SEEDS[0] unless given), a constant somatic current.  The
+    initial jitter is the reference's own rand() sequence (srand(0)), so its
+    CUDA build runs exactly this system from the same model file; with
+    jitter="seeded" it is drawn from numpy with seed."""
     rows = M.pkj_synthetic(tree_seed if tree_seed is not None else PKJ_STABLE_SEEDS[0])
     n = nx * ny
-    return [Spec(M.PKJ, nx, ny, rows, _jitter(rng, n), stim=(rows.shape[0] - 1, amp, 0.0, 1e9),
+    jit = reference_jitter(M.PKJ, n) if jitter == "reference" else _jitter(np.random.default_rng(seed), n)
+    return [Spec(M.PKJ, nx, ny, rows, jit, stim=(rows.shape[0] - 1, amp, 0.0, 1e9),
                  gap=gap, gj_pairs=M.PKJ_GJ_PAIRS, tag=f"pkj{nx}x{ny}")]
 
 
@@ -115,10 +135,78 @@ def mixed_batch(seed=2, n_gr=4096, n_go=1024, n_pkj=256, io_side=16, amp_max=Non
     return specs
 
 
+# The mixed batch's per-type current bounds as its specification states them
+# (U[0, 0.6] nA for every cell), in each model's units: mA for GrC / GoC / PC;
+# for the olive, whose injected current is a density (uA/cm^2, io.cu:247),
+# 0.6 nA = 6e-4 uA over its dendrite's lateral area (pi x 6 um x 53.07 um =
+# 1.0e-5 cm^2): 60 uA/cm^2.
+IO_DEND_AREA_CM2 = np.pi * 6.0e-4 * 53.07e-4
+STATED_AMP = {M.GR: 0.6e-3, M.GO: 0.6e-3, M.PKJ: 0.6e-3, M.IO: 0.6e-3 / IO_DEND_AREA_CM2}
+
+
+def stated_mixed_batch(seed=2, n_gr=4096, n_go=1024, n_pkj=256, io_side=16):
+    """The mixed batch with the stated currents (STATED_AMP), a distinct seeded
+    Golgi tree per Golgi cell and a distinct seeded Purkinje tree per Purkinje
+    cell (tapered diameters: untapered trees go non-finite within
+    milliseconds under the reference's frozen-current splitting, in its own
+    build too)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    gr_rows = M.gr_reduced4()
+    for i in range(n_gr):
+        specs.append(Spec(M.GR, 1, 1, gr_rows, _jitter(rng, 1),
+                          stim=(1, rng.uniform(0, STATED_AMP[M.GR]), rng.uniform(0, 20.0), 1e9), tag="gr"))
+    for i in range(n_go):
+        rows = M.go_synthetic(seed * 100000 + i)
+        specs.append(Spec(M.GO, 1, 1, rows, _jitter(rng, 1),
+                          stim=(30, rng.uniform(0, STATED_AMP[M.GO]), rng.uniform(0, 20.0), 1e9), tag=f"go#{i}"))
+    for i in range(n_pkj):
+        rows = M.pkj_synthetic(seed * 100000 + i)
+        specs.append(Spec(M.PKJ, 1, 1, rows, _jitter(rng, 1),
+                          stim=(rows.shape[0] - 1, rng.uniform(0, STATED_AMP[M.PKJ]), rng.uniform(0, 20.0), 1e9),
+                          tag=f"pkj#{i}"))
+    if io_side > 0:
+        n = io_side * io_side
+        specs.append(Spec(M.IO, io_side, io_side, M.io_rows(), _jitter(rng, n),
+                          stim=(np.zeros(n, np.int32), rng.uniform(0, STATED_AMP[M.IO], n), rng.uniform(0, 20.0, n),
+                                np.full(n, 1e9)),
+                          gap=True, io_gap_g=G_C_IO * rng.uniform(0.5, 1.5, 4 * n), tag="io"))
+    return specs
+
+
+def scaled_stated_batch(fraction: float, seed=2):
+    """stated_mixed_batch with every population but the olive network scaled
+    (bounded CPU samples and accuracy samples)."""
+    return stated_mixed_batch(seed=seed, n_gr=max(1, int(4096 * fraction)), n_go=max(1, int(1024 * fraction)),
+                              n_pkj=max(1, int(256 * fraction)), io_side=16)
+
+
 def scaled_mixed_batch(fraction: float, seed=2):
     """The mixed batch with every population scaled (for bounded CPU samples)."""
     return mixed_batch(seed=seed, n_gr=max(1, int(4096 * fraction)), n_go=max(1, int(1024 * fraction)),
                        n_pkj=max(1, int(256 * fraction)), io_side=16)
+
+
+def sweep_batch(seed=4, n_gr=32768, n_go=32768, amp_max=0.4e-3, ts_ms=(100.0, 1000.0)):
+    """Parameter-sweep batch: n_gr reduced granule cells and n_go Golgi cells
+    (one seeded tree), every instance its own RKC system, no gap junctions.
+    Each instance scales every channel density by its own U[0.8, 1.2]
+    (cond_scale_ch, the per-compartment conductances the reference builds
+    from its model rows, gr.cu:31-35, go.cu:33-38), takes a step current
+    U[0, amp_max] switched on at t = 0 at the reference's stimulated
+    compartment, and runs for its own duration U[ts_ms] (whole intervals,
+    kept in spec.extra["n_intervals"]: the engine's per-system interval
+    budget)."""
+    rng = np.random.default_rng(seed)
+    gr_rows, go_rows = M.gr_reduced4(), M.go_synthetic(seed * 1000)
+    specs = []
+    for t, n, rows, comp, ncond in ((M.GR, n_gr, gr_rows, 1, 10), (M.GO, n_go, go_rows, 30, 13)):
+        for i in range(n):
+            sp = Spec(t, 1, 1, rows, _jitter(rng, 1), stim=(comp, rng.uniform(0, amp_max), 0.0, 1e9),
+                      cond_scale_ch=rng.uniform(0.8, 1.2, ncond), tag="gr" if t == M.GR else "go")
+            sp.extra["n_intervals"] = int(round(rng.uniform(*ts_ms) / 0.125))
+            specs.append(sp)
+    return specs
 
 
 @dataclass
@@ -274,13 +362,15 @@ def add_to(engine, specs):
     ids = []
     for s in specs:
         ids.append(engine.add_system(s.cell_type, s.nx, s.ny, s.rows, s.jitter, stim=s.stim,
-                                     gj_pairs=s.gj_pairs, gap=s.gap, io_gap_g=s.io_gap_g, tol=s.tol))
+                                     gj_pairs=s.gj_pairs, gap=s.gap, io_gap_g=s.io_gap_g, tol=s.tol,
+                                     cond_scale_ch=s.cond_scale_ch))
     return ids
 
 
 def add_to_oracle(O, s: Spec, canon=False):
     sysm = O.System(s.cell_type, s.nx, s.ny, s.rows, s.jitter, stim=s.stim, gj_pairs=s.gj_pairs,
-                    io_gap=s.gap, go_gj=s.gap, pkj_gj=s.gap, io_gap_g=s.io_gap_g, tol=s.tol, canon=canon)
+                    io_gap=s.gap, go_gj=s.gap, pkj_gj=s.gap, io_gap_g=s.io_gap_g, tol=s.tol, canon=canon,
+                    cond_scale_ch=s.cond_scale_ch)
     rc = sysm.init()
     if rc != 0:
         raise RuntimeError(f"oracle init failed ({rc})")

@@ -83,6 +83,7 @@ struct HostSystem {
   std::vector<int> stim_comp;
   std::vector<double> stim_amp, stim_t0, stim_t1;
   std::vector<double> cond_scale;             // per cell, empty: 1
+  std::vector<double> cond_scale_ch;          // per cell and channel (replaces cond_scale), empty: none
   double tol, hmin;
   bool idle = false;                          // a free slot until reset
   // built
@@ -353,6 +354,7 @@ static void coef_table(int mmax, std::vector<double> &coef, std::vector<long> &o
 // ----------------------------------------------------------------- pools
 struct DeviceMem {
   std::vector<void *> ptrs;
+  std::vector<size_t> sizes;   // bytes of each allocation (gbrkc_autotune's snapshots)
   ~DeviceMem() {
     for (void *p : ptrs) cudaFree(p);
   }
@@ -362,6 +364,7 @@ struct DeviceMem {
     cudaError_t e = cudaMalloc((void **)d, bytes);
     if (e != cudaSuccess) return fail(GBRKC_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
     ptrs.push_back(*d);
+    sizes.push_back(bytes);
     if (!h.empty()) {
       e = cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
       if (e != cudaSuccess) return fail(GBRKC_ECUDA, "cudaMemcpy: %s", cudaGetErrorString(e));
@@ -553,6 +556,11 @@ static int add_system_impl(gbrkc_engine *E, const gbrkc_system_desc *d, int *sys
     for (double x : S.cond_scale)
       if (!(x >= 0.0) || !std::isfinite(x)) return fail(GBRKC_EINVAL, "conductance scale must be finite and >= 0");
   }
+  if (d->cond_scale_ch) {
+    S.cond_scale_ch.assign(d->cond_scale_ch, d->cond_scale_ch + (size_t)S.n * NCOND[S.type]);
+    for (double x : S.cond_scale_ch)
+      if (!(x >= 0.0) || !std::isfinite(x)) return fail(GBRKC_EINVAL, "conductance scale must be finite and >= 0");
+  }
   S.idle = d->idle != 0;
   S.tol = d->tol > 0 ? d->tol : TOL_DEFAULT[S.type];
   S.hmin = d->hmin > 0 ? d->hmin : pow(2.0, (double)HMIN_LOG2_DEFAULT[S.type]);
@@ -654,7 +662,9 @@ void fill_state(gbrkc_engine *E, PoolHost &P, const HostSystem &S, long off, int
   for (int i = 0; i < S.nc; i++) {
     const int j = i % S.ncomp, cell = i / S.ncomp;
     const long g = off + i;
-    if (S.cond_scale.empty()) {
+    if (!S.cond_scale_ch.empty()) {
+      for (int k = 0; k < ncond; k++) P.cond[(size_t)k * nc + g] = T.cond[k][j] * S.cond_scale_ch[(size_t)cell * ncond + k];
+    } else if (S.cond_scale.empty()) {
       for (int k = 0; k < ncond; k++) P.cond[(size_t)k * nc + g] = T.cond[k][j];
     } else {
       for (int k = 0; k < ncond; k++) P.cond[(size_t)k * nc + g] = T.cond[k][j] * S.cond_scale[cell];
@@ -1508,6 +1518,101 @@ extern "C" int gbrkc_advance(gbrkc_engine *E, double t0, int n_iv) {
 
 extern "C" int gbrkc_retired_systems(gbrkc_engine *E) { return E ? E->n_retired : 0; }
 
+// ------------------------------------------------------- gbrkc_autotune
+// Granule systems run one per lane; how many lanes of a warp take systems
+// (cells per warp, hence per CTA) trades divergence -- a warp runs the union
+// of its lanes' step-attempt paths -- against warps, i.e. CTAs taken from the
+// other roles.  The best count depends on the workload's dynamics and mix,
+// so it is measured: the same launch (t0, n_iv, from the engine's present
+// state) runs once per candidate, twice each, from a device snapshot of the
+// engine, and the fastest candidate is kept.  Scheduling never changes a
+// system's arithmetic, so every candidate computes the same bits; the state,
+// the CTA split between roles and the soma / spike records are restored
+// afterwards, so the call leaves the simulation where it found it.
+namespace {
+
+struct Snapshot {
+  std::vector<void *> dev;
+  std::vector<std::pair<void *, size_t>> src;
+  ~Snapshot() {
+    for (void *p : dev) cudaFree(p);
+  }
+  int take(void *p, size_t n) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, n);
+    if (e != cudaSuccess) return fail(GBRKC_ENOMEM, "autotune snapshot: %s", cudaGetErrorString(e));
+    dev.push_back(q);
+    src.push_back({p, n});
+    e = cudaMemcpy(q, p, n, cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) return fail(GBRKC_ECUDA, "autotune snapshot: %s", cudaGetErrorString(e));
+    return 0;
+  }
+  int restore() const {
+    for (size_t k = 0; k < dev.size(); k++) {
+      cudaError_t e = cudaMemcpy(src[k].first, dev[k], src[k].second, cudaMemcpyDeviceToDevice);
+      if (e != cudaSuccess) return fail(GBRKC_ECUDA, "autotune restore: %s", cudaGetErrorString(e));
+    }
+    return 0;
+  }
+};
+
+int autotune_impl(gbrkc_engine *E, double t0, int n_iv, int *lanes_out) {
+  if (!E || n_iv <= 0 || !lanes_out) return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  if (E->sv.n > 0) return fail(GBRKC_EINVAL, "engines with synapses are not tuned");
+  *lanes_out = E->lanes;
+  if (!E->mega || E->role_ctas[GR] == 0) return 0;      // no granule lanes to tune
+  int rc;
+  if (E->pending_init) {
+    // systems reset since the last advance: initialise them first, as the
+    // next advance would
+    if ((rc = launch_all(E, t0, 0, E->soma_iv, 1))) return rc;
+    E->pending_init = false;
+  }
+  Snapshot S;
+  for (size_t k = 0; k < E->mem.ptrs.size(); k++)
+    if ((rc = S.take(E->mem.ptrs[k], E->mem.sizes[k]))) return rc;
+  for (auto &P : E->pools)
+    if (P.d_spk_log && P.spk_cap > 0 && (rc = S.take(P.d_spk_log, (size_t)P.spk_cap * sizeof(SpikeRec)))) return rc;
+  int ctas[NTYPES], warps = E->gr_warps, lanes0 = E->lanes;
+  double work[NTYPES];
+  for (int t = 0; t < NTYPES; t++) { ctas[t] = E->role_ctas[t]; work[t] = E->role_work[t]; }
+  const long active = E->gr_active;
+  auto restore_host = [&]() {
+    for (int t = 0; t < NTYPES; t++) { E->role_ctas[t] = ctas[t]; E->role_work[t] = work[t]; }
+    E->gr_warps = warps;
+    E->gr_active = active;
+  };
+  for (int t = 0; t < NTYPES; t++) {
+    E->pools[t].vd.soma_out = nullptr;     // the records are not written while tuning
+    E->pools[t].vf.soma_out = nullptr;
+  }
+  static const int cand[] = {32, 16, 8};
+  int best = lanes0;
+  double best_ms = 1e300;
+  for (int c : cand) {
+    for (int rep = 0; rep < 2; rep++) {
+      if ((rc = S.restore())) return rc;
+      restore_host();
+      E->lanes = c;
+      fit_granule_warps(E);
+      if ((rc = launch_all(E, t0, n_iv, E->soma_iv, 0))) return rc;
+      if (E->last_ms < best_ms) { best_ms = E->last_ms; best = c; }
+    }
+  }
+  if ((rc = S.restore())) return rc;
+  restore_host();
+  E->lanes = best;
+  *lanes_out = best;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int gbrkc_autotune(gbrkc_engine *E, double t0, int n_iv, int *lanes_out) {
+  return no_throw([&] { return autotune_impl(E, t0, n_iv, lanes_out); });
+}
+
 extern "C" int gbrkc_read(gbrkc_engine *E, int id, int field, int k, double *host, long n) {
   PoolHost *P = nullptr;
   HostSystem *S = nullptr;
@@ -1867,6 +1972,11 @@ static int systems_reset_impl(gbrkc_engine *E, int first_id, int n, const gbrkc_
         const double x = d->cond_scale[cells + c];
         if (!(x >= 0.0) || !std::isfinite(x)) return fail(GBRKC_EINVAL, "conductance scale must be finite and >= 0");
       }
+      if (d->cond_scale_ch)
+        for (int q = 0; q < NCOND[S.type]; q++) {
+          const double x = d->cond_scale_ch[(size_t)(cells + c) * NCOND[S.type] + q];
+          if (!(x >= 0.0) || !std::isfinite(x)) return fail(GBRKC_EINVAL, "conductance scale must be finite and >= 0");
+        }
     }
     if (d->io_gap_g && S.type == IO && !S.gap_pre.empty()) {
       // same edges, new conductances (gap.cu:4-120)
@@ -1897,6 +2007,10 @@ static int systems_reset_impl(gbrkc_engine *E, int first_id, int n, const gbrkc_
     }
     if (d->cond_scale) S.cond_scale.assign(d->cond_scale + cells, d->cond_scale + cells + S.n);
     else S.cond_scale.clear();
+    if (d->cond_scale_ch)
+      S.cond_scale_ch.assign(d->cond_scale_ch + (size_t)cells * NCOND[S.type],
+                             d->cond_scale_ch + (size_t)(cells + S.n) * NCOND[S.type]);
+    else S.cond_scale_ch.clear();
     if (d->io_gap_g && S.type == IO && !S.gap_pre.empty()) {
       S.io_gap_g.assign(d->io_gap_g + 4 * cells, d->io_gap_g + 4 * (cells + S.n));
       S.gap_g = std::move(new_gap_g[k]);

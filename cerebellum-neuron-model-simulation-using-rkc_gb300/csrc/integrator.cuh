@@ -652,7 +652,7 @@ struct Sys {
     }
     // err^(1/3), shared by the reject and accept paths (one evaluation per
     // attempt whichever way the lanes of a warp go)
-    const double cr = cm_pow(err, 1.0 / 3.0);
+    const double cr = cm_cbrt(err);
     if (err > 1.0) {
       c.absh = 0.8 * c.absh / cr;
       c.n_rej++;

@@ -284,7 +284,7 @@ struct LaneSys {
       c.status |= ST_NAN;
       return Sys<CT, R, BlockTeam>::ATT_FAIL;
     }
-    const double cr = cm_pow(err, 1.0 / 3.0);
+    const double cr = cm_cbrt(err);
     if (err > 1.0) {
       c.absh = 0.8 * c.absh / cr;
       c.n_rej++;

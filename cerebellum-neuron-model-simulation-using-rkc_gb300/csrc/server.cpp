@@ -253,6 +253,7 @@ static int server_add_class_impl(gbrkc_server *S, const gbrkc_slot_class *c, int
   C->shape.stim_comp = nullptr;
   C->shape.stim_amp = C->shape.stim_t0 = C->shape.stim_t1 = nullptr;
   C->shape.cond_scale = nullptr;
+  C->shape.cond_scale_ch = nullptr;
   C->shape.idle = 1;
   C->slots_req = c->slots;
   C->share = c->share;

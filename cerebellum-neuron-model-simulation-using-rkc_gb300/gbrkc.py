@@ -31,6 +31,7 @@ class SystemDesc(C.Structure):
         ("stim_amp", C.POINTER(C.c_double)), ("stim_t0", C.POINTER(C.c_double)),
         ("stim_t1", C.POINTER(C.c_double)), ("tol", C.c_double), ("hmin", C.c_double),
         ("cond_scale", C.POINTER(C.c_double)), ("idle", C.c_int),
+        ("cond_scale_ch", C.POINTER(C.c_double)),
     ]
 
 
@@ -66,6 +67,7 @@ class ResetDesc(C.Structure):
         ("stim_amp", C.POINTER(C.c_double)), ("stim_t0", C.POINTER(C.c_double)),
         ("stim_t1", C.POINTER(C.c_double)), ("cond_scale", C.POINTER(C.c_double)),
         ("io_gap_g", C.POINTER(C.c_double)), ("n_intervals", C.c_int),
+        ("cond_scale_ch", C.POINTER(C.c_double)),
     ]
 
 
@@ -123,6 +125,7 @@ def lib() -> C.CDLL:
         L.gbrkc_rewind_soma.argtypes = [P]
         L.gbrkc_record_width.argtypes = [P, C.c_int, C.c_int]
         L.gbrkc_retired_systems.argtypes = [P]
+        L.gbrkc_autotune.argtypes = [P, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.gbrkc_launch_layout.argtypes = [P, C.POINTER(C.c_int)]
         L.gbrkc_compartment_updates.argtypes = [P, C.c_int]
         L.gbrkc_compartment_updates.restype = C.c_longlong
@@ -196,7 +199,7 @@ class Engine:
             pass
 
     def add_system(self, cell_type, nx, ny, rows, jitter, stim=None, gj_pairs=None, gap=True,
-                   io_gap_g=None, tol=0.0, hmin=0.0, cond_scale=None, idle=False) -> int:
+                   io_gap_g=None, tol=0.0, hmin=0.0, cond_scale=None, idle=False, cond_scale_ch=None) -> int:
         n = nx * ny
         rows = np.ascontiguousarray(rows, dtype=np.float64)
         jitter = np.ascontiguousarray(jitter, dtype=np.float64)
@@ -226,6 +229,10 @@ class Engine:
             d.cond_scale = _dp(cs)
             keep.append(cs)
         d.idle = int(idle)
+        if cond_scale_ch is not None:
+            cc = np.ascontiguousarray(cond_scale_ch, dtype=np.float64).reshape(-1)
+            d.cond_scale_ch = _dp(cc)
+            keep.append(cc)
         sid = C.c_int()
         _check(lib().gbrkc_add_system(self.h, C.byref(d), C.byref(sid)))
         self._keep.append(keep)
@@ -233,7 +240,7 @@ class Engine:
         return sid.value
 
     def reset_systems(self, first: int, n: int, jitter, stim=None, cond_scale=None, io_gap_g=None,
-                      n_intervals: int = -1):
+                      n_intervals: int = -1, cond_scale_ch=None):
         """Refill systems first .. first+n-1 (one run of one type) with new cells of the same shape."""
         jitter = np.ascontiguousarray(jitter, dtype=np.float64)
         cells = jitter.size
@@ -254,6 +261,10 @@ class Engine:
             gg = np.ascontiguousarray(io_gap_g, dtype=np.float64)
             d.io_gap_g = _dp(gg)
             keep.append(gg)
+        if cond_scale_ch is not None:
+            cc = np.ascontiguousarray(cond_scale_ch, dtype=np.float64).reshape(-1)
+            d.cond_scale_ch = _dp(cc)
+            keep.append(cc)
         d.n_intervals = n_intervals
         _check(lib().gbrkc_systems_reset(self.h, first, n, C.byref(d)))
 
@@ -349,6 +360,13 @@ class Engine:
 
     def retired(self) -> int:
         return lib().gbrkc_retired_systems(self.h)
+
+    def autotune(self, t0: float, n_intervals: int) -> int:
+        """Time the next launch with 32, 16 and 8 granule systems per warp (the
+        state is restored after each) and keep the fastest; returns it."""
+        lanes = C.c_int()
+        _check(lib().gbrkc_autotune(self.h, t0, n_intervals, C.byref(lanes)))
+        return lanes.value
 
     def nc(self, sid: int) -> int:
         return lib().gbrkc_system_nc(self.h, sid)

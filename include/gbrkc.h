@@ -67,6 +67,10 @@ typedef struct gbrkc_system_desc {
                                (no counterpart in the reference: its densities are fixed) */
   int idle;                 /* nonzero: a free slot -- neither initialised nor advanced
                                until gbrkc_systems_reset fills it */
+  const double *cond_scale_ch; /* nx*ny*NCOND factors, one per channel density of each
+                               cell in the type's conductance order (GrC 10, GoC 13,
+                               PC 11, IO 8), replacing cond_scale; or NULL (no
+                               counterpart in the reference) */
 } gbrkc_system_desc;
 
 /* Create an engine on the current CUDA device.  precision: GBRKC_FP64 (plain
@@ -92,6 +96,20 @@ int gbrkc_build(gbrkc_engine *e);
 int gbrkc_advance(gbrkc_engine *e, double t0, int n_intervals);
 /* Number of retired systems so far. */
 int gbrkc_retired_systems(gbrkc_engine *e);
+
+/* Measure and keep the best number of granule systems per warp (cells per
+ * warp, hence per CTA, of the persistent launch): the launch that
+ * gbrkc_advance(e, t0, n_intervals) would make runs once per candidate (32,
+ * 16, 8 lanes; twice each, the shorter time counts) from a device snapshot
+ * of the engine, and the fastest is kept for the following advances.  The
+ * engine's state, its CTA split between cell types and its soma / spike
+ * records are restored, so the simulation is where it was; results never
+ * depend on the choice (scheduling only).  Allocates the snapshot (the
+ * engine's device footprint) for the duration of the call.  Engines with
+ * synapses are refused.  *lanes_out receives the kept count (unchanged
+ * when the engine has no granule lanes).  No counterpart in the reference,
+ * whose launch shape is fixed at 128 threads (gr_solve.cu:198-199). */
+int gbrkc_autotune(gbrkc_engine *e, double t0, int n_intervals, int *lanes_out);
 
 /* Copy n values of a per-compartment field of one system to host memory. */
 int gbrkc_read(gbrkc_engine *e, int sys_id, int field, int k, double *host, long n);
@@ -251,6 +269,7 @@ typedef struct gbrkc_reset_desc {
   const double *cond_scale; /* per cell, or NULL (1) */
   const double *io_gap_g;   /* IO networks: 4 per cell, or NULL (keep) */
   int n_intervals;          /* budget from now on; -1: none */
+  const double *cond_scale_ch; /* per cell and channel (as gbrkc_system_desc), or NULL */
 } gbrkc_reset_desc;
 
 /* Reset systems first_id .. first_id+n-1, which must be consecutive systems

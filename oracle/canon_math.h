@@ -19,12 +19,13 @@
  *   pow: exp(y log x) for x >= 0.
  *
  * The canonical step-size controller evaluates err^(1/3) once per step with
- * cm_pow, takes err^(2/3) as its square and reuses the cube root of the
- * previous error (the reference calls pow three times, solve_rkc.cu:1038-1051).
+ * cm_cbrt (below), takes err^(2/3) as its square and reuses the cube root of
+ * the previous error (the reference calls pow three times,
+ * solve_rkc.cu:1038-1051).
  *
  * Measured error against the exact result (tests/test_canon_math.py): exp
- * within 0.76 ulp, log within 1.8 ulp, pow(x, 1/3) within 7 ulp over the
- * controller's range.  The CUDA product carries its own copy of the same
+ * within 0.76 ulp, log within 1.8 ulp, pow(x, 1/3) within 7 ulp, cm_cbrt
+ * within 4 ulp over the controller's range.  The CUDA product carries its own copy of the same
  * algorithm (csrc/canon_math.cuh); the GPU parity tests, bit-exact through
  * whole trajectories, check that the two agree.  Compile with
  * -ffp-contract=off: every fma here is explicit.
@@ -101,5 +102,48 @@ static inline double cm_log(double x) {
 }
 
 static inline double cm_pow(double x, double y) { return cm_exp(y * cm_log(x)); }
+
+#define CM_FN static inline
+/* Cube root for the step-size controller's err^(1/3), err >= 0.
+ * x = 2^e m with m in [1, 2); e = 3q + r (r = 0, 1, 2) and z = 2^r m in
+ * [1, 8), so cbrt(x) = 2^q cbrt(z).  The reciprocal cube root y = z^(-1/3)
+ * is seeded in FP32 by a least-squares quadratic in z (relative error below
+ * 0.09), refined by three FP32 Newton steps y <- y (4 - z y^3) / 3 (error
+ * ~3e-7, the FP32 rounding level) and two FP64 steps Y <- Y + Y (1 - Z Y^3)/3
+ * (quadratic convergence: below 1e-25 before rounding); then
+ * cbrt(z) = Z Y Y and the exact scaling by 2^q.  No division.  Every
+ * operation is written out (FP32 products unfused, FP64 fma explicit), so
+ * host and device give the same bits.  Measured against 60-digit
+ * arithmetic: within 4 ulp, 0.7 ulp on average (tests/test_canon_math.py).  0, +inf and NaN
+ * return themselves. */
+CM_FN double cm_cbrt(double x) {
+  if (!(x > 0.0) || x == HUGE_VAL) return x;
+  int e = 0;
+  if (x < 0x1p-1022) { x *= 0x1p54; e = -54; }
+  const uint64_t u = cm_bits(x);
+  e += (int)((u >> 52) & 0x7ff) - 1023;
+  const int q = (e >= 0) ? e / 3 : -((2 - e) / 3);
+  const int r = e - 3 * q;
+  const double Z = cm_from_bits((u & 0x000fffffffffffffULL) | ((uint64_t)(1023 + r) << 52));
+  const float zf = (float)Z;
+  float y = 0x1.0b5c7ap+0f;
+  y = y + (-0x1.1bfbb8p-3f) * zf;
+  y = y + (0x1.2a6c02p-7f) * zf * zf;
+  for (int k = 0; k < 3; k++) {
+    const float y3 = y * y * y;
+    const float t = 4.0f - zf * y3;
+    y = (y * t) * 0x1.555556p-2f;
+  }
+  double Y = (double)y;
+  for (int k = 0; k < 2; k++) {
+    const double Y3 = (Y * Y) * Y;
+    const double d = fma(-Z, Y3, 1.0);
+    Y = fma(Y * d, 0x1.5555555555555p-2, Y);
+  }
+  const double c = (Z * Y) * Y;
+  return c * cm_from_bits((uint64_t)(q + 1023) << 52);
+}
+#undef CM_FN
+
 
 #endif

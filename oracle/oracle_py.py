@@ -28,7 +28,7 @@ class Desc(C.Structure):
         ("io_gap_g", C.POINTER(C.c_double)),
         ("tol", C.c_double), ("hmin", C.c_double),
         ("io_gap", C.c_int), ("go_gj", C.c_int), ("pkj_gj", C.c_int),
-        ("canon", C.c_int), ("cond_scale", C.POINTER(C.c_double)),
+        ("canon", C.c_int), ("cond_scale", C.POINTER(C.c_double)), ("cond_scale_ch", C.POINTER(C.c_double)),
     ]
 
 
@@ -83,6 +83,8 @@ def lib() -> C.CDLL:
             getattr(L, f).argtypes = [C.c_double]
         L.orc_cm_pow.restype = C.c_double
         L.orc_cm_pow.argtypes = [C.c_double, C.c_double]
+        L.orc_cm_cbrt.restype = C.c_double
+        L.orc_cm_cbrt.argtypes = [C.c_double]
         L.orc_ion_update.argtypes = [P, C.POINTER(C.c_double), C.c_double]
         L.orc_update_b.argtypes = [P, C.POINTER(C.c_double)]
         L.orc_set_elem_v.argtypes = [P, C.POINTER(C.c_double)]
@@ -134,7 +136,7 @@ class System:
 
     def __init__(self, cell_type, nx, ny, rows, jitter, stim=None, gj_pairs=None,
                  tol=0.0, hmin=0.0, io_gap=True, go_gj=True, pkj_gj=True, io_gap_g=None,
-                 canon=False, cond_scale=None):
+                 canon=False, cond_scale=None, cond_scale_ch=None):
         L = lib()
         self._keep = []
         rows = np.ascontiguousarray(rows, dtype=np.float64)
@@ -168,6 +170,10 @@ class System:
             cs = np.ascontiguousarray(np.broadcast_to(cond_scale, n), dtype=np.float64)
             d.cond_scale = _dp(cs)
             self._keep.append(cs)
+        if cond_scale_ch is not None:
+            cc = np.ascontiguousarray(cond_scale_ch, dtype=np.float64).reshape(-1)
+            d.cond_scale_ch = _dp(cc)
+            self._keep.append(cc)
         self.h = L.orc_create(C.byref(d))
         if not self.h:
             raise RuntimeError("orc_create failed")

@@ -418,6 +418,7 @@ long long orc_pivot_swaps(void) { return g_pivot_swaps; }
 double orc_cm_exp(double x) { return cm_exp(x); }
 double orc_cm_log(double x) { return cm_log(x); }
 double orc_cm_pow(double x, double y) { return cm_pow(x, y); }
+double orc_cm_cbrt(double x) { return cm_cbrt(x); }
 
 static int pivot_solve(int n, double *A /* n*n row-major */, double *bvec) {
   for (int i = 0; i < n - 1; i++) {
@@ -1169,7 +1170,11 @@ orc_sys *orc_create(const orc_desc *d) {
   }
   alloc_state(s);
   if (setup_cells(s, d) != 0) { orc_destroy(s); return NULL; }
-  if (d->cond_scale)
+  if (d->cond_scale_ch)
+    for (int i = 0; i < s->nc; i++)
+      for (int k = 0; k < s->ncond; k++)
+        s->cond[k][i] = s->cond[k][i] * d->cond_scale_ch[(size_t)(i / s->ncomp) * s->ncond + k];
+  else if (d->cond_scale)
     for (int i = 0; i < s->nc; i++)
       for (int k = 0; k < s->ncond; k++) s->cond[k][i] = s->cond[k][i] * d->cond_scale[i / s->ncomp];
   /* the reference computes the initial gating on the host with libm
@@ -1505,7 +1510,7 @@ static void rkclow(orc_sys *s) {
     if (s->canon) {
       /* canonical: err^(1/3) once; err^(2/3) as its square; errold^(1/3)
        * carried over from the previous accepted step */
-      const double cr = cm_pow(err, 1.0 / 3.0);
+      const double cr = cm_cbrt(err);
       if (s->naccpt == 1) {
         temp2 = cr;
         if (0.8 < fac * temp2) fac = 0.8 / temp2;

@@ -54,6 +54,8 @@ typedef struct {
                           the GPU plain-FP64 path; 0 = the reference's literal expressions */
   const double *cond_scale; /* n factors on every channel density of a cell, NULL = 1
                           (synthetic variation; the reference's densities are fixed) */
+  const double *cond_scale_ch; /* n*ncond factors, one per channel density of each cell
+                          (replaces cond_scale), or NULL */
 } orc_desc;
 
 orc_sys *orc_create(const orc_desc *d);
@@ -104,6 +106,7 @@ long long orc_pivot_swaps(void);
 double orc_cm_exp(double x);
 double orc_cm_log(double x);
 double orc_cm_pow(double x, double y);
+double orc_cm_cbrt(double x);
 
 /* static setup, for the setup pins: Cm, area, cond k, shell, CSR */
 const double *orc_cm(const orc_sys *s);

@@ -83,3 +83,19 @@ def test_special_values(O):
     assert O.cm_log(math.inf) == math.inf
     assert O.cm_exp(0.0) == 1.0
     assert O.cm_log(1.0) == 0.0
+
+
+def test_cbrt_accuracy(O):
+    """The controller's err^(1/3): within 4 ulp of the exact cube root over
+    the error norms the controller sees, and exact at 0, inf and NaN."""
+    rng = np.random.default_rng(3)
+    xs = list(10.0 ** rng.uniform(-12, 6, 3000)) + [1.0, 8.0, 0.125, 2.0, 3.0, 1e-300, 1e-310, 5e-324, 1e300]
+    worst = 0.0
+    for x in xs:
+        got = O.lib().orc_cm_cbrt(float(x))
+        exact = Decimal(float(x)) ** (Decimal(1) / Decimal(3))
+        worst = max(worst, float(ulp_err(got, exact)))
+    assert worst <= 4.0, worst
+    assert O.lib().orc_cm_cbrt(0.0) == 0.0
+    assert O.lib().orc_cm_cbrt(math.inf) == math.inf
+    assert math.isnan(O.lib().orc_cm_cbrt(math.nan))

@@ -56,7 +56,7 @@ def test_two_rank_reductions():
 
 def test_reference_arm_runs_on_rank_zero_only():
     out = launch(["bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3",
-                  "--config", "pkj3x3"])
+                  "--config", "pkj3x3", "--window-ms", "0.5"])
     assert '"impl": "reference"' in out[0]
     assert out[1].strip() == ""
     import json
@@ -66,4 +66,5 @@ def test_reference_arm_runs_on_rank_zero_only():
         assert k in line, k
     assert line["n_gpus"] == 2 and line["steps"] == 1 and line["warmup"] == 3 and line["value"] > 0
     assert line["config"]["workload"] and line["cpu_baseline"]["kind"] == "port"
+    assert line["config"]["window_ms"] == [0.0, 0.5]
     assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
