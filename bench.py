@@ -40,8 +40,10 @@ H_MAX = 0.125
 ALG_BYTES = {"mixed": 56, "fp64": 68}   # algorithmic bytes per compartment-update
 # the simulated window each workload's timed steps cover from t = 0: the
 # workloads' own durations (the sweep's systems run 100-1000 ms each; its
-# default window is their first 50 ms, when every system is still running)
-WINDOW_MS = {"mixed": 500.0, "screened": 500.0, "pkj3x3": 200.0, "sweep": 50.0}
+# default window is their first 50 ms, when every system is still running;
+# the network's 1000 ms take minutes of host-timed launches, its default
+# window is its first 20 ms)
+WINDOW_MS = {"mixed": 500.0, "screened": 500.0, "pkj3x3": 200.0, "sweep": 50.0, "network": 20.0}
 
 
 # Arm CPU part numbers (/proc/cpuinfo "CPU part", implementer 0x41)
@@ -166,36 +168,91 @@ def run_network(args, G, configs, torch, precision, rank, world, dist):
     """The network workload: 2048 GrC, 512 GoC, 512 PC as independent systems
     coupled by 780 404 chemical synapses with delays (configs.network_batch).
     Network mode advances every system one interval per launch, then updates
-    every synapse; a step is --step-ms of simulated time, timed on the host
-    wall clock around the synchronous advance (launches included)."""
+    every synapse.  Warm-up steps run on a first engine; a fresh engine is
+    then timed over [0, window] (an engine with synapses cannot refill its
+    systems), on the host wall clock around the synchronous advances
+    (launches included).  The same window then runs in plain FP64 -- the
+    throughput ratio -- and in FP64 with every initial jitter moved by
+    1e-14, the floor for the mixed precision's voltage and spike-time
+    differences."""
     specs, groups = configs.network_batch()
-    eng = G.Engine(G.MIXED if precision == "mixed" else G.FP64)
-    configs.add_network(eng, specs, groups)
+    window = args.window_ms
+    n_iv = int(round(window / args.steps / H_MAX))
+    if n_iv < 1 or abs(n_iv * args.steps * H_MAX - window) > 1e-9:
+        raise SystemExit(f"--window-ms {window} is not {args.steps} steps of whole 0.125 ms intervals")
+    step_ms = n_iv * H_MAX
+    n_all = int(round(window / H_MAX))
+
+    def build(prec, sp=specs):
+        e = G.Engine(prec)
+        configs.add_network(e, sp, groups)
+        e.build()
+        return e
+
+    eng = build(G.MIXED if precision == "mixed" else G.FP64)
+    for k in range(args.warmup):
+        eng.advance(k * step_ms, n_iv, tolerate_retire=True)
+    eng.close()
     t0 = time.perf_counter()
-    eng.build()
+    eng = build(G.MIXED if precision == "mixed" else G.FP64)
     setup_s = time.perf_counter() - t0
-    n_iv = int(round(args.step_ms / H_MAX))
-    t = 0.0
-    for _ in range(args.warmup):
-        eng.advance(t, n_iv, tolerate_retire=True)
-        t += n_iv * H_MAX
+    for ty, w in RASTER_W.items():
+        eng.record_width(ty, w)
+    eng.record_soma(n_all)
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
-    u0 = eng.compartment_updates(-1)
     torch.cuda.synchronize()
     w0 = time.perf_counter()
-    for _ in range(args.steps):
-        eng.advance(t, n_iv, tolerate_retire=True)
-        t += n_iv * H_MAX
+    for k in range(args.steps):
+        eng.advance(k * step_ms, n_iv, tolerate_retire=True)
     torch.cuda.synchronize()
     wall = barrier_max(dist, time.perf_counter() - w0)
     clk = clocks.stop()
-    units = barrier_sum(dist, eng.compartment_updates(-1) - u0)
+    units = barrier_sum(dist, eng.compartment_updates(-1))
     nsyn = sum(len(g["post_system"]) for g in groups)
     n_spk = eng.read_synapses(G.SYNF_S0, nsyn)
+    ids = list(range(len(specs)))
+    stopped = stopped_systems(G, eng, specs, ids)
+    res = {"run": (np.concatenate([eng.vnew(i) for i in ids]), raster_traces(eng, n_all), stopped)}
+    eng.close()
     peak, peak_kind = peaks()
     bpu = ALG_BYTES[precision]
     achieved = bpu * units / wall / 1e9
+    vs_fp64 = None
+    if rank == 0 and precision == "mixed" and not args.no_fp64_compare:
+        import copy
+        pert = []
+        for sp in specs:
+            q = copy.copy(sp)
+            q.jitter = np.asarray(sp.jitter, dtype=np.float64) + 1e-14
+            pert.append(q)
+        walls = {}
+        for name, sp in (("fp64", specs), ("fp64_perturbed", pert)):
+            e = build(G.FP64, sp)
+            for ty, w in RASTER_W.items():
+                e.record_width(ty, w)
+            e.record_soma(n_all)
+            w1 = time.perf_counter()
+            e.advance(0.0, n_all, tolerate_retire=True)
+            walls[name] = (time.perf_counter() - w1, e.compartment_updates(-1))
+            res[name] = (np.concatenate([e.vnew(i) for i in ids]), raster_traces(e, n_all),
+                         stopped_systems(G, e, sp, ids))
+            e.close()
+        sp_of = {}
+        for name in ("run", "fp64", "fp64_perturbed"):
+            tr = res[name][1]
+            sp_of[name] = sum((spike_times(tr[ty], ty=ty) for ty in sorted(tr)), [])
+        fp64_v = walls["fp64"][1] / walls["fp64"][0]
+        vs_fp64 = {"fp64_value": fp64_v, "mixed_value": units / wall, "ratio": (units / wall) / fp64_v,
+                   "window_ms": [0.0, window], "unit": "compartment-updates/s (host wall clock, same window)",
+                   "accuracy": {"max_abs_err_mv": float(np.max(np.abs(res["run"][0] - res["fp64"][0]))),
+                                "sensitivity_floor_mv": float(np.max(np.abs(res["fp64_perturbed"][0] -
+                                                                            res["fp64"][0]))),
+                                "at_ms": window,
+                                "spikes_mixed_vs_fp64": compare_spikes(sp_of["fp64"], sp_of["run"]),
+                                "spikes_fp64_floor": compare_spikes(sp_of["fp64"], sp_of["fp64_perturbed"]),
+                                "stopped": {"fp64": res["fp64"][2], "fp64_perturbed": res["fp64_perturbed"][2]},
+                                "floor": "the same FP64 run with every initial jitter + 1e-14"}}
     if rank == 0:
         counts = configs.type_counts(specs)
         out = {"metric": "compartment-updates/s", "value": units / wall, "unit": "compartment-updates/s",
@@ -203,20 +260,23 @@ def run_network(args, G, configs, torch, precision, rank, world, dist):
                "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64 state+stages, f32 gating" if precision == "mixed" else "f64",
                "data": "synthetic (seeded cells, synapses, weights and delays)",
-               "config": {"workload": "network: 2048 GrC x4 + 512 GoC x131 + 512 PC x1600, 780404 synapses "
-                                      "(MF->GrC Poisson 5-50 Hz, GrC->GoC, GoC->GrC, GrC->PC), lognormal weights, "
-                                      "delays U[1,5] ms", "precision": precision, "step_sim_ms": args.step_ms,
-                          "cells": {k: v[0] for k, v in counts.items()}, "synapses": nsyn,
-                          "synapses_with_activity": int(np.count_nonzero(n_spk)),
-                          "retired_systems": eng.retired(), "setup_s": round(setup_s, 2),
-                          "timing": "host wall clock; one persistent launch and one synapse launch per interval",
-                          "sim_ms_per_wall_s": args.steps * args.step_ms / wall},
+               "config": {"workload": "network: 2048 GrC x4 + 512 GoC x131 + 512 PC x1600 (a distinct seeded tree "
+                                      "per GoC and per PC), 780404 synapses (MF->GrC Poisson 5-50 Hz, GrC->GoC, "
+                                      "GoC->GrC, GrC->PC), lognormal weights (sigma 0.25: at 0.5 the mossy-fibre "
+                                      "tail drives some granule cells non-finite), delays U[1,5] ms",
+                          "window_ms": [0.0, window], "step_sim_ms": step_ms},
+               "run": {"precision": precision, "cells": {k: v[0] for k, v in counts.items()}, "synapses": nsyn,
+                       "synapses_with_activity": int(np.count_nonzero(n_spk)), "stopped_systems": len(stopped),
+                       "stopped": stopped[:64], "setup_s": round(setup_s, 2),
+                       "timing": "host wall clock; one persistent launch and one synapse launch per interval",
+                       "sim_ms_per_wall_s": window / wall},
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": None, "kernel": "k_mega + k_syn_update",
                             "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_update": bpu},
                "gpu_launches": 2 * args.steps * n_iv, "clocks": clk}
+        if vs_fp64:
+            out["vs_plain_fp64"] = vs_fp64
         print(json.dumps(out))
-    eng.close()
     if dist is not None:
         dist.destroy_process_group()
 
@@ -405,7 +465,8 @@ def accuracy_vs_fp64(G, configs, sample, horizon_ms=100.0, checkpoints=(1.0, 5.0
 
 
 # ------------------------------------------------------------ serving
-def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_scale=1):
+def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_scale=1, ts_ms=(5.0, 25.0),
+              compare_ms=None):
     """Serve a Poisson request stream (configs.serve_workload) through the
     request server on the wall clock: requests are submitted when their
     arrival time has passed, every round admits what fits and advances all
@@ -414,7 +475,7 @@ def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_sc
     FP64 engine (build, advance, read back), for the throughput ratio and the
     served results' voltage error and spike counts against FP64."""
     import configs
-    classes, reqs = configs.serve_workload(n_requests, seed=seed, slots_scale=slots_scale)
+    classes, reqs = configs.serve_workload(n_requests, seed=seed, slots_scale=slots_scale, ts_ms=ts_ms)
     prec = G.MIXED if precision == "mixed" else G.FP64
     srv = G.Server(prec, 0, quantum)
     cids = [srv.add_class(c.cell_type, c.nx, c.ny, c.rows, slots=c.slots, gap=c.gap) for c in classes]
@@ -480,7 +541,8 @@ def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_sc
            "hbm_reserved_gb": st["hbm_reserved"] / 1e9, "slots": st["slots"],
            "sim_cell_ms_per_wall_s": sim_cell_ms / wall, "arena_build_s": build_s,
            "workload": (f"{len(reqs)} requests, Poisson 200/s; 20% IO 4x4 network sets (1-8), else 1-4096 GrC x4 "
-                        f"/ 1-128 GoC x131 (6 shapes) / 1-16 PC x1600 (5 shapes); 5-25 ms each; seed {seed}")}
+                        f"/ 1-128 GoC x131 (6 shapes) / 1-16 PC x1600 (5 shapes); {ts_ms[0]:g}-{ts_ms[1]:g} ms "
+                        f"each; seed {seed}")}
     # one request at a time, plain FP64, on a sample of the same requests
     sample = []
     for ty in (0, 1, 2, 3):
@@ -495,6 +557,10 @@ def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_sc
     for k in sample:
         r, c = reqs[k], classes[reqs[k].cls]
         cells = c.nx * c.ny
+        # with compare_ms, a long request runs alone only for its first
+        # compare_ms (its rate is what the estimate needs); the served result
+        # is then not compared
+        n_run = r.n_intervals if compare_ms is None else min(r.n_intervals, int(round(compare_ms / H_MAX)))
         w0 = time.perf_counter()
         eng = G.Engine(G.FP64)
         for j in range(r.n_systems):
@@ -504,21 +570,22 @@ def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_sc
                            io_gap_g=None if r.io_gap_g is None else r.io_gap_g[4 * j * cells:4 * (j + 1) * cells])
         eng.build()
         eng.record_spikes(1 << 20)
-        eng.advance(0.0, r.n_intervals, tolerate_retire=True)
+        eng.advance(0.0, n_run, tolerate_retire=True)
         v = np.concatenate([eng.read(j, G.F_VNEW) for j in range(r.n_systems)])
         dt = time.perf_counter() - w0
         seq_wall += dt
         seq_cu += eng.compartment_updates(-1)
         pt = per_type.setdefault(c.cell_type, [0.0, 0.0])
-        pt[0] += cell_ms(r)
+        pt[0] += cell_ms(r) * n_run / r.n_intervals
         pt[1] += dt
         ft, _, _ = eng.read_spikes(c.cell_type)
         eng.close()
-        got = srv.read(ids[k], v.size)
-        err = max(err, float(np.max(np.abs(got - v))))
-        gt, _ = srv.spikes(ids[k])
-        spk_same += int(len(gt) == len(ft))
-        spk_total += 1
+        if n_run == r.n_intervals:
+            got = srv.read(ids[k], v.size)
+            err = max(err, float(np.max(np.abs(got - v))))
+            gt, _ = srv.spikes(ids[k])
+            spk_same += int(len(gt) == len(ft))
+            spk_total += 1
     # the whole stream served one request at a time: each request's cell-ms
     # at its type's sampled sequential rate
     est = sum(cell_ms(r) * per_type[classes[r.cls].cell_type][1] / per_type[classes[r.cls].cell_type][0]
@@ -529,7 +596,9 @@ def run_serve(G, precision, n_requests, seed=5, quantum=8, n_compare=8, slots_sc
                                  "includes": "engine build, advance and read-back per request"}
     out["vs_one_at_a_time_fp64"] = est / wall
     out["served_vs_fp64"] = {"max_abs_err_mv": err, "spike_counts_equal": f"{spk_same}/{spk_total}",
-                             "precision": precision}
+                             "precision": precision, "requests_compared": spk_total}
+    if compare_ms is not None:
+        out["one_at_a_time_fp64"]["sampled_for_ms"] = compare_ms
     srv.close()
     return out
 
@@ -742,7 +811,6 @@ def main():
     ap.add_argument("--window-ms", type=float, default=None,
                     help="simulated window timed from t = 0, split into the steps (default: the workload's own, "
                          "500 ms mixed, 200 ms pkj3x3)")
-    ap.add_argument("--step-ms", type=float, default=5.0, help="network workload: simulated ms per step")
     ap.add_argument("--accuracy-ms", type=float, default=100.0, help="horizon of the mixed-vs-FP64 accuracy sample")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -751,6 +819,9 @@ def main():
                     help="population fraction of the mixed batch (small profiling cases; 1 = the benchmark)")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--serve-slots", type=int, default=1, help="multiplier on the serving arenas' slot counts")
+    ap.add_argument("--serve-ts", type=float, nargs=2, default=None, metavar=("LO", "HI"),
+                    help="request durations U[LO, HI] ms (default 5 25 beside the mixed workload, 50 1000 for "
+                         "--config serve)")
     ap.add_argument("--serve-requests", type=int, default=None,
                     help="requests of the serving stream (default 48 beside the mixed workload, 128 for "
                          "--config serve; 0: none)")
@@ -772,7 +843,9 @@ def main():
         return
     if args.config == "serve":
         # the serving stream on its own: value = compartment-updates/s over the stream's wall time
-        sv = run_serve(G, precision, args.serve_requests or 128, slots_scale=args.serve_slots)
+        ts = tuple(args.serve_ts) if args.serve_ts else (50.0, 1000.0)
+        sv = run_serve(G, precision, args.serve_requests or 24, slots_scale=args.serve_slots, ts_ms=ts,
+                       compare_ms=25.0 if ts[1] > 100.0 else None)
         if rank == 0:
             out = {"metric": "compartment-updates/s", "value": sv["value"], "unit": "compartment-updates/s",
                    "n_gpus": world, "steps": 1, "warmup": args.warmup, "ms_per_step": sv["wall_s"] * 1e3,
@@ -956,7 +1029,8 @@ def run_batch(args, G, configs, torch, specs, wl, precision, rank, world, dist):
     serving = None
     n_serve = 48 if args.serve_requests is None else args.serve_requests
     if n_serve > 0 and rank == 0 and args.config in ("mixed", "screened"):
-        serving = run_serve(G, precision, n_serve, slots_scale=args.serve_slots)
+        serving = run_serve(G, precision, n_serve, slots_scale=args.serve_slots,
+                            ts_ms=tuple(args.serve_ts) if args.serve_ts else (5.0, 25.0))
     cpu = None
     if not args.no_cpu and rank == 0:
         cpu = cpu_baseline_single(args)

@@ -289,11 +289,12 @@ NET_PKJ_SEEDS = (7, 8, 12, 13)
 
 
 def network_batch(seed=3, n_gr=2048, n_go=512, n_pkj=512, n_syn=780404, mf_groups=8, sigma=0.25,
-                  scale=(1.0, 1.0, 1.0, 1.0)):
-    """Network workload: n_gr reduced granule cells, n_go Golgi cells (the
-    screened tree variants), n_pkj Purkinje cells (screened trees), each its
-    own system (shapes NET_GO_VARIANTS, NET_PKJ_SEEDS), coupled by n_syn
-    chemical synapses with the reference's
+                  scale=(1.0, 1.0, 1.0, 1.0), distinct_trees=True):
+    """Network workload: n_gr reduced granule cells, n_go Golgi cells and
+    n_pkj Purkinje cells, each its own system -- with distinct_trees a
+    distinct seeded tree per Golgi and per Purkinje cell (tapered Purkinje
+    diameters), else the shapes NET_GO_VARIANTS / NET_PKJ_SEEDS -- coupled by
+    n_syn chemical synapses with the reference's
     kinetics: 4 mossy fibres per granule cell (Poisson, groups at 5-50 Hz),
     100 granule cells onto each Golgi soma, 4 Golgi cells onto each granule
     soma, and the rest granule -> Purkinje onto random dendritic
@@ -308,11 +309,15 @@ def network_batch(seed=3, n_gr=2048, n_go=512, n_pkj=512, n_syn=780404, mf_group
     indices into specs."""
     rng = np.random.default_rng(seed)
     gr_rows = M.gr_reduced4()
-    go_rows = [M.go_synthetic(2000 + k) for k in NET_GO_VARIANTS]
-    pk_rows = [M.pkj_synthetic(k) for k in NET_PKJ_SEEDS]
+    if distinct_trees:
+        go_rows = [M.go_synthetic(seed * 100000 + i) for i in range(n_go)]
+        pk_rows = [M.pkj_synthetic(seed * 100000 + 50000 + i) for i in range(n_pkj)]
+    else:
+        go_rows = [M.go_synthetic(2000 + k) for k in NET_GO_VARIANTS]
+        pk_rows = [M.pkj_synthetic(k) for k in NET_PKJ_SEEDS]
     specs = [Spec(M.GR, 1, 1, gr_rows, _jitter(rng, 1), tag="gr") for _ in range(n_gr)]
-    specs += [Spec(M.GO, 1, 1, go_rows[i % len(go_rows)], _jitter(rng, 1), tag="go") for i in range(n_go)]
-    specs += [Spec(M.PKJ, 1, 1, pk_rows[i % len(pk_rows)], _jitter(rng, 1), tag="pkj") for i in range(n_pkj)]
+    specs += [Spec(M.GO, 1, 1, go_rows[i % len(go_rows)], _jitter(rng, 1), tag=f"go#{i}") for i in range(n_go)]
+    specs += [Spec(M.PKJ, 1, 1, pk_rows[i % len(pk_rows)], _jitter(rng, 1), tag=f"pkj#{i}") for i in range(n_pkj)]
     gr = np.arange(n_gr)
     go = n_gr + np.arange(n_go)
     pk = n_gr + n_go + np.arange(n_pkj)

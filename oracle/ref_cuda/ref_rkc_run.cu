@@ -1,12 +1,13 @@
 // Runs the reference simulator's own RKC path on the GPU -- its X_initialize
 // / X_solve_initialize / X_set_current / X_solve_update_v / X_output_file
 // entry points, compiled from its sources by this directory's Makefile --
-// in the per-interval loop of its main.cu:182-311 (RKC solver, no network),
+// in the per-interval loop of its main.cu:182-311,
 // with the simulated time, the stimulus and extra outputs chosen on the
 // command line.  Test infrastructure and the reference baseline; not part of
 // the product.
 //
 //   ref_rkc_run GRX GRY GOX GOY PKJX PKJY IOX IOY TS_MS STIM OUTDIR DUMP_IV
+//               [SOLVERS [NETWORK]]
 //
 //   STIM    "ref": the reference's X_set_current protocols, as main.cu runs
 //           them; "const:gr=A,go=A,pkj=A,io=A" (any subset): a current A
@@ -19,6 +20,15 @@
 //           DUMP_IV intervals, every compartment's v_new of every type as
 //           raw float64 (<type>_vnew.bin, interval-major), and the initial
 //           elem[v] (<type>_v0.bin).
+//   SOLVERS "RKC" (default) or four comma-separated solver names for GrC,
+//           GoC, PC and IO (RKC, CN or BE, as main.cu's arguments), e.g.
+//           "CN,RKC,RKC,CN" as the reference's network1.sh runs them; a
+//           BE / CN type takes DT = 0.025 ms sub-steps within each interval
+//           (main.cu:193-200) and its voltage is read from elem[v].  The
+//           CSV names carry each type's solver name, as main.cu's do.
+//   NETWORK 1: main.cu's network branch -- no X_set_current, and after
+//           every interval the three synapse updates of main.cu:302-306 --
+//           which main.cu itself leaves off (network_sim = false, main.cu:39).
 // Model files are read by the reference's loaders from the working
 // directory.  srand(0) as main.cu:38, so the initial jitter follows its
 // rand() order (GrC, GoC, PC, IO).  Prints one JSON line: the loop's wall
@@ -119,9 +129,19 @@ int main(int argc, char **argv) {
       if (const char *at = strchr(eq + 1, '@')) t_on[k] = atof(at + 1);
     }
   }
+  char solvers[4][8] = {"RKC", "RKC", "RKC", "RKC"};
+  if (argc > 13 && strcmp(argv[13], "RKC") != 0) {
+    char buf[64];
+    snprintf(buf, sizeof buf, "%s", argv[13]);
+    int k = 0;
+    for (char *tok = strtok(buf, ","); tok && k < 4; tok = strtok(nullptr, ","), k++) snprintf(solvers[k], 8, "%s", tok);
+    if (k != 4) {
+      fprintf(stderr, "SOLVERS: four names or RKC\n");
+      return 1;
+    }
+  }
+  const bool network = argc > 14 && atoi(argv[14]) != 0;
   srand(0);
-  char solver[8];
-  strcpy(solver, "RKC");
   TypeRun T[4];
   const char *names[4] = {"gr", "go", "pkj", "io"};
   for (int k = 0; k < 4; k++) {
@@ -130,14 +150,14 @@ int main(int argc, char **argv) {
     T[k].ps = (neuron_solve_t *)malloc(sizeof(neuron_solve_t));
   }
   // main.cu:105-134: each type initialised in this order (rand() order)
-  T[0].d = gr_initialize(dims[0], dims[1], solver, T[0].p);
-  T[0].ds = gr_solve_initialize(T[0].ps, solver, T[0].p, T[0].d);
-  T[1].d = go_initialize(dims[2], dims[3], solver, T[1].p);
-  T[1].ds = go_solve_initialize(T[1].ps, solver, T[1].p, T[1].d);
-  T[2].d = pkj_initialize(dims[4], dims[5], solver, T[2].p);
-  T[2].ds = pkj_solve_initialize(T[2].ps, solver, T[2].p, T[2].d);
-  T[3].d = io_initialize(dims[6], dims[7], solver, T[3].p);
-  T[3].ds = io_solve_initialize(T[3].ps, solver, T[3].p, T[3].d);
+  T[0].d = gr_initialize(dims[0], dims[1], solvers[0], T[0].p);
+  T[0].ds = gr_solve_initialize(T[0].ps, solvers[0], T[0].p, T[0].d);
+  T[1].d = go_initialize(dims[2], dims[3], solvers[1], T[1].p);
+  T[1].ds = go_solve_initialize(T[1].ps, solvers[1], T[1].p, T[1].d);
+  T[2].d = pkj_initialize(dims[4], dims[5], solvers[2], T[2].p);
+  T[2].ds = pkj_solve_initialize(T[2].ps, solvers[2], T[2].p, T[2].d);
+  T[3].d = io_initialize(dims[6], dims[7], solvers[3], T[3].p);
+  T[3].ds = io_solve_initialize(T[3].ps, solvers[3], T[3].p, T[3].d);
   // main.cu:137-145
   synapse_t *mfgr = mfgr_create(T[0].p->n);
   synapse_t *gogr = gogr_create(T[1].p->nx, T[1].p->ny, T[0].p->nx, T[0].p->ny);
@@ -150,9 +170,9 @@ int main(int argc, char **argv) {
     R.n = R.p->n;
     R.nc = R.p->nc;
     char nm[64];
-    snprintf(nm, sizeof nm, "%s_v_by_RKC.csv", R.name);
+    snprintf(nm, sizeof nm, "%s_v_by_%s.csv", R.name, solvers[k]);
     R.fv = open_out(dir, nm, "w");
-    snprintf(nm, sizeof nm, "%s_raster_by_RKC.csv", R.name);
+    snprintf(nm, sizeof nm, "%s_raster_by_%s.csv", R.name, solvers[k]);
     R.fr = open_out(dir, nm, "w");
     if (R.nc == 0) continue;
     R.host = (double *)malloc(sizeof(double) * R.nc);
@@ -177,23 +197,30 @@ int main(int argc, char **argv) {
       TypeRun &R = T[k];
       if (R.n == 0) continue;
       const int blocks = R.n / 128 + 1;
-      if (ref_stim) {
-        switch (k) {
-          case 0: gr_set_current<<<blocks, 128>>>(R.d, t); break;
-          case 1: go_set_current<<<blocks, 128>>>(R.d, t); break;
-          case 2: pkj_set_current<<<blocks, 128>>>(R.d, t); break;
-          default: io_set_current<<<blocks, 128>>>(R.d, t); break;
+      // main.cu:193-200: sub-steps of the type's DT within the interval
+      for (double l_dt = 0.0; l_dt < H_MAX; l_dt += R.p->DT) {
+        if (network) {
+        } else if (ref_stim) {
+          switch (k) {
+            case 0: gr_set_current<<<blocks, 128>>>(R.d, t + l_dt); break;
+            case 1: go_set_current<<<blocks, 128>>>(R.d, t + l_dt); break;
+            case 2: pkj_set_current<<<blocks, 128>>>(R.d, t + l_dt); break;
+            default: io_set_current<<<blocks, 128>>>(R.d, t + l_dt); break;
+          }
+        } else if (on[k]) {
+          const_current<<<blocks, 128>>>(R.d, STIM_COMP[k], NCOMP[k], (t + l_dt >= t_on[k]) ? amp[k] : 0.0);
         }
-      } else if (on[k]) {
-        const_current<<<blocks, 128>>>(R.d, STIM_COMP[k], NCOMP[k], (t >= t_on[k]) ? amp[k] : 0.0);
+        switch (k) {
+          case 0: gr_solve_update_v(R.d, R.ds, R.p, R.ps, mfgr, gogr); break;
+          case 1: go_solve_update_v(R.d, R.ds, R.p, R.ps, grgo); break;
+          case 2: pkj_solve_update_v(R.d, R.ds, R.p, R.ps, grpkj, mlipkj); break;
+          default: io_solve_update_v(R.d, R.ds, R.p, R.ps, io_gap); break;
+        }
       }
-      switch (k) {
-        case 0: gr_solve_update_v(R.d, R.ds, R.p, R.ps, mfgr, gogr); break;
-        case 1: go_solve_update_v(R.d, R.ds, R.p, R.ps, grgo); break;
-        case 2: pkj_solve_update_v(R.d, R.ds, R.p, R.ps, grpkj, mlipkj); break;
-        default: io_solve_update_v(R.d, R.ds, R.p, R.ps, io_gap); break;
-      }
-      cudaMemcpy(R.host, R.ps->vec[v_new], sizeof(double) * R.nc, cudaMemcpyDeviceToHost);
+      if (R.p->n_solver == kRKC)
+        cudaMemcpy(R.host, R.ps->vec[v_new], sizeof(double) * R.nc, cudaMemcpyDeviceToHost);
+      else
+        cudaMemcpy(R.host, R.p->elem[v], sizeof(double) * R.nc, cudaMemcpyDeviceToHost);
       if (isnan(R.host[1])) bad = k;
       switch (k) {
         case 0: gr_output_file(R.p, R.host, R.raster, t + H_MAX, R.fv, R.fr); break;
@@ -202,6 +229,12 @@ int main(int argc, char **argv) {
         default: io_output_file(R.p, R.host, R.raster, t + H_MAX, R.fv, R.fr); break;
       }
       if (R.fdump && iv < dump_iv) fwrite(R.host, sizeof(double), R.nc, R.fdump);
+    }
+    if (network && bad < 0) {
+      // main.cu:302-306
+      gr_synapse_update(t, H_MAX, mfgr, gogr, T[1].d, T[0].ps);
+      go_synapse_update(t, H_MAX, grgo, T[0].d, T[1].ps);
+      pkj_synapse_update(t, H_MAX, grpkj, mlipkj, T[0].d, T[2].ps);
     }
     iv++;
     t += H_MAX;
@@ -215,9 +248,11 @@ int main(int argc, char **argv) {
     if (T[k].fdump) fclose(T[k].fdump);
   }
   printf("{\"wall_s\": %.6f, \"intervals\": %d, \"ts_ms\": %.6f, \"nan_type\": %d, \"cuda\": \"%s\", "
+         "\"solvers\": \"%s,%s,%s,%s\", \"network\": %d, "
          "\"nc\": {\"gr\": %d, \"go\": %d, \"pkj\": %d, \"io\": %d}, "
          "\"cells\": {\"gr\": %d, \"go\": %d, \"pkj\": %d, \"io\": %d}, \"stim\": \"%s\"}\n",
-         wall, iv, t, bad, cudaGetErrorString(err), T[0].nc, T[1].nc, T[2].nc, T[3].nc, T[0].n, T[1].n, T[2].n,
+         wall, iv, t, bad, cudaGetErrorString(err), solvers[0], solvers[1], solvers[2], solvers[3], (int)network,
+         T[0].nc, T[1].nc, T[2].nc, T[3].nc, T[0].n, T[1].n, T[2].n,
          T[3].n, stim);
   return bad >= 0 ? 3 : 0;
 }
