@@ -1481,7 +1481,8 @@ static void rkclow(orc_sys *s) {
     if (s->idid == 3.0) return;
     err = sqrt(err / (double)nc);
     if (err > 1.0) {
-      s->absh = 0.8 * s->absh / (POW(err, 1.0 / 3.0));
+      /* canonical: the same cube root as the accept path (cm_cbrt) */
+      s->absh = 0.8 * s->absh / (g_canon ? cm_cbrt(err) : pow(err, 1.0 / 3.0));
       s->n_rej++;
       if (s->absh < hmin) {
         s->idid = 4;
