@@ -341,7 +341,7 @@ def stopped_systems(G, eng, specs, ids):
         for j in np.nonzero(st)[0]:
             k = ks[int(j)]
             out.append({"index": k, "tag": specs[k].tag, "type": int(ty), "status": int(st[j]),
-                        "why": G.STATUS_BITS.get(int(st[j]) & 15, str(int(st[j])))})
+                        "why": next((v for b, v in G.STATUS_BITS.items() if int(st[j]) & b), str(int(st[j])))})
     return out
 
 

@@ -416,6 +416,7 @@ struct PoolHost {
   double *d_spk_prev = nullptr;
   SpikeRec *d_spk_log = nullptr;         // owned here (re-sized by gbrkc_record_spikes)
   int *d_spk_count = nullptr;
+  unsigned *d_grid_bar = nullptr;        // grid team: the barrier's words (zeroed before each launch)
   int spk_cap = 0;
   std::vector<char> retired;
 };
@@ -617,6 +618,24 @@ int cluster_min_nc() {
   return 4096;
 }
 
+// Whether pool P is one system of at least cluster_min_nc() compartments
+// (GBRKC_GRID_MIN_NC overrides) and the engine's only one: such a system
+// runs on every SM of the device as one grid team, where a cluster would
+// give it 16 SMs.  GBRKC_GRID=0, or a forced cluster size
+// (GBRKC_CLUSTER_SIZE), keeps it on a cluster.
+bool grid_team_fits(const gbrkc_engine *E, const PoolHost &P) {
+  const char *g = getenv("GBRKC_GRID");
+  if (g && g[0] == '0') return false;
+  const char *cs = getenv("GBRKC_CLUSTER_SIZE");
+  if (cs && cs[0]) return false;
+  const char *m = getenv("GBRKC_GRID_MIN_NC");
+  const long min_nc = (m && m[0]) ? atol(m) : cluster_min_nc();
+  if (P.systems.size() != 1 || P.max_nc < min_nc) return false;
+  for (const HostSystem &S : E->systems)
+    if (S.type != P.type) return false;
+  return true;
+}
+
 // Output compartments per cell: the voltage record (the soma; the
 // reference's output_file columns) and the raster (the compartment whose
 // threshold crossing output_file logs): gr.cu:257-280, go.cu:271-290,
@@ -792,6 +811,23 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
     P.block = MEGA_BLOCK;
   }
   else if (P.max_nc <= 320) { P.team = TEAM_WARP; P.block = 128; }
+  else if (grid_team_fits(E, P)) {
+    // a lone large system: every SM of the device on it
+    const int g = (E->precision == GBRKC_FP64) ? grid_capacity<double>(P.type) : grid_capacity<float>(P.type);
+    const long nc = P.max_nc;
+    if (g > 0 && (nc + GRID_BLOCK - 1) / GRID_BLOCK <= GRID_MAX_BLOCKS &&
+        (nc + (long)g * GRID_BLOCK - 1) / ((long)g * GRID_BLOCK) <= GRID_MAX_ROWS) {
+      P.team = TEAM_GRID;
+      P.block = GRID_BLOCK;
+      P.grid = g;
+      P.ws_tile = (long)WS_VECS * ((P.max_nc + 1) & ~1);
+      P.ws_in_smem = 0;
+      P.smem = 0;
+      return 0;
+    }
+    P.team = TEAM_CLUSTER16;
+    P.block = 256;
+  }
   else if (P.max_nc >= cluster_min_nc()) { P.team = TEAM_CLUSTER16; P.block = 256; }
   else { P.team = TEAM_BLOCK; P.block = 256; }
   if (P.team == TEAM_CLUSTER16) {
@@ -857,6 +893,15 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
   UP(P.sys_ncomp, V.sys_ncomp); UP(P.sys_tmpl, V.sys_tmpl); UP(P.sys_csr, V.sys_csr);
   UP(P.sys_cell0, V.sys_cell0); UP(P.sys_gap0, V.sys_gap0); UP(P.sys_ngap, V.sys_ngap);
   UP(P.sys_ws, V.sys_ws); UP(P.ctl, V.ctl);
+  V.grid_red = nullptr;
+  V.grid_bar = nullptr;
+  if (P.team == TEAM_GRID) {
+    const std::vector<double> red(2 * GRID_MAX_BLOCKS, 0.0);
+    const std::vector<unsigned> bar(sizeof(GridBarrier) / sizeof(unsigned), 0u);
+    UP(red, V.grid_red);
+    UP(bar, V.grid_bar);
+    P.d_grid_bar = V.grid_bar;
+  }
   std::vector<double> zws(P.ws_total, 0.0);
   UP(zws, V.ws);
   std::vector<double> zero(P.nc, 0.0);
@@ -1041,6 +1086,7 @@ int launch_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
         (P.block != MEGA_BLOCK || !P.ws_in_smem ||
          P.smem < (size_t)MEGA_BLOCK * (size_t)P.ws_tile * sizeof(double)))
       return fail(GBRKC_ESTATE, "single-lane pool %d: launch shape does not cover its workspaces", t);
+    if (P.team == TEAM_GRID) CUDA_TRY(cudaMemsetAsync(P.d_grid_bar, 0, sizeof(GridBarrier), E->streams[t]));
     CUDA_TRY(cudaEventRecord(E->ev_k0[t], E->streams[t]));
     if (E->precision == GBRKC_FP64)
       rc = launch_pool<double>(t, P.vd, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
@@ -1057,6 +1103,12 @@ int launch_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
   for (int t = 0; t < NTYPES; t++) {
     E->last_kernel_ms[t] = 0.0f;
     if (!E->pools[t].systems.empty()) CUDA_TRY(cudaEventElapsedTime(&E->last_kernel_ms[t], E->ev_k0[t], E->ev_k1[t]));
+    if (E->pools[t].team == TEAM_GRID && !E->pools[t].systems.empty()) {
+      GridBarrier gb{};
+      CUDA_TRY(cudaMemcpy(&gb, E->pools[t].d_grid_bar, sizeof gb, cudaMemcpyDeviceToHost));
+      if (gb.abort)
+        return fail(GBRKC_ECUDA, "grid team (type %d): a barrier gave up waiting; the system is stopped", t);
+    }
   }
   return 0;
 }
@@ -1156,7 +1208,8 @@ int setup_mega(gbrkc_engine *E) {
   if (no && no[0] == '1') return 0;
   // pools of very large systems run on clusters, one launch per pool
   for (int t = 0; t < NTYPES; t++)
-    if (!E->pools[t].systems.empty() && team_cluster_size(E->pools[t].team) > 0) return 0;
+    if (!E->pools[t].systems.empty() &&
+        (team_cluster_size(E->pools[t].team) > 0 || E->pools[t].team == TEAM_GRID)) return 0;
   const PoolHost &G = E->pools[GR], &O = E->pools[GO];
   if (!G.systems.empty() && G.max_nc > LANE_MAX_NC) return 0;
   if (!O.systems.empty() && O.max_nc > 320) return 0;

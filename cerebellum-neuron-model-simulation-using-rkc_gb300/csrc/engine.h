@@ -33,6 +33,7 @@ enum Status : int {
   ST_COEF_TABLE = 4,   // stage count beyond the coefficient table
   ST_IDID = 8,         // rkclow returned an idid other than 1/2 (solve_rkc.cu:1155)
   ST_INIT = 16,        // waiting for initialisation (set by the host; cleared by the init launch)
+  ST_BARRIER = 32,     // a grid-team barrier gave up waiting (bounded spin)
 };
 
 // One threshold crossing of a cell's spike compartment, logged on the device
@@ -116,6 +117,10 @@ struct PoolView {
   const double *syn_val;              // per synapse: conductance value (engine-wide table)
   const double *syn_e;                // per synapse: reversal potential
   double *syn_buf;                    // [stride] synaptic current taken at interval start
+  // grid team (one system over every CTA of a cooperative launch): block
+  // sums of the reductions, double-buffered, and the grid barrier's words
+  double *grid_red;                   // [2][GRID_MAX_BLOCKS]
+  unsigned *grid_bar;                 // GridBarrier
 };
 
 // How a pool takes its synaptic current (solve_rkc.cu): granule cells add
@@ -158,9 +163,11 @@ int launch_syn_update(const SynView &S, void *stream, double t, long long interv
 // TEAM_CLUSTER8 / TEAM_CLUSTER16: one system per cluster of 8 / 16 CTAs
 // (very large systems; 16 is a non-portable cluster size, used where the
 // device can co-schedule it).
+// TEAM_GRID: one system over every CTA of a cooperative launch (a system
+// that is alone in its engine and larger than a cluster holds efficiently).
 enum TeamKind {
   TEAM_THREAD = 1, TEAM_LANE4 = 2, TEAM_TILE4 = 4, TEAM_WARP = 32, TEAM_BLOCK = 0,
-  TEAM_CLUSTER8 = 108, TEAM_CLUSTER16 = 116
+  TEAM_CLUSTER8 = 108, TEAM_CLUSTER16 = 116, TEAM_GRID = 200
 };
 constexpr int team_cluster_size(int team) {
   return team == TEAM_CLUSTER8 ? 8 : team == TEAM_CLUSTER16 ? 16 : 0;
@@ -190,6 +197,18 @@ constexpr int CLUSTER_BLOCK = 256;
 constexpr int CLUSTER_MAX_ROWS = 14;
 constexpr int CLUSTER_RED_DOUBLES = 2 * CLUSTER_MAX_ROWS + 8 * CLUSTER_MAX_ROWS + 2;
 constexpr int LANE_MAX_NC = 8;   // largest system integrated by a single lane
+// Grid team: CTAs of GRID_BLOCK threads; element i of a workspace vector is
+// owned by thread (i mod gridDim * GRID_BLOCK); a reduction covers at most
+// GRID_MAX_BLOCKS blocks of GRID_BLOCK elements and GRID_MAX_ROWS rows of
+// gridDim * GRID_BLOCK elements.
+constexpr int GRID_BLOCK = 256;
+constexpr int GRID_MAX_BLOCKS = 256;
+constexpr int GRID_MAX_ROWS = 8;
+// The grid barrier's words: arrivals, generation, abort flag.
+struct GridBarrier {
+  unsigned count, gen;
+  int abort, pad;
+};
 
 template <typename R>
 int launch_mega(const MegaView<R> &M, int grid, size_t smem, void *stream, double t0, int n_iv, int iv0,
@@ -207,5 +226,8 @@ int prepare_pool_kernel(int type, int team, size_t smem);
 // with this shared memory (0: the shape does not fit).
 template <typename R>
 int cluster_capacity(int type, int team, size_t smem);
+// CTAs of the grid team's cooperative launch (0: the device cannot launch it).
+template <typename R>
+int grid_capacity(int type);
 
 }  // namespace gbrkc

@@ -44,7 +44,7 @@ struct WVec {
 // a slot offset (vec_at) and gives the slot length for ncp elements
 // (vstride).  CLUSTER > 0 marks a team spread over a thread-block cluster.
 struct BlockTeam {
-  static constexpr int LS = 1, NCF = 0, CLUSTER = 0;
+  static constexpr int LS = 1, NCF = 0, CLUSTER = 0, GRID = 0;
   typedef WVec<1> Vec;
   __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off}; }
   __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
@@ -55,7 +55,7 @@ struct BlockTeam {
 
 template <int T>
 struct TileTeam {
-  static constexpr int LS = 1, NCF = 0, CLUSTER = 0;
+  static constexpr int LS = 1, NCF = 0, CLUSTER = 0, GRID = 0;
   typedef WVec<1> Vec;
   __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off}; }
   __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
@@ -75,7 +75,7 @@ struct TileTeam {
 // would otherwise serialise the loop) and the pairwise sums run in registers.
 template <int BLOCK, int NCF_ = 0>
 struct LaneTeam {
-  static constexpr int LS = BLOCK, NCF = NCF_, CLUSTER = 0;
+  static constexpr int LS = BLOCK, NCF = NCF_, CLUSTER = 0, GRID = 0;
   typedef WVec<BLOCK> Vec;
   __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off * BLOCK}; }
   __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
@@ -107,7 +107,7 @@ struct CVec {
 template <int C>
 struct ClusterTeam {
   static_assert((C & (C - 1)) == 0 && C <= 16, "cluster size must be a power of two up to 16");
-  static constexpr int LS = 1, NCF = 0, CLUSTER = C;
+  static constexpr int LS = 1, NCF = 0, CLUSTER = C, GRID = 0;
   typedef CVec<C> Vec;
   int crank;                   // this CTA's rank in the cluster
   double *const *bases;        // [C] workspace bases (distributed shared memory)
@@ -122,6 +122,59 @@ struct ClusterTeam {
   __device__ __forceinline__ void sync() const {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
+};
+
+// One system over every CTA of a cooperative launch (GridTeam): the
+// workspace stays in global memory (the L2 holds it), element i is owned by
+// thread i mod (gridDim * GRID_BLOCK), and the team barrier is a software
+// grid barrier.  The barrier's wait is bounded: a CTA that waits more than
+// GRID_SPIN_LIMIT polls raises the abort flag, after which no barrier waits
+// and every CTA leaves its system at the next tick (status ST_BARRIER); the
+// host reads the flag after the launch.  A cooperative launch makes every
+// CTA co-resident, so the bound is a guard, not a schedule.
+constexpr long GRID_SPIN_LIMIT = 1L << 22;
+
+__device__ __forceinline__ void grid_barrier(GridBarrier *b) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile GridBarrier *vb = b;
+    if (!vb->abort) {
+      // the generation can only move once this CTA has arrived
+      const unsigned g = atomicAdd(&b->gen, 0u);
+      __threadfence();
+      if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+        atomicExch(&b->count, 0u);
+        __threadfence();
+        atomicAdd(&b->gen, 1u);
+      } else {
+        long it = 0;
+        while (atomicAdd(&b->gen, 0u) == g) {
+          if (++it > GRID_SPIN_LIMIT || vb->abort) {
+            atomicExch(&b->abort, 1);
+            break;
+          }
+          __nanosleep(64);
+        }
+      }
+      __threadfence();
+    }
+  }
+  __syncthreads();
+}
+
+struct GridTeam {
+  static constexpr int LS = 1, NCF = 0, CLUSTER = 0, GRID = 1;
+  typedef WVec<1> Vec;
+  GridBarrier *bar;
+  double *red;                 // [2][GRID_MAX_BLOCKS] block sums (global)
+  double *wp;                  // [GRID_MAX_ROWS][8] warp partials (shared)
+  double *res;                 // the reduction's result (shared)
+  __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off}; }
+  __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
+  __device__ __forceinline__ int rank() const { return (int)blockIdx.x * GRID_BLOCK + (int)threadIdx.x; }
+  __device__ __forceinline__ int size() const { return (int)gridDim.x * GRID_BLOCK; }
+  __device__ __forceinline__ void sync() const { grid_barrier(bar); }
+  __device__ __forceinline__ bool aborted() const { return ((volatile GridBarrier *)bar)->abort != 0; }
 };
 
 // pairwise tree over a[0..N) in registers, the same order as Sys::tree_sum
@@ -315,6 +368,7 @@ struct Sys {
   // pairwise tree over a[0..n): stride doubling, identical to the oracle
   __device__ __forceinline__ double tree_sum(const V a, int n) const {
     if constexpr (Team::CLUSTER > 0) return cluster_tree_sum(a, n);
+    if constexpr (Team::GRID > 0) return grid_tree_sum(a, n);
     tm.sync();
     for (int stride = 1; stride < n; stride *= 2) {
       const int step = 2 * stride;
@@ -397,6 +451,81 @@ struct Sys {
     }
     __syncthreads();
     return *res;
+  }
+
+  // tree_sum on a grid team: cluster_tree_sum's additions in the same order.
+  // Element i is owned by the thread that writes it in the team loops, so the
+  // aligned block of GRID_BLOCK elements starting at row k, CTA b (block
+  // index k * gridDim + b) lies in CTA b, one element per thread: levels 0-4
+  // are warp shuffles, 5-7 combine the block's 8 warp partials, the block sum
+  // goes to global memory, and after one grid barrier warp 0 of every CTA
+  // combines all block sums (levels 8 and up), every CTA computing the same
+  // value.  The block sums are double-buffered, as on a cluster.
+  __device__ __forceinline__ double grid_tree_sum(const V a, int n) const {
+    if constexpr (Team::GRID > 0) {
+      constexpr int B = GRID_BLOCK, RR = GRID_MAX_BLOCKS / 32;
+      const int t = threadIdx.x, lane = t & 31, warp = t >> 5, b = blockIdx.x, G = gridDim.x;
+      const int size = G * B;
+      const int rows = (n + size - 1) / size;
+      double *red = tm.red, *wp = tm.wp;
+      const int buf = red_buf;
+      red_buf ^= 1;
+      for (int k = 0; k < rows; k++) {
+        const int i0 = k * size + b * B;
+        if (i0 >= n) break;
+        const int i = i0 + t;
+        double x = (i < n) ? a[i] : 0.0;
+#pragma unroll
+        for (int st = 1; st < 32; st *= 2) {
+          const double y = __shfl_down_sync(0xffffffffu, x, st);
+          if ((lane & (2 * st - 1)) == 0 && i + st < n) x = x + y;
+        }
+        if (lane == 0) wp[k * 8 + warp] = x;
+      }
+      __syncthreads();
+      if (t < rows) {
+        const int i0 = t * size + b * B;
+        if (i0 < n) {
+          double w[8];
+#pragma unroll
+          for (int j = 0; j < 8; j++) w[j] = wp[t * 8 + j];
+#pragma unroll
+          for (int st = 1; st < 8; st *= 2)
+#pragma unroll
+            for (int j = 0; j + st < 8; j += 2 * st)
+              if (i0 + (j + st) * 32 < n) w[j] = w[j] + w[j + st];
+          red[buf * GRID_MAX_BLOCKS + t * G + b] = w[0];
+        }
+      }
+      tm.sync();
+      if (warp == 0) {
+        const int nb = (n + B - 1) / B;
+        double v[RR];
+#pragma unroll
+        for (int r = 0; r < RR; r++) {
+          const int j = lane + 32 * r;
+          v[r] = (j < nb) ? __ldcg(red + buf * GRID_MAX_BLOCKS + j) : 0.0;
+        }
+#pragma unroll
+        for (int st = 1; st < 32; st *= 2)
+#pragma unroll
+          for (int r = 0; r < RR; r++) {
+            if (32 * r >= nb) break;
+            const double y = __shfl_down_sync(0xffffffffu, v[r], st);
+            if ((lane & (2 * st - 1)) == 0 && lane + 32 * r + st < nb) v[r] = v[r] + y;
+          }
+#pragma unroll
+        for (int st = 1; st < RR; st *= 2)
+#pragma unroll
+          for (int r = 0; r + st < RR; r += 2 * st)
+            if (32 * (r + st) < nb) v[r] = v[r] + v[r + st];
+        if (lane == 0) *tm.res = v[0];
+      }
+      __syncthreads();
+      return *tm.res;
+    } else {
+      return 0.0;
+    }
   }
 
   template <class A>
@@ -941,9 +1070,17 @@ __device__ __forceinline__ void run_system(const PoolView<R> &P, const Team &tm,
   if (init) {
     S.initialize();
     S.c.status &= ~ST_INIT;
+    if constexpr (Team::GRID > 0)
+      if (tm.aborted()) S.c.status |= ST_BARRIER;
   } else {
     int r = S.start(t0, n_iv, iv0_global);
     while (r != TICK_DONE) {
+      if constexpr (Team::GRID > 0) {
+        if (tm.aborted()) {
+          S.c.status |= ST_BARRIER;
+          break;
+        }
+      }
       if (r == TICK_ION) {
         S.ion_due();
         r = TICK_MORE;

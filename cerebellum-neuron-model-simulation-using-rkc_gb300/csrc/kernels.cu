@@ -7,6 +7,7 @@
 //
 // Built with -fmad=false (see integrator.cuh).  R selects FP64 or FP32
 // gating; the instantiations live in kernels_fp64.cu / kernels_fp32.cu.
+#include <algorithm>
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -63,6 +64,17 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK, 1) k_advance_cluster(const __gr
   for (int s = cid; s < P.nsys; s += ncl) run_system<CT, R, ClusterTeam<C>>(P, tm, s, smem, t0, n_iv, iv0, init != 0);
   // no CTA leaves while a peer may still reach its shared memory
   cl.sync();
+}
+
+// One large system over every CTA of a cooperative launch (GridTeam): all
+// CTAs take the pool's systems one after another.
+template <int CT, typename R>
+__global__ void __launch_bounds__(GRID_BLOCK, 1) k_advance_grid(const __grid_constant__ PoolView<R> P, double t0,
+                                                                 int n_iv, int iv0, int init) {
+  __shared__ double s_wp[GRID_MAX_ROWS * 8];
+  __shared__ double s_res;
+  const GridTeam tm{(GridBarrier *)P.grid_bar, P.grid_red, s_wp, &s_res};
+  for (int s = 0; s < P.nsys; s++) run_system<CT, R, GridTeam>(P, tm, s, nullptr, t0, n_iv, iv0, init != 0);
 }
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -164,6 +176,7 @@ int launch_mega(const MegaView<R> &M, int grid, size_t smem, void *stream, doubl
 template <int CT, typename R>
 static const void *kernel_for(int team) {
   switch (team) {
+    case TEAM_GRID: return (const void *)k_advance_grid<CT, R>;
     case TEAM_CLUSTER8: return (const void *)k_advance_cluster<CT, R, 8>;
     case TEAM_CLUSTER16: return (const void *)k_advance_cluster<CT, R, 16>;
     case TEAM_LANE4:
@@ -217,6 +230,23 @@ static cudaLaunchConfig_t cluster_config(int team, int grid, size_t smem, cudaSt
   return cfg;
 }
 
+// CTAs of the grid team's kernel the device co-schedules (cooperative
+// launch: every CTA resident at once), 0 when it cannot launch cooperatively.
+template <typename R>
+int grid_capacity(int type) {
+  int dev = 0, coop = 0, sms = 0, bps = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!coop) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel_ptr<R>(type, TEAM_GRID), GRID_BLOCK, 0) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return sms * std::min(bps, 1);
+}
+
 template <typename R>
 int cluster_capacity(int type, int team, size_t smem) {
   if (prepare_pool_kernel<R>(type, team, smem) != 0) {
@@ -239,6 +269,10 @@ int launch_pool(int type, const PoolView<R> &P, int team, int grid, int block, s
   const void *k = kernel_ptr<R>(type, team);
   PoolView<R> Pc = P;
   void *args[] = {(void *)&Pc, (void *)&t0, (void *)&n_iv, (void *)&iv0, (void *)&init};
+  if (team == TEAM_GRID) {
+    if (block != GRID_BLOCK) return (int)cudaErrorInvalidConfiguration;
+    return (int)cudaLaunchCooperativeKernel(k, dim3(grid), dim3(block), args, 0, (cudaStream_t)stream);
+  }
   if (team_cluster_size(team) > 0) {
     if (block != CLUSTER_BLOCK || grid % team_cluster_size(team) != 0) return (int)cudaErrorInvalidConfiguration;
     cudaLaunchAttribute attr[1];

@@ -19,7 +19,7 @@ FP64, MIXED = 0, 1
 F_VNEW, F_V, F_CA, F_B, F_ION, F_REV, F_YN = 0, 1, 2, 3, 4, 5, 6
 H_MAX = 0.125
 STATUS_BITS = {1: "non-finite error norm", 2: "step loop bound", 4: "stage count beyond table",
-               8: "unexpected idid"}
+               8: "unexpected idid", 32: "grid barrier gave up waiting"}
 
 
 class SystemDesc(C.Structure):

@@ -141,8 +141,10 @@ def _pkj_grid(O, nx, ny, ncomp, n_iv):
     return layout
 
 
-def test_largest_cluster_system(oracle):
+def test_largest_cluster_system(oracle, monkeypatch):
     # 6 x 6 cells of 1592 compartments = 57 312 <= 16 CTAs x 14 rows x 256
+    # (a lone system this large takes the grid team by default: off here)
+    monkeypatch.setenv("GBRKC_GRID", "0")
     persistent, ctas = _pkj_grid(oracle, 6, 6, 1592, 4)
     print("layout", persistent, ctas)
     # the 16-CTA cluster; where the device cannot co-schedule 16 CTAs of
@@ -150,8 +152,10 @@ def test_largest_cluster_system(oracle):
     assert persistent or ctas[M.PKJ] == 16, (persistent, ctas)
 
 
-def test_system_beyond_cluster_capacity(oracle):
+def test_system_beyond_cluster_capacity(oracle, monkeypatch):
     # 6 x 6 cells of 1600 compartments = 57 600: no cluster holds the
-    # workspace, so one CTA integrates it with the workspace in HBM
+    # workspace, so without the grid team one CTA integrates it with the
+    # workspace in HBM
+    monkeypatch.setenv("GBRKC_GRID", "0")
     persistent, ctas = _pkj_grid(oracle, 6, 6, 1600, 3)
     assert persistent and ctas[M.PKJ] >= 1, (persistent, ctas)

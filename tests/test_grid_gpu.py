@@ -1,0 +1,83 @@
+"""A system alone in its engine and larger than a cluster holds efficiently
+runs as one grid team: every CTA of a cooperative launch takes a slice of
+its workspace (kept in global memory, in L2), and a bounded software grid
+barrier separates the stages.  Bit for bit with the oracle like every other
+team: the reductions combine 256-element block sums in the same pairwise
+order.  GBRKC_GRID_MIN_NC lowers the size threshold so that small cases take
+the path."""
+import numpy as np
+import pytest
+
+import gbrkc as G
+import morph as M
+from gpu_cases import jitter_for
+from test_gpu_parity import HORIZON, run_pair
+
+pytestmark = pytest.mark.gpu
+
+
+def _sms():
+    import torch
+    return torch.cuda.get_device_properties(0).multi_processor_count
+
+
+@pytest.mark.parametrize("name", ["pkj_cell", "pkj_2x1_gj", "gr_full", "go_2x2_gj"])
+def test_grid_team_bit_exact(oracle, monkeypatch, name):
+    monkeypatch.setenv("GBRKC_GRID_MIN_NC", "300")
+    n = HORIZON.get(name, 64)
+    s, eng, sid = run_pair(oracle, name, [1, n // 2 - 1, n // 2])
+    persistent, ctas = eng.launch_layout()
+    assert persistent is False and max(ctas) == _sms(), ctas
+    eng.close()
+
+
+def test_grid_io_network(oracle, monkeypatch):
+    """A 12x12 olive network (nonlinear gap junctions across CTAs)."""
+    monkeypatch.setenv("GBRKC_GRID_MIN_NC", "400")
+    O = oracle
+    O.libc_srand(0)
+    jit = O.draw_jitter(O.IO, 144)
+    stim = (0, 5.5, 1.0, 30.0)
+    s = O.System(O.IO, 12, 12, M.io_rows(), jit, stim=stim, canon=True)
+    assert s.init() == 0
+    eng = G.Engine(G.FP64)
+    sid = eng.add_system(M.IO, 12, 12, M.io_rows(), jit, stim=stim, gap=True)
+    eng.build()
+    assert max(eng.launch_layout()[1]) == _sms()
+    t = 0.0
+    for chunk in (1, 15, 16):
+        eng.advance(t, chunk)
+        for _ in range(chunk):
+            assert s.advance(t) == 0
+            t += G.H_MAX
+        np.testing.assert_array_equal(eng.vnew(sid), s.vnew(), err_msg=f"t={t}")
+    ctl, st, status = eng.ctl(sid)
+    assert status == 0 and st == s.stats()
+    eng.close()
+
+
+def test_grid_system_beyond_cluster_capacity(oracle):
+    """6 x 6 Purkinje cells of 1600 compartments (57 600; two rows of the
+    grid's threads): the default path for it is now the grid team."""
+    rows = M.pkj_synthetic(4, 1600)
+    stim = (1599, 0.5e-3, 0.0, 1e9)
+    jit = jitter_for(oracle, M.PKJ, 36)
+    s = oracle.System(M.PKJ, 6, 6, rows, jit, stim=stim, gj_pairs=M.PKJ_GJ_PAIRS, pkj_gj=True, canon=True)
+    assert s.init() == 0
+    eng = G.Engine(G.FP64)
+    sid = eng.add_system(M.PKJ, 6, 6, rows, jit, stim=stim, gj_pairs=M.PKJ_GJ_PAIRS, gap=True)
+    eng.build()
+    persistent, ctas = eng.launch_layout()
+    assert not persistent and ctas[M.PKJ] == _sms(), ctas
+    t = 0.0
+    for chunk in (1, 2):
+        eng.advance(t, chunk)
+        for _ in range(chunk):
+            assert s.advance(t) == 0
+            t += G.H_MAX
+        np.testing.assert_array_equal(eng.vnew(sid), s.vnew())
+    ctl, st, status = eng.ctl(sid)
+    assert status == 0
+    for k, v in s.stats().items():
+        assert st[k] == v, (k, st[k], v)
+    eng.close()
