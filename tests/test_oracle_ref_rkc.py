@@ -12,7 +12,10 @@ arithmetic (libm, no canonical choices) and must match:
 
 * the initial membrane voltages bit for bit;
 * after the first interval, every voltage to 1e-12 relative to the largest
-  |v| for Golgi and Purkinje cells -- the reference's GPU arithmetic (CUDA's
+  |v| for Golgi and Purkinje cells (or 30 x the floor below, for the trees
+  whose first steps already turn last bits into different decisions:
+  Golgi tree 200043's own two arithmetics differ by 4e-9 after one
+  interval) -- the reference's GPU arithmetic (CUDA's
   device exp and fused multiply-adds, cuBLAS and atomic summation order)
   differs from the oracle's only in last bits.  The granule cell (tolerance
   1e-9: every accepted step carries a local error of that order) is held to
@@ -101,7 +104,7 @@ def test_oracle_matches_reference_cuda_build(oracle, name):
         floor = max([floor] + [np.max(np.abs(got - w.vnew())) / scale for w in variants])
         err = np.max(np.abs(got - want)) / scale
         if k == 0:
-            assert err < FIRST_INTERVAL[t], f"first interval: {err:.3e}"
+            assert err < max(FIRST_INTERVAL[t], 30.0 * floor), f"first interval: {err:.3e}, floor {floor:.3e}"
         assert err <= max(1e-4, 30.0 * floor), f"interval {k + 1}: {err:.3e} against floor {floor:.3e}"
         x = got[np.arange(c["nx"] * c["ny"]) * ncomp + RASTER_COMP[t]]
         for cell in np.nonzero((x > THRESH[t]) & (prev <= THRESH[t]))[0]:
