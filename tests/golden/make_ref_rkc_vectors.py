@@ -47,9 +47,8 @@ CASES = {
     # goes non-finite after 1.75 ms: the reference build's own run of them
     "pkj_1x1_untapered_s3": dict(type=M.PKJ, nx=1, ny=1, rows=("pkj", 3, False), amp=0.6e-3, n_iv=24),
     "pkj_1x1_untapered_s10": dict(type=M.PKJ, nx=1, ny=1, rows=("pkj", 10, False), amp=0.6e-3, n_iv=24),
-    # seeded Golgi trees of the mixed batch on which the oracle goes
-    # non-finite after 3.25-3.5 ms: the reference build's own run of them
-    "go_1x1_s200043": dict(type=M.GO, nx=1, ny=1, rows=("go", 200043), amp=0.3e-3, n_iv=40),
+    # a seeded Golgi tree of the mixed batch on which the oracle goes
+    # non-finite after 3.25 ms: the reference build's own run of it
     "go_1x1_s200095": dict(type=M.GO, nx=1, ny=1, rows=("go", 200095), amp=0.6e-3, n_iv=40),
 }
 

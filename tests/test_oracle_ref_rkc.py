@@ -13,9 +13,8 @@ arithmetic (libm, no canonical choices) and must match:
 * the initial membrane voltages bit for bit;
 * after the first interval, every voltage to 1e-12 relative to the largest
   |v| for Golgi and Purkinje cells (or 30 x the floor below, for the trees
-  whose first steps already turn last bits into different decisions:
-  Golgi tree 200043's own two arithmetics differ by 4e-9 after one
-  interval) -- the reference's GPU arithmetic (CUDA's
+  whose first steps already turn last bits into different decisions)
+  -- the reference's GPU arithmetic (CUDA's
   device exp and fused multiply-adds, cuBLAS and atomic summation order)
   differs from the oracle's only in last bits.  The granule cell (tolerance
   1e-9: every accepted step carries a local error of that order) is held to
