@@ -77,6 +77,26 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def fp64_peak_tflops(torch, n=4096, reps=5):
+    """Measured FP64 throughput of this GPU: a cuBLAS DGEMM (torch.matmul in
+    float64, n^3), best of reps, CUDA events -- the FP64 counterpart of the
+    measured bf16 peak, for the FP64-pipe fraction of the kernels."""
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     def __init__(self, gpu_index=0):
@@ -997,6 +1017,10 @@ def run_batch(args, G, configs, torch, specs, wl, precision, rank, world, dist):
         roofline["role_ctas"] = {names[k]: role_ctas[k] for k in range(4)}
     if fp64_ncu is not None:
         roofline["fp64_pipe_active_ncu"] = fp64_ncu
+    try:
+        roofline["fp64_peak_tflops_dgemm"] = fp64_peak_tflops(torch)
+    except Exception as ex:      # a measurement beside the line, never a reason to fail it
+        roofline["fp64_peak_tflops_dgemm"] = f"unmeasured: {ex}"
     eng.close()
     del flush
 
