@@ -416,31 +416,42 @@ def compare_spikes(a, b):
 
 
 # ------------------------------------------------------------ accuracy against FP64
+TYPE_NAMES = {0: "gr", 1: "go", 2: "pkj", 3: "io"}
+PERTURB = {1: 1e-14, 2: 1e-7}     # FP64 floor copies: initial jitter moved by this much
+
+
 def accuracy_vs_fp64(G, configs, sample, horizon_ms=100.0, checkpoints=(1.0, 5.0, 20.0, 100.0)):
     """Mixed precision against plain FP64 on a sample of the workload, from
-    t = 0, next to the FP64 sensitivity floor: the same FP64 run with every
-    cell's initial jitter moved by 1e-14 (its initial voltage by a few units in
-    the last place: V0 = V_init + 2..10 x jitter).  Both FP64 runs
-    share one engine (the perturbed copy is a second set of systems).  Reports
-    max |V - V_fp64| over every compartment at the checkpoints, and the
-    interpolated spike times of every cell (device raster rule) over the
-    horizon."""
+    t = 0, next to two FP64 sensitivity floors: the same FP64 run with every
+    cell's initial jitter moved by 1e-14 (its initial voltage by a few units
+    in the last place: V0 = V_init + 2..10 x jitter), and by 1e-7 (V0 by
+    2e-7..1e-6 mV, under FP32's resolution of a membrane voltage, 3.8e-6 mV at
+    -65 mV: the size of the rounding the mixed path's FP32 gating starts
+    from).  The three FP64 copies share one engine.  Reports max |V - V_fp64|
+    over every compartment at the checkpoints, in all and per cell type; the
+    same split by whether a system took the FP64 run's step decisions (equal
+    step, rejection, stage and power-iteration counts) up to the checkpoint;
+    and the interpolated spike times of every cell (device raster rule) over
+    the horizon."""
     import copy
-    pert = []
-    for sp in sample:
-        q = copy.copy(sp)
-        q.jitter = np.asarray(sp.jitter, dtype=np.float64) + 1e-14
-        pert.append(q)
+    copies = [sample]
+    for c in sorted(PERTURB):
+        pert = []
+        for sp in sample:
+            q = copy.copy(sp)
+            q.jitter = np.asarray(sp.jitter, dtype=np.float64) + PERTURB[c]
+            pert.append(q)
+        copies.append(pert)
     n_iv = int(round(horizon_ms / H_MAX))
     nsys = len(sample)
-    # FP64 engine: both copies, ordered by cell type (each type one run of
+    ncopy = len(copies)
+    # FP64 engine: every copy, ordered by cell type (each type one run of
     # ids), the unperturbed copy first within a type
-    combo = sorted([(sp.cell_type, 0, k) for k, sp in enumerate(sample)] +
-                   [(sp.cell_type, 1, k) for k, sp in enumerate(pert)])
+    combo = sorted((sp.cell_type, c, k) for c in range(ncopy) for k, sp in enumerate(sample))
     res = {}
     for name, prec in (("fp64", G.FP64), ("mixed", G.MIXED)):
         keys = combo if name == "fp64" else [(sp.cell_type, 0, k) for k, sp in enumerate(sample)]
-        specs = [(sample if c == 0 else pert)[k] for _, c, k in keys]
+        specs = [copies[c][k] for _, c, k in keys]
         e = G.Engine(prec)
         ids = configs.add_to(e, specs)
         e.build()
@@ -448,39 +459,67 @@ def accuracy_vs_fp64(G, configs, sample, horizon_ms=100.0, checkpoints=(1.0, 5.0
             if e.type_cells(ty):
                 e.record_width(ty, w)
         e.record_soma(n_iv)
-        v, t, done = [], 0.0, 0
+        v, st, t, done = [], [], 0.0, 0
         for cp in checkpoints:
             k = int(round(cp / H_MAX)) - done
             e.advance(t, k, tolerate_retire=True)
             t += k * H_MAX
             done += k
-            by = {(c, kk): e.read(i, G.F_VNEW) for (_, c, kk), i in zip(keys, ids)}
-            v.append({c: np.concatenate([by[(c, kk)] for kk in range(nsys)]) for c in {c for _, c, _ in keys}})
+            v.append({(c, kk): e.read(i, G.F_VNEW) for (_, c, kk), i in zip(keys, ids)})
+            st.append({(c, kk): e.ctl(i)[1] for (_, c, kk), i in zip(keys, ids)})
         tr = raster_traces(e, n_iv)
         stop = [dict(x, copy=keys[x["index"]][1], index=keys[x["index"]][2]) for x in stopped_systems(G, e, specs, ids)]
-        res[name] = (v, tr, stop)
+        res[name] = (v, st, tr, stop)
         e.close()
     ncomp = sum(sp.nc for sp in sample)
-    v64 = [x[0] for x in res["fp64"][0]]
-    vpert = [x[1] for x in res["fp64"][0]]
-    v32 = [x[0] for x in res["mixed"][0]]
-    tr64, tr32 = res["fp64"][1], res["mixed"][1]
-    sp64, sppert, sp32 = [], [], []
-    for ty in sorted(tr64):
-        h = tr64[ty].shape[1] // 2
-        sp64 += spike_times(tr64[ty][:, :h], ty=ty)
-        sppert += spike_times(tr64[ty][:, h:], ty=ty)
-        sp32 += spike_times(tr32[ty], ty=ty)
+    v64, st64 = res["fp64"][0], res["fp64"][1]
+    v32, st32 = res["mixed"][0], res["mixed"][1]
+    runs = {"mixed": (v32, st32, 0), "floor": (v64, st64, 1), "floor_fp32_resolution": (v64, st64, 2)}
+
+    def err(vv, c, j, kk):
+        return float(np.max(np.abs(vv[j][(c, kk)] - v64[j][(0, kk)])))
+
+    errs = {r: [[err(vv, c, j, kk) for kk in range(nsys)] for j in range(len(checkpoints))]
+            for r, (vv, _, c) in runs.items()}
     out = {"sample": f"{nsys} systems, {ncomp} compartments, from t = 0 to {horizon_ms:g} ms",
-           "max_abs_err_mv": {f"{cp:g}ms": float(np.max(np.abs(a - b))) for cp, a, b in zip(checkpoints, v32, v64)},
-           "sensitivity_floor_mv": {f"{cp:g}ms": float(np.max(np.abs(a - b)))
-                                    for cp, a, b in zip(checkpoints, vpert, v64)},
-           "spikes_mixed_vs_fp64": compare_spikes(sp64, sp32),
-           "spikes_fp64_floor": compare_spikes(sp64, sppert),
-           "stopped": {"fp64": [x for x in res["fp64"][2] if x["copy"] == 0],
-                       "fp64_perturbed": [x for x in res["fp64"][2] if x["copy"] == 1],
-                       "mixed": res["mixed"][2]},
-           "floor": "the same FP64 run with every initial jitter + 1e-14 (V0 moved by a few units in the last place)"}
+           "max_abs_err_mv": {f"{cp:g}ms": max(errs["mixed"][j]) for j, cp in enumerate(checkpoints)},
+           "sensitivity_floor_mv": {f"{cp:g}ms": max(errs["floor"][j]) for j, cp in enumerate(checkpoints)},
+           "sensitivity_floor_fp32_resolution_mv": {f"{cp:g}ms": max(errs["floor_fp32_resolution"][j])
+                                                    for j, cp in enumerate(checkpoints)}}
+    by_type = {}
+    for ty in sorted({sp.cell_type for sp in sample}):
+        ks = [kk for kk, sp in enumerate(sample) if sp.cell_type == ty]
+        by_type[TYPE_NAMES.get(ty, str(ty))] = {
+            f"{cp:g}ms": {r: max(errs[r][j][kk] for kk in ks) for r in runs} for j, cp in enumerate(checkpoints)}
+    out["max_abs_err_mv_by_type"] = by_type
+    # split by whether the system took the FP64 run's step decisions
+    dec = {}
+    for j, cp in enumerate(checkpoints):
+        row = {}
+        for r, (_, ss, c) in runs.items():
+            same = [kk for kk in range(nsys) if ss[j][(c, kk)] == st64[j][(0, kk)]]
+            diff = [kk for kk in range(nsys) if kk not in set(same)]
+            row[r] = {"same": len(same), "max_err_same_mv": max([errs[r][j][kk] for kk in same], default=0.0),
+                      "differ": len(diff), "max_err_differ_mv": max([errs[r][j][kk] for kk in diff], default=0.0)}
+        dec[f"{cp:g}ms"] = row
+    out["by_step_decisions"] = dec
+    tr64, tr32 = res["fp64"][2], res["mixed"][2]
+    sp = {r: [] for r in ("fp64", "mixed", "floor", "floor_fp32_resolution")}
+    for ty in sorted(tr64):
+        h = tr64[ty].shape[1] // ncopy
+        sp["fp64"] += spike_times(tr64[ty][:, :h], ty=ty)
+        sp["floor"] += spike_times(tr64[ty][:, h:2 * h], ty=ty)
+        sp["floor_fp32_resolution"] += spike_times(tr64[ty][:, 2 * h:3 * h], ty=ty)
+        sp["mixed"] += spike_times(tr32[ty], ty=ty)
+    out["spikes_mixed_vs_fp64"] = compare_spikes(sp["fp64"], sp["mixed"])
+    out["spikes_fp64_floor"] = compare_spikes(sp["fp64"], sp["floor"])
+    out["spikes_fp64_floor_fp32_resolution"] = compare_spikes(sp["fp64"], sp["floor_fp32_resolution"])
+    out["stopped"] = {"fp64": [x for x in res["fp64"][3] if x["copy"] == 0],
+                      "fp64_perturbed": [x for x in res["fp64"][3] if x["copy"] != 0],
+                      "mixed": res["mixed"][3]}
+    out["floor"] = ("the same FP64 run with every initial jitter + 1e-14 (V0 moved by a few units in the last "
+                    "place); floor_fp32_resolution: + 1e-7 (V0 moved by 2e-7..1e-6 mV, under FP32's resolution "
+                    "of a membrane voltage)")
     return out
 
 

@@ -33,6 +33,17 @@ namespace gbrkc {
 
 static thread_local std::string g_last_error;
 
+// GBRKC_MIXED_GR=fp64 keeps FP64 gating for granule pools in a mixed
+// engine.  A granule cell's step decisions (tolerance 1e-9) follow the last
+// bits of its channel currents, and a different decision moves its voltage
+// by up to ~0.1 mV within a millisecond; with FP64 gating its results are
+// the FP64 engine's, bit for bit, at the cost of its FP64 Markov and gating
+// updates (about half the mixed batch's throughput).
+bool mixed_granules_fp64() {
+  const char *v = getenv("GBRKC_MIXED_GR");
+  return v && (strcmp(v, "fp64") == 0 || strcmp(v, "FP64") == 0);
+}
+
 static int fail(int code, const char *fmt, ...) {
   char buf[512];
   va_list ap;
@@ -375,6 +386,7 @@ struct DeviceMem {
 
 struct PoolHost {
   int type;
+  bool f64 = false;                    // the pool's gating arithmetic: FP64 (vd) or FP32 (vf)
   std::vector<int> systems;            // engine system ids
   long nc = 0;
   int ncell = 0;
@@ -400,6 +412,8 @@ struct PoolHost {
   int max_nc = 0, min_nc = 1 << 30, max_ncell = 0;
   // launch configuration
   int team = TEAM_BLOCK, block = 256, grid = 1;
+  int grid_bw = GRID_BLOCK;                 // grid team: threads of each CTA that own elements
+  int grid_rl = 0, grid_maxdeg = 0;         // grid team: row slots per CTA, entries per slot (0: no copy)
   size_t smem = 0;
   int ws_in_smem = 0;
   long ws_tile = 0;
@@ -427,6 +441,7 @@ using namespace gbrkc;
 
 struct gbrkc_engine {
   int precision = GBRKC_FP64;
+  bool gr_f64 = false;                 // mixed precision: granule pools keep FP64 gating (GBRKC_MIXED_GR=fp64)
   bool built = false;
   std::vector<Template> templates;
   std::map<std::pair<int, std::vector<double>>, int> tmpl_index;
@@ -494,6 +509,7 @@ extern "C" int gbrkc_engine_create(int precision, gbrkc_engine **out) {
   if (e != cudaSuccess || ndev == 0) return fail(GBRKC_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
   std::unique_ptr<gbrkc_engine> E(new gbrkc_engine());
   E->precision = precision;
+  E->gr_f64 = precision == GBRKC_MIXED && mixed_granules_fp64();
   // lanes per warp that take single-lane systems: fewer systems in a warp
   // diverge less but need more warps (measured on the GB300: 1024 granule
   // cells on 32 SMs took 115 / 103 / 95 ms per simulated ms with 32 / 16 / 8
@@ -634,6 +650,37 @@ bool grid_team_fits(const gbrkc_engine *E, const PoolHost &P) {
   for (const HostSystem &S : E->systems)
     if (S.type != P.type) return false;
   return true;
+}
+
+// The grid team's shape for a system of nc compartments on at most cap
+// co-resident CTAs: the element-owning threads per CTA (bw, a power of two
+// from 32 to GRID_BLOCK) and the CTA count.  It minimises the elements of the
+// busiest CTA (every CTA integrates its elements' stages on its own SM's
+// FP64 pipe), then the CTA count (every CTA takes part in every barrier);
+// within the reduction's limits (at most GRID_MAX_BLOCKS chunks of bw
+// elements, GRID_MAX_ROWS per thread).  GBRKC_GRID_BW and GBRKC_GRID_CTAS
+// fix either.  Returns false when no shape fits.
+bool grid_shape(long nc, int cap, int *bw_out, int *ctas_out) {
+  const char *eb = getenv("GBRKC_GRID_BW"), *ec = getenv("GBRKC_GRID_CTAS");
+  const int want_bw = (eb && eb[0]) ? atoi(eb) : 0, want_ctas = (ec && ec[0]) ? atoi(ec) : 0;
+  long best_load = -1;
+  for (int bw = 32; bw <= GRID_BLOCK; bw *= 2) {
+    if (want_bw > 0 && bw != want_bw) continue;
+    const long chunks = (nc + bw - 1) / bw;
+    if (chunks > GRID_MAX_BLOCKS) continue;
+    long ctas = std::min<long>(cap, chunks);
+    if (want_ctas > 0) ctas = std::min<long>(cap, want_ctas);
+    if (ctas < 1) continue;
+    const long rows = (chunks + ctas - 1) / ctas;
+    if (rows > GRID_MAX_ROWS) continue;
+    const long load = rows * bw;
+    if (best_load < 0 || load < best_load || (load == best_load && ctas < *ctas_out)) {
+      best_load = load;
+      *bw_out = bw;
+      *ctas_out = (int)ctas;
+    }
+  }
+  return best_load > 0;
 }
 
 // Output compartments per cell: the voltage record (the soma; the
@@ -813,16 +860,31 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
   else if (P.max_nc <= 320) { P.team = TEAM_WARP; P.block = 128; }
   else if (grid_team_fits(E, P)) {
     // a lone large system: every SM of the device on it
-    const int g = (E->precision == GBRKC_FP64) ? grid_capacity<double>(P.type) : grid_capacity<float>(P.type);
-    const long nc = P.max_nc;
-    if (g > 0 && (nc + GRID_BLOCK - 1) / GRID_BLOCK <= GRID_MAX_BLOCKS &&
-        (nc + (long)g * GRID_BLOCK - 1) / ((long)g * GRID_BLOCK) <= GRID_MAX_ROWS) {
+    const int g = P.f64 ? grid_capacity<double>(P.type) : grid_capacity<float>(P.type);
+    int bw = 0, ctas = 0;
+    if (g > 0 && grid_shape(P.max_nc, g, &bw, &ctas)) {
       P.team = TEAM_GRID;
       P.block = GRID_BLOCK;
-      P.grid = g;
+      P.grid = ctas;
+      P.grid_bw = bw;
       P.ws_tile = (long)WS_VECS * ((P.max_nc + 1) & ~1);
       P.ws_in_smem = 0;
-      P.smem = 0;
+      // each CTA's operator rows in shared memory when they fit: row slots
+      // of the widest row (diagonal dropped) of any of the pool's systems
+      int maxdeg = 0;
+      for (size_t k = 0; k < P.systems.size(); k++) {
+        const bool own = P.sys_csr[k] >= 0;
+        const int *r = own ? P.s_row.data() + P.s_row0[P.sys_csr[k]] : P.t_row.data() + P.t_row0[P.sys_tmpl[k]];
+        const int nr = own ? P.sys_nc[k] : P.sys_ncomp[k];
+        for (int j = 0; j < nr; j++) maxdeg = std::max(maxdeg, r[j + 1] - r[j]);
+      }
+      const long rl = (P.max_nc + (long)ctas * bw - 1) / ((long)ctas * bw) * bw;
+      const bool fits = maxdeg > 0 && grid_rows_smem(rl, maxdeg) <= GRID_ROWS_SMEM_MAX;
+      const char *ec = getenv("GBRKC_GRID_ROWS_SMEM");
+      const bool want = !(ec && ec[0] == '0');
+      P.grid_rl = (int)rl;
+      P.grid_maxdeg = (fits && want) ? maxdeg : 0;
+      P.smem = P.grid_maxdeg ? grid_rows_smem(rl, maxdeg) : 0;
       return 0;
     }
     P.team = TEAM_CLUSTER16;
@@ -842,7 +904,7 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
       const long slot = (long)((((P.max_nc + 1) & ~1) + 256 * C - 1) / (256 * C)) * 256;
       const size_t need = ((size_t)WS_VECS * slot + CLUSTER_RED_DOUBLES) * sizeof(double);
       if (need > 200 * 1024 || slot / 256 > CLUSTER_MAX_ROWS) continue;
-      const int cap = (E->precision == GBRKC_FP64) ? cluster_capacity<double>(P.type, team, need)
+      const int cap = P.f64 ? cluster_capacity<double>(P.type, team, need)
                                                    : cluster_capacity<float>(P.type, team, need);
       if (cap < 1) continue;
       P.team = team;
@@ -895,6 +957,9 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
   UP(P.sys_ws, V.sys_ws); UP(P.ctl, V.ctl);
   V.grid_red = nullptr;
   V.grid_bar = nullptr;
+  V.grid_bw = P.grid_bw;
+  V.grid_rl = P.grid_rl;
+  V.grid_maxdeg = P.grid_maxdeg;
   if (P.team == TEAM_GRID) {
     const std::vector<double> red(2 * GRID_MAX_BLOCKS, 0.0);
     const std::vector<unsigned> bar(sizeof(GridBarrier) / sizeof(unsigned), 0u);
@@ -1015,16 +1080,29 @@ void fit_granule_warps(gbrkc_engine *E) {
   }
 }
 
+// The persistent launch's pool views and role boundaries; returns the CTA
+// count.  A mixed engine's FP64 granule pool goes to gr64.
 template <typename R>
-int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
-  MegaView<R> M{};
+int mega_pools(gbrkc_engine *E, MegaView<R> &M) {
   int end = 0;
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
-    M.pool[t] = P.systems.empty() ? PoolView<R>{} : pool_view<R>(P);
+    const bool wide = !std::is_same<R, double>::value && P.f64;
+    M.pool[t] = (P.systems.empty() || wide) ? PoolView<R>{} : pool_view<R>(P);
+    if (wide && t == GR) {
+      M.gr64 = P.vd;
+      M.gr_f64 = 1;
+    }
     end += E->role_ctas[t];
     M.role_end[t] = end;
   }
+  return end;
+}
+
+template <typename R>
+int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
+  MegaView<R> M{};
+  const int end = mega_pools<R>(E, M);
   if (end > E->mega_grid || end <= 0)
     return fail(GBRKC_ESTATE, "persistent launch: %d role CTAs for a grid of %d", end, E->mega_grid);
   M.gr_nc4 = E->pools[GR].team == TEAM_LANE4;
@@ -1088,7 +1166,7 @@ int launch_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
       return fail(GBRKC_ESTATE, "single-lane pool %d: launch shape does not cover its workspaces", t);
     if (P.team == TEAM_GRID) CUDA_TRY(cudaMemsetAsync(P.d_grid_bar, 0, sizeof(GridBarrier), E->streams[t]));
     CUDA_TRY(cudaEventRecord(E->ev_k0[t], E->streams[t]));
-    if (E->precision == GBRKC_FP64)
+    if (P.f64)
       rc = launch_pool<double>(t, P.vd, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
     else
       rc = launch_pool<float>(t, P.vf, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
@@ -1470,6 +1548,7 @@ static int build_impl(gbrkc_engine *E) {
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
     if (P.systems.empty()) continue;
+    P.f64 = E->precision == GBRKC_FP64 || (t == GR && E->gr_f64);
     int rc = assemble_pool(E, P);
     if (rc) return rc;
   }
@@ -1480,7 +1559,7 @@ static int build_impl(gbrkc_engine *E) {
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
     if (P.systems.empty()) continue;
-    int rc = (E->precision == GBRKC_FP64) ? upload_pool<double>(E, P, P.vd) : upload_pool<float>(E, P, P.vf);
+    int rc = P.f64 ? upload_pool<double>(E, P, P.vd) : upload_pool<float>(E, P, P.vf);
     if (rc) return rc;
   }
   if (E->mega) {
@@ -1690,7 +1769,7 @@ extern "C" int gbrkc_read(gbrkc_engine *E, int id, int field, int k, double *hos
     }
     case GBRKC_F_ION: {
       if (k < 0 || k >= NION[S->type]) return fail(GBRKC_EINVAL, "bad ion slot");
-      if (E->precision == GBRKC_FP64) {
+      if (P->f64) {
         CUDA_TRY(cudaMemcpy(host, (double *)P->d_ion + (size_t)k * P->nc + off, n * sizeof(double), cudaMemcpyDeviceToHost));
       } else {
         std::vector<float> tmp(n);
@@ -1718,7 +1797,7 @@ extern "C" int gbrkc_field_device_ptr(gbrkc_engine *E, int id, int field, double
     case GBRKC_F_V: base = P->d_v; break;
     case GBRKC_F_CA: base = P->d_ca; break;
     case GBRKC_F_REV: base = P->d_rev; break;
-    case GBRKC_F_IEXT: base = (E->precision == GBRKC_FP64) ? P->vd.iext : P->vf.iext; break;
+    case GBRKC_F_IEXT: base = P->f64 ? P->vd.iext : P->vf.iext; break;
     default: return fail(GBRKC_EINVAL, "field %d has no per-compartment device array", field);
   }
   *ptr = base ? base + off : nullptr;
@@ -1754,7 +1833,7 @@ extern "C" int gbrkc_set_stim(gbrkc_engine *E, int id, const int *comp, const do
   for (int c = 0; c < S->n; c++)
     if (comp[c] >= S->ncomp) return fail(GBRKC_EINVAL, "stimulus compartment out of range");
   const int c0 = P->sys_cell0[S->pool_index];
-  const bool f64 = E->precision == GBRKC_FP64;
+  const bool f64 = P->f64;
   int *dc = const_cast<int *>(f64 ? P->vd.stim_comp : P->vf.stim_comp);
   double *da = const_cast<double *>(f64 ? P->vd.stim_amp : P->vf.stim_amp);
   double *d0 = const_cast<double *>(f64 ? P->vd.stim_t0 : P->vf.stim_t0);
@@ -1791,7 +1870,7 @@ extern "C" int gbrkc_set_stim_type(gbrkc_engine *E, int type, const int *comp, c
     for (int c = 0; c < S.n; c++, cell++)
       if (comp[cell] >= S.ncomp) return fail(GBRKC_EINVAL, "stimulus compartment out of range");
   }
-  const bool f64 = E->precision == GBRKC_FP64;
+  const bool f64 = P.f64;
   int *dc = const_cast<int *>(f64 ? P.vd.stim_comp : P.vf.stim_comp);
   double *da = const_cast<double *>(f64 ? P.vd.stim_amp : P.vf.stim_amp);
   double *d0 = const_cast<double *>(f64 ? P.vd.stim_t0 : P.vf.stim_t0);
@@ -2074,8 +2153,7 @@ static int systems_reset_impl(gbrkc_engine *E, int first_id, int n, const gbrkc_
     if ((int)P->retired.size() > pi) P->retired[pi] = 0;
     cells += S.n;
   }
-  rc = (E->precision == GBRKC_FP64) ? upload_run<double>(E, *P, pi0, pi0 + n)
-                                    : upload_run<float>(E, *P, pi0, pi0 + n);
+  rc = P->f64 ? upload_run<double>(E, *P, pi0, pi0 + n) : upload_run<float>(E, *P, pi0, pi0 + n);
   if (rc) return rc;
   E->pending_init = true;
   if (P->type == GR && E->gr_active >= 0) E->gr_active += n;
@@ -2205,7 +2283,7 @@ extern "C" long gbrkc_rkc_coefficients(int m, double *out, long cap) {
 extern "C" long long gbrkc_system_bytes(int precision, int cell_type, int ncomp, int ncell) {
   if (cell_type < 0 || cell_type >= NTYPES || ncomp <= 0 || ncell <= 0) return fail(GBRKC_EINVAL, "bad shape");
   const long long nc = (long long)ncomp * ncell;
-  const long long rb = (precision == GBRKC_FP64) ? 8 : 4;
+  const long long rb = (precision == GBRKC_FP64 || (cell_type == GR && mixed_granules_fp64())) ? 8 : 4;
   long long b = nc * (WS_VECS * 8 + 10 * 8 + 2 + rb * (NION[cell_type] + NCOND[cell_type]));
   b += (long long)ncell * (3 * 4 + 4 * 8 + 2 * 4);          // stimulus, output maps, raster
   b += 12 * 4 + 8 + (long long)sizeof(Ctl);                  // system tables and controller
@@ -2224,13 +2302,7 @@ namespace {
 template <typename R>
 int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, int init, unsigned long long *scratch) {
   MegaView<R> M{};
-  int end = 0;
-  for (int t = 0; t < NTYPES; t++) {
-    PoolHost &P = E->pools[t];
-    M.pool[t] = P.systems.empty() ? PoolView<R>{} : pool_view<R>(P);
-    end += E->role_ctas[t];
-    M.role_end[t] = end;
-  }
+  const int end = mega_pools<R>(E, M);
   if (end > NOALLOC_MAX_CTAS)
     return fail(GBRKC_EINVAL, "persistent launch of %d CTAs exceeds the static scratch (%d CTAs)", end,
                 NOALLOC_MAX_CTAS);

@@ -121,6 +121,11 @@ struct PoolView {
   // sums of the reductions, double-buffered, and the grid barrier's words
   double *grid_red;                   // [2][GRID_MAX_BLOCKS]
   unsigned *grid_bar;                 // GridBarrier
+  int grid_bw;                        // threads of each CTA that own elements (a power of two, 32..GRID_BLOCK)
+  // grid team: each CTA's rows of the operator in shared memory (grid_rl
+  // row slots of grid_maxdeg entries each); grid_maxdeg 0 = read the rows
+  // from global memory
+  int grid_rl, grid_maxdeg;
 };
 
 // How a pool takes its synaptic current (solve_rkc.cu): granule cells add
@@ -180,6 +185,10 @@ constexpr int team_cluster_size(int team) {
 template <typename R>
 struct MegaView {
   PoolView<R> pool[NTYPES];
+  // mixed precision with FP64 granule pools: the granule role runs the FP64
+  // path on gr64 (pool[GR] is then unused)
+  PoolView<double> gr64;
+  int gr_f64;
   int role_end[NTYPES];
   int lane_warps, lane_extra;  // granule CTA b runs lane_warps (+1 if b < lane_extra) warps
   int gr_nc4;                 // every granule system has 4 compartments
@@ -197,17 +206,26 @@ constexpr int CLUSTER_BLOCK = 256;
 constexpr int CLUSTER_MAX_ROWS = 14;
 constexpr int CLUSTER_RED_DOUBLES = 2 * CLUSTER_MAX_ROWS + 8 * CLUSTER_MAX_ROWS + 2;
 constexpr int LANE_MAX_NC = 8;   // largest system integrated by a single lane
-// Grid team: CTAs of GRID_BLOCK threads; element i of a workspace vector is
-// owned by thread (i mod gridDim * GRID_BLOCK); a reduction covers at most
-// GRID_MAX_BLOCKS blocks of GRID_BLOCK elements and GRID_MAX_ROWS rows of
-// gridDim * GRID_BLOCK elements.
+// Grid team: CTAs of GRID_BLOCK threads, of which the first grid_bw (a power
+// of two) own elements: element i of a workspace vector is owned by thread
+// (i mod gridDim * grid_bw) of that numbering; a reduction covers at most
+// GRID_MAX_BLOCKS chunks of grid_bw elements and GRID_MAX_ROWS rows of
+// gridDim * grid_bw elements.
 constexpr int GRID_BLOCK = 256;
 constexpr int GRID_MAX_BLOCKS = 256;
 constexpr int GRID_MAX_ROWS = 8;
-// The grid barrier's words: arrivals, generation, abort flag.
+constexpr size_t GRID_ROWS_SMEM_MAX = 160 * 1024;   // shared memory for a CTA's operator rows
+// bytes of that copy: per row slot its entry count, 1/Cm, and maxdeg
+// (column, conductance) pairs
+constexpr size_t grid_rows_smem(long rl, long maxdeg) { return (size_t)rl * (12 + 12 * (size_t)maxdeg); }
+// The grid barrier's words, each on its own 128-byte line: the count of
+// arrivals since the launch began (a CTA's k-th barrier ends when it reaches
+// k * gridDim) and the abort flag.
 struct GridBarrier {
-  unsigned count, gen;
-  int abort, pad;
+  unsigned long long count;
+  unsigned long long pad0[15];
+  int abort;
+  int pad1[31];
 };
 
 template <typename R>

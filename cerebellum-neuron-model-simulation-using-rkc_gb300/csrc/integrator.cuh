@@ -126,35 +126,39 @@ struct ClusterTeam {
 
 // One system over every CTA of a cooperative launch (GridTeam): the
 // workspace stays in global memory (the L2 holds it), element i is owned by
-// thread i mod (gridDim * GRID_BLOCK), and the team barrier is a software
-// grid barrier.  The barrier's wait is bounded: a CTA that waits more than
-// GRID_SPIN_LIMIT polls raises the abort flag, after which no barrier waits
-// and every CTA leaves its system at the next tick (status ST_BARRIER); the
-// host reads the flag after the launch.  A cooperative launch makes every
-// CTA co-resident, so the bound is a guard, not a schedule.
+// thread i mod (gridDim * grid_bw) among each CTA's first grid_bw threads,
+// and the team barrier is a software grid barrier: every CTA adds one to a
+// counter (a reduction, no reply awaited) and polls it with acquire loads
+// until it reaches gridDim times the CTA's own barrier count.  The wait is
+// bounded: a CTA that waits more than GRID_SPIN_LIMIT polls raises the abort
+// flag, after which no barrier waits and every CTA leaves its system at the
+// next tick (status ST_BARRIER); the host reads the flag after the launch.
+// A cooperative launch makes every CTA co-resident, so the bound is a guard,
+// not a schedule.
 constexpr long GRID_SPIN_LIMIT = 1L << 22;
 
-__device__ __forceinline__ void grid_barrier(GridBarrier *b) {
+__device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// epoch: this CTA's barrier count (shared memory, only thread 0 uses it)
+__device__ __forceinline__ void grid_barrier(GridBarrier *b, unsigned long long *epoch) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile GridBarrier *vb = b;
     if (!vb->abort) {
-      // the generation can only move once this CTA has arrived
-      const unsigned g = atomicAdd(&b->gen, 0u);
+      const unsigned long long target = (*epoch += 1) * gridDim.x;
       __threadfence();
-      if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
-        atomicExch(&b->count, 0u);
-        __threadfence();
-        atomicAdd(&b->gen, 1u);
-      } else {
-        long it = 0;
-        while (atomicAdd(&b->gen, 0u) == g) {
-          if (++it > GRID_SPIN_LIMIT || vb->abort) {
-            atomicExch(&b->abort, 1);
-            break;
-          }
-          __nanosleep(64);
+      asm volatile("red.relaxed.gpu.global.add.u64 [%0], 1;" ::"l"(&b->count) : "memory");
+      long it = 0;
+      while (ld_acquire_gpu(&b->count) < target) {
+        if (++it > GRID_SPIN_LIMIT || vb->abort) {
+          atomicExch(&b->abort, 1);
+          break;
         }
+        if (it > 64) __nanosleep(32);
       }
       __threadfence();
     }
@@ -166,14 +170,24 @@ struct GridTeam {
   static constexpr int LS = 1, NCF = 0, CLUSTER = 0, GRID = 1;
   typedef WVec<1> Vec;
   GridBarrier *bar;
-  double *red;                 // [2][GRID_MAX_BLOCKS] block sums (global)
+  double *red;                 // [2][GRID_MAX_BLOCKS] chunk sums (global)
   double *wp;                  // [GRID_MAX_ROWS][8] warp partials (shared)
   double *res;                 // the reduction's result (shared)
+  unsigned long long *epoch;   // this CTA's barrier count (shared)
+  int bw;                      // threads of each CTA that own elements
+  // the CTA's operator rows in shared memory (maxdeg 0: none): row slot
+  // k * bw + t holds thread t's k-th element's entries
+  int maxdeg;
+  double *linv, *lg;           // [rl] 1/Cm, [rl * maxdeg] conductances
+  int *lcnt, *lcol;            // [rl] entry counts, [rl * maxdeg] columns (system-wide)
   __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off}; }
   __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
-  __device__ __forceinline__ int rank() const { return (int)blockIdx.x * GRID_BLOCK + (int)threadIdx.x; }
-  __device__ __forceinline__ int size() const { return (int)gridDim.x * GRID_BLOCK; }
-  __device__ __forceinline__ void sync() const { grid_barrier(bar); }
+  // threads past bw own nothing: a rank no loop over the elements reaches
+  __device__ __forceinline__ int rank() const {
+    return (int)threadIdx.x < bw ? (int)blockIdx.x * bw + (int)threadIdx.x : 0x3fffffff;
+  }
+  __device__ __forceinline__ int size() const { return (int)gridDim.x * bw; }
+  __device__ __forceinline__ void sync() const { grid_barrier(bar, epoch); }
   __device__ __forceinline__ bool aborted() const { return ((volatile GridBarrier *)bar)->abort != 0; }
 };
 
@@ -346,8 +360,48 @@ struct Sys {
   __device__ __forceinline__ V bvec() const { return tm.vec_at(W, (long)WS_B * Team::vstride(ncp)); }
   __device__ __forceinline__ V scratch() const { return tm.vec_at(W, (long)WS_SCRATCH * Team::vstride(ncp)); }
 
+  // Grid team: copy this CTA's rows of the operator (the rows of the
+  // elements its threads own, each thread its own) into shared memory, so
+  // that a stage's dydt reads only the neighbours' values from L2.
+  __device__ __forceinline__ void grid_rows_in() const {
+    if constexpr (Team::GRID > 0) {
+      if (tm.maxdeg == 0) return;
+      const int md = tm.maxdeg;
+      for (int i = tm.rank(), k = 0; i < nc; i += tm.size(), k++) {
+        int j = i, base = 0;
+        if (!(csr || ncell == 1)) {
+          const int cidx = i / ncomp;
+          j = i - cidx * ncomp;
+          base = cidx * ncomp;
+        }
+        const int lr = k * tm.bw + (int)threadIdx.x;
+        const int r0 = __ldg(row + j), r1 = __ldg(row + j + 1);
+        tm.lcnt[lr] = r1 - r0;
+        tm.linv[lr] = __ldg(invcm + j);
+        for (int q = 0; q < r1 - r0; q++) {
+          tm.lcol[lr * md + q] = base + __ldg(col + r0 + q);
+          tm.lg[lr * md + q] = __ldg(g + r0 + q);
+        }
+      }
+    }
+  }
+
   // dydt at compartment i (solve_rkc.cu:178-196): (-b + sum g (y_j - y_i)) / Cm
   __device__ __forceinline__ double rhs(const V y, int i) const {
+    if constexpr (Team::GRID > 0) {
+      if (tm.maxdeg > 0) {
+        // i is the calling thread's element: i = k * size + blockIdx * bw + t
+        const int size = tm.size(), k = i / size;
+        const int lr = k * tm.bw + (i - k * size - (int)blockIdx.x * tm.bw);
+        double d = -(bvec()[i]);
+        const double yi = y[i];
+        const int n = tm.lcnt[lr];
+        const int *cc = tm.lcol + lr * tm.maxdeg;
+        const double *gg = tm.lg + lr * tm.maxdeg;
+        for (int q = 0; q < n; q++) d = fma(gg[q], y[cc[q]] - yi, d);
+        return d * tm.linv[lr];
+      }
+    }
     double d = -(bvec()[i]);
     const double yi = y[i];
     int r0, r1, base, j;
@@ -453,34 +507,38 @@ struct Sys {
     return *res;
   }
 
-  // tree_sum on a grid team: cluster_tree_sum's additions in the same order.
+  // tree_sum on a grid team: the pairwise tree's additions in the same order.
   // Element i is owned by the thread that writes it in the team loops, so the
-  // aligned block of GRID_BLOCK elements starting at row k, CTA b (block
-  // index k * gridDim + b) lies in CTA b, one element per thread: levels 0-4
-  // are warp shuffles, 5-7 combine the block's 8 warp partials, the block sum
-  // goes to global memory, and after one grid barrier warp 0 of every CTA
-  // combines all block sums (levels 8 and up), every CTA computing the same
-  // value.  The block sums are double-buffered, as on a cluster.
+  // aligned chunk of bw elements (a power of two) starting at row k, CTA b
+  // (chunk index k * gridDim + b) lies in CTA b, one element per thread:
+  // levels 0-4 are warp shuffles, the next combine the chunk's bw / 32 warp
+  // partials, the chunk sum goes to global memory, and after one grid barrier
+  // warp 0 of every CTA combines all chunk sums (the remaining levels), every
+  // CTA computing the same value.  The chunk sums are double-buffered, as on
+  // a cluster.
   __device__ __forceinline__ double grid_tree_sum(const V a, int n) const {
     if constexpr (Team::GRID > 0) {
-      constexpr int B = GRID_BLOCK, RR = GRID_MAX_BLOCKS / 32;
+      constexpr int RR = GRID_MAX_BLOCKS / 32;
       const int t = threadIdx.x, lane = t & 31, warp = t >> 5, b = blockIdx.x, G = gridDim.x;
+      const int B = tm.bw, nw = B >> 5;
       const int size = G * B;
       const int rows = (n + size - 1) / size;
       double *red = tm.red, *wp = tm.wp;
       const int buf = red_buf;
       red_buf ^= 1;
-      for (int k = 0; k < rows; k++) {
-        const int i0 = k * size + b * B;
-        if (i0 >= n) break;
-        const int i = i0 + t;
-        double x = (i < n) ? a[i] : 0.0;
+      if (t < B) {
+        for (int k = 0; k < rows; k++) {
+          const int i0 = k * size + b * B;
+          if (i0 >= n) break;
+          const int i = i0 + t;
+          double x = (i < n) ? a[i] : 0.0;
 #pragma unroll
-        for (int st = 1; st < 32; st *= 2) {
-          const double y = __shfl_down_sync(0xffffffffu, x, st);
-          if ((lane & (2 * st - 1)) == 0 && i + st < n) x = x + y;
+          for (int st = 1; st < 32; st *= 2) {
+            const double y = __shfl_down_sync(0xffffffffu, x, st);
+            if ((lane & (2 * st - 1)) == 0 && i + st < n) x = x + y;
+          }
+          if (lane == 0) wp[k * 8 + warp] = x;
         }
-        if (lane == 0) wp[k * 8 + warp] = x;
       }
       __syncthreads();
       if (t < rows) {
@@ -488,12 +546,12 @@ struct Sys {
         if (i0 < n) {
           double w[8];
 #pragma unroll
-          for (int j = 0; j < 8; j++) w[j] = wp[t * 8 + j];
+          for (int j = 0; j < 8; j++) w[j] = (j < nw) ? wp[t * 8 + j] : 0.0;
 #pragma unroll
           for (int st = 1; st < 8; st *= 2)
 #pragma unroll
             for (int j = 0; j + st < 8; j += 2 * st)
-              if (i0 + (j + st) * 32 < n) w[j] = w[j] + w[j + st];
+              if (j + st < nw && i0 + (j + st) * 32 < n) w[j] = w[j] + w[j + st];
           red[buf * GRID_MAX_BLOCKS + t * G + b] = w[0];
         }
       }
@@ -1067,6 +1125,7 @@ __device__ __forceinline__ void run_system(const PoolView<R> &P, const Team &tm,
   if (P.ws_in_smem) ws_in(tm, W, gws, wsn);
   Sys<CT, R, Team> S(P, tm, s, W);
   S.c = P.ctl[s];
+  S.grid_rows_in();
   if (init) {
     S.initialize();
     S.c.status &= ~ST_INIT;

@@ -1,3 +1,4 @@
+#include <type_traits>
 // The advance kernels.  k_advance: one launch advances every system of one
 // pool by n_iv output intervals (or initialises them), entirely on the
 // device.  Single lanes take the tiniest systems (one system per thread),
@@ -71,9 +72,18 @@ __global__ void __launch_bounds__(CLUSTER_BLOCK, 1) k_advance_cluster(const __gr
 template <int CT, typename R>
 __global__ void __launch_bounds__(GRID_BLOCK, 1) k_advance_grid(const __grid_constant__ PoolView<R> P, double t0,
                                                                  int n_iv, int iv0, int init) {
+  extern __shared__ __align__(16) double grid_smem[];
   __shared__ double s_wp[GRID_MAX_ROWS * 8];
   __shared__ double s_res;
-  const GridTeam tm{(GridBarrier *)P.grid_bar, P.grid_red, s_wp, &s_res};
+  __shared__ unsigned long long s_epoch;
+  if (threadIdx.x == 0) s_epoch = 0;     // the counter is zeroed before every launch
+  __syncthreads();
+  // the operator rows' copy: [rl] 1/Cm, [rl * maxdeg] g, [rl] counts, [rl * maxdeg] columns
+  const long rl = P.grid_rl, md = P.grid_maxdeg;
+  double *linv = grid_smem, *lg = grid_smem + rl;
+  int *lcnt = (int *)(lg + rl * md), *lcol = lcnt + rl;
+  const GridTeam tm{(GridBarrier *)P.grid_bar, P.grid_red, s_wp, &s_res, &s_epoch, P.grid_bw, P.grid_maxdeg,
+                    linv, lg, lcnt, lcol};
   for (int s = 0; s < P.nsys; s++) run_system<CT, R, GridTeam>(P, tm, s, nullptr, t0, n_iv, iv0, init != 0);
 }
 
@@ -129,6 +139,15 @@ __global__ void __launch_bounds__(MEGA_BLOCK, 1) k_mega(const __grid_constant__ 
     case GR:
       // single-lane granule systems on the CTA's first warps
       if ((int)(threadIdx.x >> 5) < M.lane_warps + ((int)blockIdx.x < M.lane_extra ? 1 : 0)) {
+        if constexpr (!std::is_same<R, double>::value) {
+          if (M.gr_f64) {
+            if (M.gr_nc4)
+              run_lanes_regs<GR, double, MEGA_BLOCK, 4>(M.gr64, M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
+            else
+              run_lanes<GR, double, MEGA_BLOCK>(M.gr64, M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
+            break;
+          }
+        }
         if (M.gr_nc4)
           run_lanes_regs<GR, R, MEGA_BLOCK, 4>(M.pool[GR], M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
         else
@@ -271,7 +290,7 @@ int launch_pool(int type, const PoolView<R> &P, int team, int grid, int block, s
   void *args[] = {(void *)&Pc, (void *)&t0, (void *)&n_iv, (void *)&iv0, (void *)&init};
   if (team == TEAM_GRID) {
     if (block != GRID_BLOCK) return (int)cudaErrorInvalidConfiguration;
-    return (int)cudaLaunchCooperativeKernel(k, dim3(grid), dim3(block), args, 0, (cudaStream_t)stream);
+    return (int)cudaLaunchCooperativeKernel(k, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
   }
   if (team_cluster_size(team) > 0) {
     if (block != CLUSTER_BLOCK || grid % team_cluster_size(team) != 0) return (int)cudaErrorInvalidConfiguration;

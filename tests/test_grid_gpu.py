@@ -2,9 +2,9 @@
 runs as one grid team: every CTA of a cooperative launch takes a slice of
 its workspace (kept in global memory, in L2), and a bounded software grid
 barrier separates the stages.  Bit for bit with the oracle like every other
-team: the reductions combine 256-element block sums in the same pairwise
-order.  GBRKC_GRID_MIN_NC lowers the size threshold so that small cases take
-the path."""
+team: the reductions combine chunk sums (a power-of-two chunk per CTA) in the
+same pairwise order.  GBRKC_GRID_MIN_NC lowers the size threshold so that
+small cases take the path; GBRKC_GRID_BW and GBRKC_GRID_CTAS force a shape."""
 import numpy as np
 import pytest
 
@@ -21,13 +21,57 @@ def _sms():
     return torch.cuda.get_device_properties(0).multi_processor_count
 
 
+def grid_shape(nc, cap, want_bw=0, want_ctas=0):
+    """The engine's choice of (element-owning threads per CTA, CTAs): the
+    smallest busiest-CTA load, then the fewest CTAs, within 256 chunks and 8
+    rows per thread."""
+    best = None
+    for bw in (32, 64, 128, 256):
+        if want_bw and bw != want_bw:
+            continue
+        chunks = -(-nc // bw)
+        if chunks > 256:
+            continue
+        ctas = min(cap, want_ctas) if want_ctas else min(cap, chunks)
+        rows = -(-chunks // ctas)
+        if rows > 8:
+            continue
+        key = (rows * bw, ctas)
+        if best is None or key < best[0]:
+            best = (key, bw, ctas)
+    return best[1], best[2]
+
+
+def test_grid_shape_rule():
+    assert grid_shape(14400, 152) == (128, 113)      # the Purkinje 3x3 system
+    assert grid_shape(57600, 152) == (256, 152)
+    assert grid_shape(1600, 152) == (32, 50)
+
+
 @pytest.mark.parametrize("name", ["pkj_cell", "pkj_2x1_gj", "gr_full", "go_2x2_gj"])
 def test_grid_team_bit_exact(oracle, monkeypatch, name):
     monkeypatch.setenv("GBRKC_GRID_MIN_NC", "300")
     n = HORIZON.get(name, 64)
     s, eng, sid = run_pair(oracle, name, [1, n // 2 - 1, n // 2])
     persistent, ctas = eng.launch_layout()
-    assert persistent is False and max(ctas) == _sms(), ctas
+    assert persistent is False and max(ctas) == grid_shape(s.nc, _sms())[1], ctas
+    eng.close()
+
+
+@pytest.mark.parametrize("bw,ctas,rows_smem", [(32, 0, 1), (64, 0, 1), (128, 0, 1), (256, 0, 1), (64, 7, 1),
+                                                (256, 3, 1), (128, 0, 0), (64, 7, 0)])
+def test_grid_team_shapes_bit_exact(oracle, monkeypatch, bw, ctas, rows_smem):
+    """Every element-owning width, few CTAs (several rows per thread), and
+    the operator's rows read from shared memory or (GBRKC_GRID_ROWS_SMEM=0)
+    from global memory."""
+    monkeypatch.setenv("GBRKC_GRID_MIN_NC", "300")
+    monkeypatch.setenv("GBRKC_GRID_BW", str(bw))
+    monkeypatch.setenv("GBRKC_GRID_ROWS_SMEM", str(rows_smem))
+    if ctas:
+        monkeypatch.setenv("GBRKC_GRID_CTAS", str(ctas))
+    s, eng, sid = run_pair(oracle, "pkj_2x1_gj", [1, 15, 16])
+    persistent, got = eng.launch_layout()
+    assert persistent is False and max(got) == grid_shape(s.nc, _sms(), bw, ctas)[1], got
     eng.close()
 
 
@@ -43,7 +87,7 @@ def test_grid_io_network(oracle, monkeypatch):
     eng = G.Engine(G.FP64)
     sid = eng.add_system(M.IO, 12, 12, M.io_rows(), jit, stim=stim, gap=True)
     eng.build()
-    assert max(eng.launch_layout()[1]) == _sms()
+    assert max(eng.launch_layout()[1]) == grid_shape(s.nc, _sms())[1]
     t = 0.0
     for chunk in (1, 15, 16):
         eng.advance(t, chunk)
