@@ -877,6 +877,8 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0,
                     help="population fraction of the mixed batch (small profiling cases; 1 = the benchmark)")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-pkj3x3", action="store_true",
+                    help="leave out the Purkinje 3x3 record that the mixed workload's line carries")
     ap.add_argument("--serve-slots", type=int, default=1, help="multiplier on the serving arenas' slot counts")
     ap.add_argument("--serve-ts", type=float, nargs=2, default=None, metavar=("LO", "HI"),
                     help="request durations U[LO, HI] ms (default 5 25 beside the mixed workload, 50 1000 for "
@@ -919,6 +921,8 @@ def main():
         return
     specs, wl = workload(args.config, args.scale)
     out = run_batch(args, G, configs, torch, specs, wl, precision, rank, world, dist)
+    if rank == 0 and args.config == "mixed" and args.scale == 1.0 and not args.no_pkj3x3:
+        out["pkj3x3"] = pkj3x3_record(args, G, configs, torch)
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:
@@ -1035,7 +1039,9 @@ def run_batch(args, G, configs, torch, specs, wl, precision, rank, world, dist):
         per_launch_units, per_launch_ms = units / args.steps, dev_ms / args.steps
     else:
         dom = max(range(4), key=lambda k: kern_ms[k])
-        kname, key = f"k_advance<{names[dom]}>", names[dom]
+        team = eng.type_team(dom)
+        base = {"grid": "k_advance_grid", "cluster": "k_advance_cluster"}.get(team, "k_advance")
+        kname, key = f"{base}<{names[dom]}>", names[dom]
         per_launch_units, per_launch_ms = units_t[dom] / args.steps, kern_ms[dom] / args.steps
     achieved = bpu * per_launch_units / (per_launch_ms * 1e-3) / 1e9 if per_launch_ms > 0 else 0.0
     traffic, fp64_ncu = None, None
@@ -1125,6 +1131,24 @@ def run_batch(args, G, configs, torch, specs, wl, precision, rank, world, dist):
     if cpu:
         res["cpu_baseline"] = cpu
     return res
+
+
+def pkj3x3_record(args, G, configs, torch, steps=5):
+    """The Purkinje 3x3 workload (one 14 400-compartment system, plain FP64,
+    [0, 200] ms) timed beside the mixed workload on rank 0: the same timing
+    rules as its own line (`--config pkj3x3`), in `steps` timed steps after
+    the warm-up."""
+    import copy
+    a = copy.copy(args)
+    a.config, a.window_ms, a.steps = "pkj3x3", WINDOW_MS["pkj3x3"], steps
+    a.no_cpu, a.no_fp64_compare, a.serve_requests = True, True, 0
+    specs, wl = workload("pkj3x3", 1.0)
+    r = run_batch(a, G, configs, torch, specs, wl, "fp64", 0, 1, None)
+    return {"metric": r["metric"], "value": r["value"], "unit": r["unit"], "e2e": r["e2e"]["value"],
+            "ms_per_step": r["ms_per_step"], "steps": steps, "warmup": a.warmup, "dtype": r["dtype"],
+            "config": r["config"], "wall_s_window": r["ms_per_step"] * steps * 1e-3,
+            "kernel": r["roofline"]["kernel"], "gpu_launches": r["gpu_launches"],
+            "stopped_systems": r["run"]["stopped_systems"], "clocks": r["clocks"]}
 
 
 def config_key(args, wl):

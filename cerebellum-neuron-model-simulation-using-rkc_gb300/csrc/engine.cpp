@@ -958,6 +958,12 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
   V.grid_red = nullptr;
   V.grid_bar = nullptr;
   V.grid_bw = P.grid_bw;
+  {
+    // fence.acq_rel + acquire polls; GBRKC_GRID_FENCE=sc for __threadfence
+    // on both sides of the wait (8% slower on the Purkinje 3x3 system)
+    const char *f = getenv("GBRKC_GRID_FENCE");
+    V.grid_light = (f && strcmp(f, "sc") == 0) ? 0 : 1;
+  }
   V.grid_rl = P.grid_rl;
   V.grid_maxdeg = P.grid_maxdeg;
   if (P.team == TEAM_GRID) {
@@ -1926,6 +1932,16 @@ extern "C" int gbrkc_launch_layout(gbrkc_engine *E, int *ctas_per_type) {
   for (int t = 0; t < NTYPES; t++)
     ctas_per_type[t] = E->mega ? E->role_ctas[t] : E->pools[t].systems.empty() ? 0 : E->pools[t].grid;
   return E->mega ? 1 : 0;
+}
+extern "C" int gbrkc_type_team(gbrkc_engine *E, int type) {
+  if (!E || type < 0 || type >= NTYPES) return fail(GBRKC_EINVAL, "bad arguments");
+  if (!E->built) return fail(GBRKC_ESTATE, "engine not built");
+  const PoolHost &P = E->pools[type];
+  if (P.systems.empty()) return 0;
+  if (E->mega) return GBRKC_TEAM_MEGA;
+  if (P.team == TEAM_GRID) return GBRKC_TEAM_GRID;
+  if (team_cluster_size(P.team) > 0) return GBRKC_TEAM_CLUSTER;
+  return GBRKC_TEAM_POOL;
 }
 extern "C" float gbrkc_last_kernel_ms(gbrkc_engine *E, int type) {
   return (E && type >= 0 && type < NTYPES) ? E->last_kernel_ms[type] : 0.0f;

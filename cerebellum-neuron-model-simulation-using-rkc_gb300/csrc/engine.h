@@ -122,6 +122,7 @@ struct PoolView {
   double *grid_red;                   // [2][GRID_MAX_BLOCKS]
   unsigned *grid_bar;                 // GridBarrier
   int grid_bw;                        // threads of each CTA that own elements (a power of two, 32..GRID_BLOCK)
+  int grid_light;                     // grid barrier: acq_rel fence + acquire polls (1) or sc fences (0)
   // grid team: each CTA's rows of the operator in shared memory (grid_rl
   // row slots of grid_maxdeg entries each); grid_maxdeg 0 = read the rows
   // from global memory

@@ -143,14 +143,20 @@ __device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long
   return v;
 }
 
-// epoch: this CTA's barrier count (shared memory, only thread 0 uses it)
-__device__ __forceinline__ void grid_barrier(GridBarrier *b, unsigned long long *epoch) {
+// epoch: this CTA's barrier count (shared memory, only thread 0 uses it).
+// light: order the arrival with fence.acq_rel.gpu and rely on the acquire
+// polls (the CTA's barrier carries both to its other threads); else
+// fence.sc.gpu (__threadfence) before the arrival and after the wait.
+__device__ __forceinline__ void grid_barrier(GridBarrier *b, unsigned long long *epoch, int light) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile GridBarrier *vb = b;
     if (!vb->abort) {
       const unsigned long long target = (*epoch += 1) * gridDim.x;
-      __threadfence();
+      if (light)
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+      else
+        __threadfence();
       asm volatile("red.relaxed.gpu.global.add.u64 [%0], 1;" ::"l"(&b->count) : "memory");
       long it = 0;
       while (ld_acquire_gpu(&b->count) < target) {
@@ -160,7 +166,7 @@ __device__ __forceinline__ void grid_barrier(GridBarrier *b, unsigned long long 
         }
         if (it > 64) __nanosleep(32);
       }
-      __threadfence();
+      if (!light) __threadfence();
     }
   }
   __syncthreads();
@@ -175,6 +181,7 @@ struct GridTeam {
   double *res;                 // the reduction's result (shared)
   unsigned long long *epoch;   // this CTA's barrier count (shared)
   int bw;                      // threads of each CTA that own elements
+  int light;                   // the barrier's fences (grid_barrier)
   // the CTA's operator rows in shared memory (maxdeg 0: none): row slot
   // k * bw + t holds thread t's k-th element's entries
   int maxdeg;
@@ -187,7 +194,7 @@ struct GridTeam {
     return (int)threadIdx.x < bw ? (int)blockIdx.x * bw + (int)threadIdx.x : 0x3fffffff;
   }
   __device__ __forceinline__ int size() const { return (int)gridDim.x * bw; }
-  __device__ __forceinline__ void sync() const { grid_barrier(bar, epoch); }
+  __device__ __forceinline__ void sync() const { grid_barrier(bar, epoch, light); }
   __device__ __forceinline__ bool aborted() const { return ((volatile GridBarrier *)bar)->abort != 0; }
 };
 

@@ -82,8 +82,8 @@ __global__ void __launch_bounds__(GRID_BLOCK, 1) k_advance_grid(const __grid_con
   const long rl = P.grid_rl, md = P.grid_maxdeg;
   double *linv = grid_smem, *lg = grid_smem + rl;
   int *lcnt = (int *)(lg + rl * md), *lcol = lcnt + rl;
-  const GridTeam tm{(GridBarrier *)P.grid_bar, P.grid_red, s_wp, &s_res, &s_epoch, P.grid_bw, P.grid_maxdeg,
-                    linv, lg, lcnt, lcol};
+  const GridTeam tm{(GridBarrier *)P.grid_bar, P.grid_red, s_wp, &s_res, &s_epoch, P.grid_bw, P.grid_light,
+                    P.grid_maxdeg, linv, lg, lcnt, lcol};
   for (int s = 0; s < P.nsys; s++) run_system<CT, R, GridTeam>(P, tm, s, nullptr, t0, n_iv, iv0, init != 0);
 }
 

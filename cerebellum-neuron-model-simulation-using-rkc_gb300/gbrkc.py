@@ -127,6 +127,7 @@ def lib() -> C.CDLL:
         L.gbrkc_retired_systems.argtypes = [P]
         L.gbrkc_autotune.argtypes = [P, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.gbrkc_launch_layout.argtypes = [P, C.POINTER(C.c_int)]
+        L.gbrkc_type_team.argtypes = [P, C.c_int]
         L.gbrkc_compartment_updates.argtypes = [P, C.c_int]
         L.gbrkc_compartment_updates.restype = C.c_longlong
         L.gbrkc_systems_reset.argtypes = [P, C.c_int, C.c_int, C.POINTER(ResetDesc)]
@@ -357,6 +358,16 @@ class Engine:
         if rc < 0:
             _check(rc)
         return bool(rc), list(c)
+
+    TEAMS = {1: "mega", 2: "grid", 3: "cluster", 4: "pool"}
+
+    def type_team(self, cell_type: int) -> str:
+        """How the type's systems are integrated: "mega", "grid", "cluster",
+        "pool", or "" for an empty type."""
+        rc = lib().gbrkc_type_team(self.h, cell_type)
+        if rc < 0:
+            _check(rc)
+        return self.TEAMS.get(rc, "")
 
     def retired(self) -> int:
         return lib().gbrkc_retired_systems(self.h)

@@ -156,6 +156,14 @@ float gbrkc_last_kernel_ms(gbrkc_engine *e, int cell_type);
  * negative on error. */
 int gbrkc_launch_layout(gbrkc_engine *e, int *ctas_per_type);
 
+/* How a cell type's systems are integrated, for reports: GBRKC_TEAM_MEGA (the
+ * persistent mixed-role launch), GBRKC_TEAM_GRID (one system over the SMs of a
+ * cooperative launch), GBRKC_TEAM_CLUSTER (one system per thread-block
+ * cluster) or GBRKC_TEAM_POOL (the type's own launch: a lane, warp or CTA per
+ * system); 0 for an empty type, negative on error. */
+enum { GBRKC_TEAM_MEGA = 1, GBRKC_TEAM_GRID = 2, GBRKC_TEAM_CLUSTER = 3, GBRKC_TEAM_POOL = 4 };
+int gbrkc_type_team(gbrkc_engine *e, int cell_type);
+
 /* ---- chemical synapses (network mode) ----------------------------------
  * The reference's RKC network path (syn.cu; main.cu:300-305 with
  * network_sim true): mossy fibre -> granule (Poisson input), granule ->

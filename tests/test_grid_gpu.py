@@ -75,6 +75,18 @@ def test_grid_team_shapes_bit_exact(oracle, monkeypatch, bw, ctas, rows_smem):
     eng.close()
 
 
+@pytest.mark.parametrize("name", ["pkj_2x1_gj", "go_2x2_gj"])
+def test_grid_team_sc_fence_barrier_bit_exact(oracle, monkeypatch, name):
+    """The grid barrier with sequentially consistent fences on both sides of
+    the wait (GBRKC_GRID_FENCE=sc) instead of fence.acq_rel and acquire
+    polls."""
+    monkeypatch.setenv("GBRKC_GRID_MIN_NC", "300")
+    monkeypatch.setenv("GBRKC_GRID_FENCE", "sc")
+    s, eng, sid = run_pair(oracle, name, [1, 15, 16])
+    assert eng.launch_layout()[0] is False
+    eng.close()
+
+
 def test_grid_io_network(oracle, monkeypatch):
     """A 12x12 olive network (nonlinear gap junctions across CTAs)."""
     monkeypatch.setenv("GBRKC_GRID_MIN_NC", "400")
@@ -113,6 +125,7 @@ def test_grid_system_beyond_cluster_capacity(oracle):
     eng.build()
     persistent, ctas = eng.launch_layout()
     assert not persistent and ctas[M.PKJ] == _sms(), ctas
+    assert eng.type_team(M.PKJ) == "grid" and eng.type_team(M.GR) == ""
     t = 0.0
     for chunk in (1, 2):
         eng.advance(t, chunk)
