@@ -172,10 +172,12 @@ def workload(name, scale=1.0):
                                        "256 PC x1600 (5 tapered trees) + IO 16x16 net x3; currents U[0,0.05] nA GrC, "
                                        "U[0,0.4] nA GoC/PC, U[0,6] uA/cm^2 IO")
     if name == "sweep":
-        return configs.sweep_batch(), ("parameter sweep: 32768 GrC x4 + 32768 GoC x131 (one seeded tree) independent "
-                                       "systems, every channel density x U[0.8,1.2] per instance, step current "
-                                       "U[0,0.4] nA from t = 0, durations U[100,1000] ms as per-system interval "
-                                       "budgets, no gap junctions")
+        n = max(1, int(32768 * scale))
+        return configs.sweep_batch(n_gr=n, n_go=n), (
+            f"parameter sweep: {n} GrC x4 + {n} GoC x131 (one seeded tree) independent systems, every channel "
+            "density x U[0.8,1.2] per instance, step current U[0,0.4] nA from t = 0, durations U[100,1000] ms as "
+            "per-system interval budgets, no gap junctions" + ("" if scale == 1.0 else
+                                                               f" (populations scaled x{scale:g}: small case)"))
     if name == "pkj3x3":
         return configs.pkj_grid(3, 3), ("Purkinje 3x3 grid, one RKC system of 14400 compartments (one seeded tapered "
                                         "tree), x-neighbour gap junctions, constant 0.5 nA at every soma, the "
@@ -263,11 +265,26 @@ def run_network(args, G, configs, torch, precision, rank, world, dist):
             tr = res[name][1]
             sp_of[name] = sum((spike_times(tr[ty], ty=ty) for ty in sorted(tr)), [])
         fp64_v = walls["fp64"][1] / walls["fp64"][0]
+        # per system, over the systems that stopped in none of the three runs
+        # (a stopped system keeps the state it diverged with)
+        out_of = {x["index"] for name in ("run", "fp64", "fp64_perturbed") for x in res[name][2]}
+        bounds = np.cumsum([0] + [sp.nc for sp in specs])
+        keep = [k for k in ids if k not in out_of]
+
+        def max_err(a, b, ty=None):
+            e = [float(np.max(np.abs(a[bounds[k]:bounds[k + 1]] - b[bounds[k]:bounds[k + 1]])))
+                 for k in keep if ty is None or specs[k].cell_type == ty]
+            return max(e, default=0.0)
+
+        by_type = {TYPE_NAMES[ty]: {"mixed": max_err(res["run"][0], res["fp64"][0], ty),
+                                    "floor": max_err(res["fp64_perturbed"][0], res["fp64"][0], ty)}
+                   for ty in sorted({sp.cell_type for sp in specs})}
         vs_fp64 = {"fp64_value": fp64_v, "mixed_value": units / wall, "ratio": (units / wall) / fp64_v,
                    "window_ms": [0.0, window], "unit": "compartment-updates/s (host wall clock, same window)",
-                   "accuracy": {"max_abs_err_mv": float(np.max(np.abs(res["run"][0] - res["fp64"][0]))),
-                                "sensitivity_floor_mv": float(np.max(np.abs(res["fp64_perturbed"][0] -
-                                                                            res["fp64"][0]))),
+                   "accuracy": {"max_abs_err_mv": max_err(res["run"][0], res["fp64"][0]),
+                                "sensitivity_floor_mv": max_err(res["fp64_perturbed"][0], res["fp64"][0]),
+                                "max_abs_err_mv_by_type": by_type,
+                                "systems_compared": len(keep),
                                 "at_ms": window,
                                 "spikes_mixed_vs_fp64": compare_spikes(sp_of["fp64"], sp_of["run"]),
                                 "spikes_fp64_floor": compare_spikes(sp_of["fp64"], sp_of["fp64_perturbed"]),

@@ -653,12 +653,12 @@ bool grid_team_fits(const gbrkc_engine *E, const PoolHost &P) {
 }
 
 // The grid team's shape for a system of nc compartments on at most cap
-// co-resident CTAs: the element-owning threads per CTA (bw, a power of two
-// from 32 to GRID_BLOCK) and the CTA count.  It minimises the elements of the
-// busiest CTA (every CTA integrates its elements' stages on its own SM's
-// FP64 pipe), then the CTA count (every CTA takes part in every barrier);
-// within the reduction's limits (at most GRID_MAX_BLOCKS chunks of bw
-// elements, GRID_MAX_ROWS per thread).  GBRKC_GRID_BW and GBRKC_GRID_CTAS
+// co-resident CTAs: the threads per CTA (bw, a power of two from 32 to
+// GRID_BLOCK, every one owning elements) and the CTA count.  It minimises the
+// elements of the busiest CTA (every CTA integrates its elements' stages on
+// its own SM's FP64 pipe), then the CTA count (every CTA takes part in every
+// barrier); within the reduction's limits (at most GRID_MAX_BLOCKS chunks of
+// bw elements, GRID_MAX_ROWS per thread).  GBRKC_GRID_BW and GBRKC_GRID_CTAS
 // fix either.  Returns false when no shape fits.
 bool grid_shape(long nc, int cap, int *bw_out, int *ctas_out) {
   const char *eb = getenv("GBRKC_GRID_BW"), *ec = getenv("GBRKC_GRID_CTAS");
@@ -863,8 +863,11 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
     const int g = P.f64 ? grid_capacity<double>(P.type) : grid_capacity<float>(P.type);
     int bw = 0, ctas = 0;
     if (g > 0 && grid_shape(P.max_nc, g, &bw, &ctas)) {
+      // CTAs of exactly the owning threads: every warp of a CTA repeats the
+      // controller's scalar FP64 work, so a warp without elements only
+      // costs FP64 issue slots
       P.team = TEAM_GRID;
-      P.block = GRID_BLOCK;
+      P.block = bw;
       P.grid = ctas;
       P.grid_bw = bw;
       P.ws_tile = (long)WS_VECS * ((P.max_nc + 1) & ~1);

@@ -189,7 +189,8 @@ struct GridTeam {
   int *lcnt, *lcol;            // [rl] entry counts, [rl * maxdeg] columns (system-wide)
   __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off}; }
   __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
-  // threads past bw own nothing: a rank no loop over the elements reaches
+  // (the CTA has bw threads; a thread past bw would own nothing: a rank no
+  // loop over the elements reaches)
   __device__ __forceinline__ int rank() const {
     return (int)threadIdx.x < bw ? (int)blockIdx.x * bw + (int)threadIdx.x : 0x3fffffff;
   }
@@ -896,7 +897,11 @@ struct Sys {
     c.errold = err;
     c.hold = h;
     c.idid = c.last ? 1 : 2;
-    tm.sync();
+    // A grid team skips this barrier: every thread reads and writes only its
+    // own elements until the next step's first barrier, the error norm's
+    // grid barrier has already ordered every neighbour read of this attempt,
+    // and its chunk sums are double-buffered.
+    if constexpr (Team::GRID == 0) tm.sync();
     return ATT_ACCEPT;
   }
 

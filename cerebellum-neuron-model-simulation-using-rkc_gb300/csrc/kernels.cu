@@ -289,7 +289,8 @@ int launch_pool(int type, const PoolView<R> &P, int team, int grid, int block, s
   PoolView<R> Pc = P;
   void *args[] = {(void *)&Pc, (void *)&t0, (void *)&n_iv, (void *)&iv0, (void *)&init};
   if (team == TEAM_GRID) {
-    if (block != GRID_BLOCK) return (int)cudaErrorInvalidConfiguration;
+    if (block < 32 || block > GRID_BLOCK || (block & (block - 1)) != 0 || block != P.grid_bw)
+      return (int)cudaErrorInvalidConfiguration;
     return (int)cudaLaunchCooperativeKernel(k, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
   }
   if (team_cluster_size(team) > 0) {
