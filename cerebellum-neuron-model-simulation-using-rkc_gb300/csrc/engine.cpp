@@ -414,6 +414,8 @@ struct PoolHost {
   int team = TEAM_BLOCK, block = 256, grid = 1;
   int grid_bw = GRID_BLOCK;                 // grid team: threads of each CTA that own elements
   int grid_rl = 0, grid_maxdeg = 0;         // grid team: row slots per CTA, entries per slot (0: no copy)
+  std::vector<int> grid_nbr;                // grid team: neighbour CTAs per CTA (empty: grid barriers only)
+  unsigned long long *d_grid_flags = nullptr;
   size_t smem = 0;
   int ws_in_smem = 0;
   long ws_tile = 0;
@@ -468,6 +470,7 @@ struct gbrkc_engine {
   int role_ctas[NTYPES] = {};
   int role_cap[NTYPES] = {};
   int gr_warps = 0;             // granule warps of the next launch (32 lanes each)
+  int gr_warps_need = 0;        // granule warps that would give every granule system with work its own lane
   int gr_warps_max = 0;         // granule warps the CTAs can hold beside the other roles
   int lanes = 16;               // lanes of a warp that take single-lane systems
   long gr_active = -1;          // granule systems with work (-1: not known yet)
@@ -888,6 +891,40 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
       P.grid_rl = (int)rl;
       P.grid_maxdeg = (fits && want) ? maxdeg : 0;
       P.smem = P.grid_maxdeg ? grid_rows_smem(rl, maxdeg) : 0;
+      // each CTA's neighbours: the owners of its rows' columns and the CTAs
+      // whose rows reach its elements (element i: CTA (i mod ctas*bw) / bw)
+      P.grid_nbr.clear();
+      const char *el = getenv("GBRKC_GRID_LOCAL");
+      if (!(el && el[0] == '0')) {
+        const long size = (long)ctas * bw;
+        std::vector<std::vector<char>> adj(ctas, std::vector<char>(ctas, 0));
+        for (size_t k = 0; k < P.systems.size(); k++) {
+          const bool own = P.sys_csr[k] >= 0;
+          const int nc = P.sys_nc[k], ncomp = P.sys_ncomp[k];
+          const int *r = own ? P.s_row.data() + P.s_row0[P.sys_csr[k]] : P.t_row.data() + P.t_row0[P.sys_tmpl[k]];
+          const int *cl = own ? P.s_col.data() + P.s_nz0[P.sys_csr[k]] : P.t_col.data() + P.t_nz0[P.sys_tmpl[k]];
+          for (int i = 0; i < nc; i++) {
+            const int j = (own || P.sys_ncell[k] == 1) ? i : i % ncomp, base = i - j;
+            const int a = (int)((i % size) / bw);
+            for (int e = r[j]; e < r[j + 1]; e++) {
+              const int b = (int)(((base + cl[e]) % size) / bw);
+              if (a != b) adj[a][b] = adj[b][a] = 1;
+            }
+          }
+        }
+        bool fit = true;
+        std::vector<int> nb((size_t)ctas * (GRID_MAX_NBR + 1), 0);
+        for (int a = 0; a < ctas && fit; a++) {
+          int n = 0;
+          for (int b = 0; b < ctas; b++)
+            if (adj[a][b]) {
+              if (n == GRID_MAX_NBR) { fit = false; break; }
+              nb[(size_t)a * (GRID_MAX_NBR + 1) + 1 + n++] = b;
+            }
+          nb[(size_t)a * (GRID_MAX_NBR + 1)] = n;
+        }
+        if (fit) P.grid_nbr = std::move(nb);
+      }
       return 0;
     }
     P.team = TEAM_CLUSTER16;
@@ -960,6 +997,8 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
   UP(P.sys_ws, V.sys_ws); UP(P.ctl, V.ctl);
   V.grid_red = nullptr;
   V.grid_bar = nullptr;
+  V.grid_nbr = nullptr;
+  V.grid_flags = nullptr;
   V.grid_bw = P.grid_bw;
   {
     // fence.acq_rel + acquire polls; GBRKC_GRID_FENCE=sc for __threadfence
@@ -975,6 +1014,12 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
     UP(red, V.grid_red);
     UP(bar, V.grid_bar);
     P.d_grid_bar = V.grid_bar;
+    if (!P.grid_nbr.empty()) {
+      const std::vector<unsigned long long> fl((size_t)P.grid * 16, 0ull);
+      UP(P.grid_nbr, V.grid_nbr);
+      UP(fl, V.grid_flags);
+      P.d_grid_flags = V.grid_flags;
+    }
   }
   std::vector<double> zws(P.ws_total, 0.0);
   UP(zws, V.ws);
@@ -1051,10 +1096,11 @@ template <> PoolView<double> &pool_view<double>(PoolHost &P) { return P.vd; }
 template <> PoolView<float> &pool_view<float>(PoolHost &P) { return P.vf; }
 
 // Granule warps for the next persistent launch: one lane per granule system
-// with work (parked slots, finished budgets and stopped systems need none;
-// lanes take further systems from the queue, so any count is correct), and
-// the granule CTAs re-fitted to them (at most 8 lane warps a CTA, no CTA
-// without one), the other roles giving or taking the difference.
+// with work (parked slots, finished budgets and stopped systems need none)
+// as far as the granule role's CTAs hold them (at most 8 lane warps a CTA);
+// lanes take further systems from the queue, so any count is correct and a
+// lane may run several systems in turn.  CTAs the warps leave empty go to
+// the other roles.
 void fit_granule_warps(gbrkc_engine *E) {
   if (!E->mega || E->role_ctas[GR] == 0) return;
   PoolHost &G = E->pools[GR];
@@ -1064,18 +1110,12 @@ void fit_granule_warps(gbrkc_engine *E) {
   int lanes = E->lanes;
   while (lanes < 32 && (active + lanes - 1) / lanes > E->gr_warps_max / 2) lanes = std::min(32, 2 * lanes);
   G.vd.lanes = G.vf.lanes = lanes;
-  const int want = (int)std::max(1L, std::min((long)E->gr_warps_max, (active + lanes - 1) / lanes));
-  E->gr_warps = want;
   const int per = MEGA_BLOCK / 32;
-  int c = std::max((want + per - 1) / per, std::min(want, E->role_ctas[GR]));
-  while (c > E->role_ctas[GR]) {  // take from the other role with the most CTAs
-    int best = -1;
-    for (int t = 0; t < NTYPES; t++)
-      if (t != GR && E->role_ctas[t] > 1 && (best < 0 || E->role_ctas[t] > E->role_ctas[best])) best = t;
-    if (best < 0) break;
-    E->role_ctas[best]--;
-    E->role_ctas[GR]++;
-  }
+  const long need = std::max(1L, std::min((long)E->gr_warps_max, (active + lanes - 1) / lanes));
+  E->gr_warps_need = (int)need;
+  const int want = (int)std::min(need, (long)per * E->role_ctas[GR]);
+  E->gr_warps = want;
+  const int c = std::min(want, E->role_ctas[GR]);
   while (c < E->role_ctas[GR]) {  // give to the other role with the most work per CTA
     int best = -1;
     double bv = -1.0;
@@ -1120,6 +1160,9 @@ int launch_mega_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
   M.lane_warps = 0;
   M.lane_extra = 0;
   if (E->role_ctas[GR] > 0) {
+    // the role split may have moved since the warps were fitted: at most 8
+    // warps a CTA (lanes take further systems in turn)
+    E->gr_warps = std::max(1, std::min(E->gr_warps, (MEGA_BLOCK / 32) * E->role_ctas[GR]));
     M.lane_warps = E->gr_warps / E->role_ctas[GR];
     M.lane_extra = E->gr_warps % E->role_ctas[GR];
     if (M.lane_warps + (M.lane_extra > 0) > MEGA_BLOCK / 32)
@@ -1173,7 +1216,11 @@ int launch_all(gbrkc_engine *E, double t0, int n_iv, int iv0, int init) {
         (P.block != MEGA_BLOCK || !P.ws_in_smem ||
          P.smem < (size_t)MEGA_BLOCK * (size_t)P.ws_tile * sizeof(double)))
       return fail(GBRKC_ESTATE, "single-lane pool %d: launch shape does not cover its workspaces", t);
-    if (P.team == TEAM_GRID) CUDA_TRY(cudaMemsetAsync(P.d_grid_bar, 0, sizeof(GridBarrier), E->streams[t]));
+    if (P.team == TEAM_GRID) {
+      CUDA_TRY(cudaMemsetAsync(P.d_grid_bar, 0, sizeof(GridBarrier), E->streams[t]));
+      if (P.d_grid_flags)
+        CUDA_TRY(cudaMemsetAsync(P.d_grid_flags, 0, (size_t)P.grid * 16 * sizeof(unsigned long long), E->streams[t]));
+    }
     CUDA_TRY(cudaEventRecord(E->ev_k0[t], E->streams[t]));
     if (P.f64)
       rc = launch_pool<double>(t, P.vd, P.team, P.grid, P.block, P.smem, E->streams[t], t0, n_iv, iv0, init);
@@ -1233,15 +1280,23 @@ void rebalance_roles(gbrkc_engine *E, const double *role_ms, bool tune_gr) {
         nother++;
         other_ctas += E->role_ctas[t];
       }
-    const int lo = std::max(1, std::min(E->mega_grid - nother, (E->gr_warps + MEGA_BLOCK / 32 - 1) / (MEGA_BLOCK / 32)));
-    const int hi = std::max(lo, std::min(E->gr_warps, E->mega_grid - nother));
+    // granule role time on x CTAs, A warps giving every system a lane:
+    // each lane runs max(1, A / 8x) systems in turn, and a system's serial
+    // chain slows as sqrt(warps per CTA) (FP64 issue shared on the SM)
+    const double A = std::max(1, E->gr_warps_need > 0 ? E->gr_warps_need : E->gr_warps);
+    auto gr_time = [&](double x) {
+      const double per = MEGA_BLOCK / 32;
+      return sqrt(std::min(per, A / x)) * std::max(1.0, A / (per * x));
+    };
+    const int lo = 1;
+    const int hi = std::max(lo, std::min((int)A, E->mega_grid - nother));
     int c = E->role_ctas[GR];
     if (tune_gr && others > 0.0 && role_ms[GR] > 0.0 && other_ctas > 0) {
-      const double d0 = (double)E->gr_warps / c;
+      const double f0 = gr_time(c);
       int best = c;
       double bestv = 1e300;
       for (int x = lo; x <= hi; x++) {
-        const double tg = role_ms[GR] * sqrt(((double)E->gr_warps / x) / d0);
+        const double tg = role_ms[GR] * gr_time(x) / f0;
         const int oc = E->mega_grid - x;
         if (oc < nother) continue;
         const double to = others * (double)other_ctas / (double)oc;
@@ -1342,6 +1397,7 @@ int setup_mega(gbrkc_engine *E) {
     E->gr_warps_max = (E->mega_grid - others_n) * (MEGA_BLOCK / 32);
     const long need = ((long)E->pools[GR].systems.size() + 31) / 32;
     E->gr_warps = (int)std::min<long>(need, E->gr_warps_max);
+    E->gr_warps_need = E->gr_warps;
   }
   const double w[NTYPES] = {0.0, 1.0, 0.35, 3.0};
   double ms[NTYPES];
@@ -1353,11 +1409,23 @@ int setup_mega(gbrkc_engine *E) {
     others += (t != GR && !P.systems.empty());
   }
   if (E->role_ctas[GR] > 0) {
-    // two granule warps to a CTA beside other roles, else spread over all
+    // two granule warps to a CTA beside other roles, else spread over all;
+    // beside other roles at most the granule share of the estimated work (a
+    // granule compartment costs about 29 Golgi compartments: the granule
+    // controller's tolerance of 1e-9 keeps its steps short)
     E->role_ctas[GR] = others ? (E->gr_warps + 1) / 2 : std::min(E->gr_warps, E->mega_grid);
+    if (others) {
+      double wo = 0.0;
+      for (int t = 1; t < NTYPES; t++) wo += w[t] * (double)E->pools[t].nc;
+      const double wg = 29.0 * (double)E->pools[GR].nc;
+      E->role_ctas[GR] = std::min(E->role_ctas[GR], std::max(1, (int)(E->mega_grid * wg / (wg + wo))));
+    }
     E->role_ctas[GR] = std::max(1, std::min(E->role_ctas[GR], E->mega_grid - others));
   }
   rebalance_roles(E, ms, false);
+  // the first launch's granule warps fit the granule CTAs (lanes take
+  // further systems in turn)
+  E->gr_warps = std::min(E->gr_warps, (MEGA_BLOCK / 32) * E->role_ctas[GR]);
   for (int t = 0; t < NTYPES; t++) E->role_work[t] = 0.0;
   return 0;
 }
@@ -1715,13 +1783,14 @@ int autotune_impl(gbrkc_engine *E, double t0, int n_iv, int *lanes_out) {
     if ((rc = S.take(E->mem.ptrs[k], E->mem.sizes[k]))) return rc;
   for (auto &P : E->pools)
     if (P.d_spk_log && P.spk_cap > 0 && (rc = S.take(P.d_spk_log, (size_t)P.spk_cap * sizeof(SpikeRec)))) return rc;
-  int ctas[NTYPES], warps = E->gr_warps, lanes0 = E->lanes;
+  int ctas[NTYPES], warps = E->gr_warps, warps_need = E->gr_warps_need, lanes0 = E->lanes;
   double work[NTYPES];
   for (int t = 0; t < NTYPES; t++) { ctas[t] = E->role_ctas[t]; work[t] = E->role_work[t]; }
   const long active = E->gr_active;
   auto restore_host = [&]() {
     for (int t = 0; t < NTYPES; t++) { E->role_ctas[t] = ctas[t]; E->role_work[t] = work[t]; }
     E->gr_warps = warps;
+    E->gr_warps_need = warps_need;
     E->gr_active = active;
   };
   for (int t = 0; t < NTYPES; t++) {
@@ -2331,6 +2400,9 @@ int launch_mega_static(gbrkc_engine *E, double t0, int n_iv, int iv0, int init, 
   M.lane_warps = 0;
   M.lane_extra = 0;
   if (E->role_ctas[GR] > 0) {
+    // the role split may have moved since the warps were fitted: at most 8
+    // warps a CTA (lanes take further systems in turn)
+    E->gr_warps = std::max(1, std::min(E->gr_warps, (MEGA_BLOCK / 32) * E->role_ctas[GR]));
     M.lane_warps = E->gr_warps / E->role_ctas[GR];
     M.lane_extra = E->gr_warps % E->role_ctas[GR];
     if (M.lane_warps + (M.lane_extra > 0) > MEGA_BLOCK / 32)

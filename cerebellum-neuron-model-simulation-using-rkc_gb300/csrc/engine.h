@@ -127,6 +127,11 @@ struct PoolView {
   // row slots of grid_maxdeg entries each); grid_maxdeg 0 = read the rows
   // from global memory
   int grid_rl, grid_maxdeg;
+  // grid team: per CTA its neighbour CTAs ([ctas][GRID_MAX_NBR + 1]: count,
+  // then the list) and the stage-count flags ([ctas * 16]); grid_nbr null:
+  // every stage barrier is the grid barrier
+  const int *grid_nbr;
+  unsigned long long *grid_flags;
 };
 
 // How a pool takes its synaptic current (solve_rkc.cu): granule cells add
@@ -215,6 +220,7 @@ constexpr int LANE_MAX_NC = 8;   // largest system integrated by a single lane
 constexpr int GRID_BLOCK = 256;
 constexpr int GRID_MAX_BLOCKS = 256;
 constexpr int GRID_MAX_ROWS = 8;
+constexpr int GRID_MAX_NBR = 32;   // neighbour CTAs a CTA's stage barrier can wait for (one a lane)
 constexpr size_t GRID_ROWS_SMEM_MAX = 160 * 1024;   // shared memory for a CTA's operator rows
 // bytes of that copy: per row slot its entry count, 1/Cm, and maxdeg
 // (column, conductance) pairs

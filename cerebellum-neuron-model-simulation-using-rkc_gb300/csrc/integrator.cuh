@@ -172,6 +172,47 @@ __device__ __forceinline__ void grid_barrier(GridBarrier *b, unsigned long long 
   __syncthreads();
 }
 
+// The grid team's stage barrier (grid_local_barrier): between the stages of
+// one step a CTA reads only the elements of the CTAs that own its rows'
+// neighbours (the operator is symmetric, so those are also the CTAs that
+// read its elements), so it waits for those alone.  Each CTA publishes its
+// stage count in its own flag (a release store on a 128-byte line) and warp
+// 0's lanes poll the neighbours' flags with acquire loads, one flag a lane.
+// nbr[b * (GRID_MAX_NBR + 1)] is CTA b's neighbour count, followed by the
+// neighbours.  The wait is bounded like grid_barrier's and raises the same
+// abort flag.
+__device__ __forceinline__ void grid_local_barrier(GridBarrier *b, unsigned long long *flags, const int *nbr,
+                                                   unsigned long long *lepoch) {
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    volatile GridBarrier *vb = b;
+    if (!vb->abort) {
+      const int lane = threadIdx.x;
+      unsigned long long k = 0;
+      if (lane == 0) {
+        k = (*lepoch += 1);
+        asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(flags + (long)blockIdx.x * 16), "l"(k)
+                     : "memory");
+      }
+      k = __shfl_sync(0xffffffffu, k, 0);
+      const int *my = nbr + (long)blockIdx.x * (GRID_MAX_NBR + 1);
+      if (lane < my[0]) {
+        const unsigned long long *f = flags + (long)my[1 + lane] * 16;
+        long it = 0;
+        while (ld_acquire_gpu(f) < k) {
+          if (++it > GRID_SPIN_LIMIT || vb->abort) {
+            atomicExch(&b->abort, 1);
+            break;
+          }
+          if (it > 64) __nanosleep(32);
+        }
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+}
+
 struct GridTeam {
   static constexpr int LS = 1, NCF = 0, CLUSTER = 0, GRID = 1;
   typedef WVec<1> Vec;
@@ -187,6 +228,10 @@ struct GridTeam {
   int maxdeg;
   double *linv, *lg;           // [rl] 1/Cm, [rl * maxdeg] conductances
   int *lcnt, *lcol;            // [rl] entry counts, [rl * maxdeg] columns (system-wide)
+  // stage barriers with the neighbouring CTAs only (nbr null: the grid barrier)
+  const int *nbr;
+  unsigned long long *flags;   // [gridDim * 16] stage counts, one 128-byte line a CTA
+  unsigned long long *lepoch;  // this CTA's stage-barrier count (shared)
   __device__ __forceinline__ Vec vec_at(double *W, long off) const { return Vec{W + off}; }
   __device__ __forceinline__ static long vstride(int ncp) { return ncp; }
   // (the CTA has bw threads; a thread past bw would own nothing: a rank no
@@ -196,6 +241,12 @@ struct GridTeam {
   }
   __device__ __forceinline__ int size() const { return (int)gridDim.x * bw; }
   __device__ __forceinline__ void sync() const { grid_barrier(bar, epoch, light); }
+  __device__ __forceinline__ void sync_stage() const {
+    if (nbr)
+      grid_local_barrier(bar, flags, nbr, lepoch);
+    else
+      grid_barrier(bar, epoch, light);
+  }
   __device__ __forceinline__ bool aborted() const { return ((volatile GridBarrier *)bar)->abort != 0; }
 };
 
@@ -698,6 +749,15 @@ struct Sys {
     c.idid = 6;
   }
 
+  // the barrier between a step's stages: a stage reads its rows'
+  // neighbours only, so a grid team waits for the CTAs that own them
+  __device__ __forceinline__ void stage_sync() const {
+    if constexpr (Team::GRID > 0)
+      tm.sync_stage();
+    else
+      tm.sync();
+  }
+
   // ----------------------------------------------------------------- step
   __device__ __forceinline__ bool step(double h, int m) {
     if (m > P.coef_mmax) {
@@ -727,7 +787,7 @@ struct Sys {
         }
       }
     }
-    tm.sync();
+    stage_sync();
     for (int j = 1; j < m; j++) {
       const double *q = T + 1 + 5 * (j - 1);
       const double mu = __ldg(q), nu = __ldg(q + 1), omn = __ldg(q + 2), mus = __ldg(q + 3), ajm1 = __ldg(q + 4);
@@ -760,7 +820,7 @@ struct Sys {
       c.map[LV2] = c.map[LV1];
       c.map[LV1] = c.map[LY];
       c.map[LY] = t2;
-      tm.sync();
+      stage_sync();
     }
     const int t3 = c.map[LY];
     c.map[LY] = c.map[LV1];

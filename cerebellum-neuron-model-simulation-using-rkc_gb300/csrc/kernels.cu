@@ -75,15 +75,15 @@ __global__ void __launch_bounds__(GRID_BLOCK, 1) k_advance_grid(const __grid_con
   extern __shared__ __align__(16) double grid_smem[];
   __shared__ double s_wp[GRID_MAX_ROWS * 8];
   __shared__ double s_res;
-  __shared__ unsigned long long s_epoch;
-  if (threadIdx.x == 0) s_epoch = 0;     // the counter is zeroed before every launch
+  __shared__ unsigned long long s_epoch, s_lepoch;
+  if (threadIdx.x == 0) s_epoch = s_lepoch = 0;     // counter and flags are zeroed before every launch
   __syncthreads();
   // the operator rows' copy: [rl] 1/Cm, [rl * maxdeg] g, [rl] counts, [rl * maxdeg] columns
   const long rl = P.grid_rl, md = P.grid_maxdeg;
   double *linv = grid_smem, *lg = grid_smem + rl;
   int *lcnt = (int *)(lg + rl * md), *lcol = lcnt + rl;
   const GridTeam tm{(GridBarrier *)P.grid_bar, P.grid_red, s_wp, &s_res, &s_epoch, P.grid_bw, P.grid_light,
-                    P.grid_maxdeg, linv, lg, lcnt, lcol};
+                    P.grid_maxdeg, linv, lg, lcnt, lcol, P.grid_nbr, P.grid_flags, &s_lepoch};
   for (int s = 0; s < P.nsys; s++) run_system<CT, R, GridTeam>(P, tm, s, nullptr, t0, n_iv, iv0, init != 0);
 }
 

@@ -87,6 +87,17 @@ def test_grid_team_sc_fence_barrier_bit_exact(oracle, monkeypatch, name):
     eng.close()
 
 
+@pytest.mark.parametrize("name", ["pkj_2x1_gj", "go_2x2_gj"])
+def test_grid_team_grid_barrier_stages_bit_exact(oracle, monkeypatch, name):
+    """Every stage barrier a grid barrier (GBRKC_GRID_LOCAL=0) instead of a
+    wait for the neighbouring CTAs only."""
+    monkeypatch.setenv("GBRKC_GRID_MIN_NC", "300")
+    monkeypatch.setenv("GBRKC_GRID_LOCAL", "0")
+    s, eng, sid = run_pair(oracle, name, [1, 15, 16])
+    assert eng.launch_layout()[0] is False
+    eng.close()
+
+
 def test_grid_io_network(oracle, monkeypatch):
     """A 12x12 olive network (nonlinear gap junctions across CTAs)."""
     monkeypatch.setenv("GBRKC_GRID_MIN_NC", "400")
