@@ -1095,12 +1095,23 @@ template <typename R> PoolView<R> &pool_view(PoolHost &P);
 template <> PoolView<double> &pool_view<double>(PoolHost &P) { return P.vd; }
 template <> PoolView<float> &pool_view<float>(PoolHost &P) { return P.vf; }
 
+// Whether the warps that give every granule system with work its own lane
+// fit in half the CTAs the other roles leave (8 warps a CTA): then every
+// system is in flight, the latency a request server needs; else lanes run
+// several systems in turn and the role split decides the granule CTAs.
+bool granules_all_in_flight(const gbrkc_engine *E, long warps) {
+  int nother = 0;
+  for (int t = 0; t < NTYPES; t++) nother += (t != GR && E->role_ctas[t] > 0);
+  return (warps + MEGA_BLOCK / 32 - 1) / (MEGA_BLOCK / 32) <= (E->mega_grid - nother) / 2;
+}
+
 // Granule warps for the next persistent launch: one lane per granule system
-// with work (parked slots, finished budgets and stopped systems need none)
-// as far as the granule role's CTAs hold them (at most 8 lane warps a CTA);
-// lanes take further systems from the queue, so any count is correct and a
-// lane may run several systems in turn.  CTAs the warps leave empty go to
-// the other roles.
+// with work (parked slots, finished budgets and stopped systems need none).
+// When they are all in flight (granules_all_in_flight) the granule CTAs are
+// re-fitted to them at once, the other roles giving the difference; else
+// the warps fill the granule role's CTAs (at most 8 a CTA) and lanes take
+// further systems from the queue in turn (any count is correct).  CTAs the
+// warps leave empty go to the other roles.
 void fit_granule_warps(gbrkc_engine *E) {
   if (!E->mega || E->role_ctas[GR] == 0) return;
   PoolHost &G = E->pools[GR];
@@ -1113,9 +1124,19 @@ void fit_granule_warps(gbrkc_engine *E) {
   const int per = MEGA_BLOCK / 32;
   const long need = std::max(1L, std::min((long)E->gr_warps_max, (active + lanes - 1) / lanes));
   E->gr_warps_need = (int)need;
-  const int want = (int)std::min(need, (long)per * E->role_ctas[GR]);
+  const bool all_in = granules_all_in_flight(E, need);
+  const int want = all_in ? (int)need : (int)std::min(need, (long)per * E->role_ctas[GR]);
   E->gr_warps = want;
-  const int c = std::min(want, E->role_ctas[GR]);
+  const int c = all_in ? std::max((want + per - 1) / per, std::min(want, E->role_ctas[GR]))
+                       : std::min(want, E->role_ctas[GR]);
+  while (c > E->role_ctas[GR]) {  // take from the other role with the most CTAs
+    int best = -1;
+    for (int t = 0; t < NTYPES; t++)
+      if (t != GR && E->role_ctas[t] > 1 && (best < 0 || E->role_ctas[t] > E->role_ctas[best])) best = t;
+    if (best < 0) break;
+    E->role_ctas[best]--;
+    E->role_ctas[GR]++;
+  }
   while (c < E->role_ctas[GR]) {  // give to the other role with the most work per CTA
     int best = -1;
     double bv = -1.0;
@@ -1288,7 +1309,9 @@ void rebalance_roles(gbrkc_engine *E, const double *role_ms, bool tune_gr) {
       const double per = MEGA_BLOCK / 32;
       return sqrt(std::min(per, A / x)) * std::max(1.0, A / (per * x));
     };
-    const int lo = 1;
+    const int lo = granules_all_in_flight(E, (long)A)
+                       ? std::max(1, std::min(E->mega_grid - nother, ((int)A + MEGA_BLOCK / 32 - 1) / (MEGA_BLOCK / 32)))
+                       : 1;
     const int hi = std::max(lo, std::min((int)A, E->mega_grid - nother));
     int c = E->role_ctas[GR];
     if (tune_gr && others > 0.0 && role_ms[GR] > 0.0 && other_ctas > 0) {
