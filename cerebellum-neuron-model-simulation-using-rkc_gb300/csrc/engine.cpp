@@ -399,10 +399,10 @@ struct PoolHost {
   std::vector<uint8_t> ctype, flags;
   // templates used by this pool
   std::vector<int> t_row0, t_nz0, t_cm0, t_row, t_col;
-  std::vector<double> t_g, t_invcm;
+  std::vector<double> t_g, t_invcm, t_gc, t_Gc;
   std::map<int, int> tmpl_local;
   std::vector<int> s_row0, s_nz0, s_cm0, s_row, s_col;
-  std::vector<double> s_g, s_invcm;
+  std::vector<double> s_g, s_invcm, s_gc, s_Gc;
   std::vector<int> gap_pre, gap_post;
   std::vector<double> gap_g;
   std::vector<int> stim_comp, cell_soma, cell_spk;
@@ -791,8 +791,16 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
       int cnt = 0;
       for (int r = 0; r < T.ncomp; r++) {
         P.t_row.push_back(cnt);
+        double sum = 0.0;
         for (int j = T.row[r]; j < T.row[r + 1]; j++)
-          if (T.col[j] != r) { P.t_col.push_back(T.col[j]); P.t_g.push_back(T.val[j]); cnt++; }
+          if (T.col[j] != r) {
+            P.t_col.push_back(T.col[j]);
+            P.t_g.push_back(T.val[j]);
+            P.t_gc.push_back(T.val[j] * T.invcm[r]);
+            sum += T.val[j] * T.invcm[r];
+            cnt++;
+          }
+        P.t_Gc.push_back(sum);
       }
       P.t_row.push_back(cnt);
       for (double x : T.invcm) P.t_invcm.push_back(x);
@@ -808,8 +816,16 @@ int assemble_pool(gbrkc_engine *E, PoolHost &P) {
       int cnt = 0;
       for (int r = 0; r < S.nc; r++) {
         P.s_row.push_back(cnt);
+        double sum = 0.0;
         for (int j = C.row[r]; j < C.row[r + 1]; j++)
-          if (C.col[j] != r) { P.s_col.push_back(C.col[j]); P.s_g.push_back(C.val[j]); cnt++; }
+          if (C.col[j] != r) {
+            P.s_col.push_back(C.col[j]);
+            P.s_g.push_back(C.val[j]);
+            P.s_gc.push_back(C.val[j] * C.invcm[r]);
+            sum += C.val[j] * C.invcm[r];
+            cnt++;
+          }
+        P.s_Gc.push_back(sum);
       }
       P.s_row.push_back(cnt);
       for (double x : C.invcm) P.s_invcm.push_back(x);
@@ -1032,8 +1048,10 @@ int upload_pool(gbrkc_engine *E, PoolHost &P, PoolView<R> &V) {
   UP(ion, V.ion); UP(cond, V.cond);
   UP(P.t_row0, V.t_row0); UP(P.t_nz0, V.t_nz0); UP(P.t_cm0, V.t_cm0); UP(P.t_row, V.t_row);
   UP(P.t_col, V.t_col); UP(P.t_g, V.t_g); UP(P.t_invcm, V.t_invcm);
+  UP(P.t_gc, V.t_gc); UP(P.t_Gc, V.t_Gc);
   UP(P.s_row0, V.s_row0); UP(P.s_nz0, V.s_nz0); UP(P.s_cm0, V.s_cm0); UP(P.s_row, V.s_row);
   UP(P.s_col, V.s_col); UP(P.s_g, V.s_g); UP(P.s_invcm, V.s_invcm);
+  UP(P.s_gc, V.s_gc); UP(P.s_Gc, V.s_Gc);
   UP(P.gap_pre, V.gap_pre); UP(P.gap_post, V.gap_post); UP(P.gap_g, V.gap_g);
   UP(P.stim_comp, V.stim_comp); UP(P.stim_amp, V.stim_amp); UP(P.stim_t0, V.stim_t0);
   UP(P.stim_t1, V.stim_t1); UP(P.cell_soma, V.cell_soma); UP(P.cell_spk, V.cell_spk);
@@ -1151,18 +1169,13 @@ void fit_granule_warps(gbrkc_engine *E) {
 }
 
 // The persistent launch's pool views and role boundaries; returns the CTA
-// count.  A mixed engine's FP64 granule pool goes to gr64.
+// count.
 template <typename R>
 int mega_pools(gbrkc_engine *E, MegaView<R> &M) {
   int end = 0;
   for (int t = 0; t < NTYPES; t++) {
     PoolHost &P = E->pools[t];
-    const bool wide = !std::is_same<R, double>::value && P.f64;
-    M.pool[t] = (P.systems.empty() || wide) ? PoolView<R>{} : pool_view<R>(P);
-    if (wide && t == GR) {
-      M.gr64 = P.vd;
-      M.gr_f64 = 1;
-    }
+    M.pool[t] = P.systems.empty() ? PoolView<R>{} : pool_view<R>(P);
     end += E->role_ctas[t];
     M.role_end[t] = end;
   }
@@ -1371,6 +1384,10 @@ void rebalance_roles(gbrkc_engine *E, const double *role_ms, bool tune_gr) {
 int setup_mega(gbrkc_engine *E) {
   const char *no = getenv("GBRKC_NO_MEGA");
   if (no && no[0] == '1') return 0;
+  // a mixed engine with FP64 granule pools advances each type in its own
+  // launch (the granule pool's FP64 kernel beside the others' FP32 kernels,
+  // on their own streams): the persistent kernel holds one precision
+  if (E->gr_f64 && !E->pools[GR].systems.empty()) return 0;
   // pools of very large systems run on clusters, one launch per pool
   for (int t = 0; t < NTYPES; t++)
     if (!E->pools[t].systems.empty() &&

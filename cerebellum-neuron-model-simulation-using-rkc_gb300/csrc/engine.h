@@ -77,10 +77,12 @@ struct PoolView {
   const int *t_row0, *t_nz0, *t_cm0;  // per template offsets
   const int *t_row, *t_col;
   const double *t_g, *t_invcm;
+  const double *t_gc, *t_Gc;          // mixed precision: g / Cm per entry, their row sums (like t_invcm)
   // system CSRs (multi-cell systems with linear gap junctions)
   const int *s_row0, *s_nz0, *s_cm0;
   const int *s_row, *s_col;
   const double *s_g, *s_invcm;
+  const double *s_gc, *s_Gc;
   // IO nonlinear gap junctions: per system edge list (post compartment, pre or -1)
   const int *gap_pre, *gap_post;
   const double *gap_g;
@@ -191,10 +193,6 @@ constexpr int team_cluster_size(int team) {
 template <typename R>
 struct MegaView {
   PoolView<R> pool[NTYPES];
-  // mixed precision with FP64 granule pools: the granule role runs the FP64
-  // path on gr64 (pool[GR] is then unused)
-  PoolView<double> gr64;
-  int gr_f64;
   int role_end[NTYPES];
   int lane_warps, lane_extra;  // granule CTA b runs lane_warps (+1 if b < lane_extra) warps
   int gr_nc4;                 // every granule system has 4 compartments

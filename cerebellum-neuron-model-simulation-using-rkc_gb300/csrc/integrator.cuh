@@ -26,6 +26,7 @@
 // count, and the ion update is by far the longest path, so running it for 4
 // lanes at a time would cost nearly as much as for 32.
 #pragma once
+#include <type_traits>
 #include "engine.h"
 #include "physics.cuh"
 
@@ -379,6 +380,7 @@ struct Sys {
   bool csr;
   const int *row, *col;
   const double *g, *invcm;
+  const double *gc, *Gc;       // mixed precision: g / Cm and its row sums
   double *W;
   Ctl c;
   // flat driver state
@@ -406,12 +408,16 @@ struct Sys {
       col = P.s_col + P.s_nz0[k];
       g = P.s_g + P.s_nz0[k];
       invcm = P.s_invcm + P.s_cm0[k];
+      gc = P.s_gc + P.s_nz0[k];
+      Gc = P.s_Gc + P.s_cm0[k];
     } else {
       const int t = P.sys_tmpl[s];
       row = P.t_row + P.t_row0[t];
       col = P.t_col + P.t_nz0[t];
       g = P.t_g + P.t_nz0[t];
       invcm = P.t_invcm + P.t_cm0[t];
+      gc = P.t_gc + P.t_nz0[t];
+      Gc = P.t_Gc + P.t_cm0[t];
     }
   }
 
@@ -460,6 +466,21 @@ struct Sys {
         for (int q = 0; q < n; q++) d = fma(gg[q], y[cc[q]] - yi, d);
         return d * tm.linv[lr];
       }
+    }
+    if constexpr (!std::is_same<R, double>::value) {
+      // mixed precision: -b / Cm + sum (g / Cm) y_j - (sum g / Cm) y_i, the
+      // same operator with one FP64 operation fewer per entry (the rounding
+      // differs from the FP64 path's in the last bits)
+      int j = i, base = 0;
+      if (!(csr || ncell == 1)) {
+        const int cidx = i / ncomp;
+        j = i - cidx * ncomp;
+        base = cidx * ncomp;
+      }
+      const int r0 = __ldg(row + j), r1 = __ldg(row + j + 1);
+      double d = -(bvec()[i]) * __ldg(invcm + j);
+      for (int k = r0; k < r1; k++) d = fma(__ldg(gc + k), y[base + __ldg(col + k)], d);
+      return fma(-__ldg(Gc + j), y[i], d);
     }
     double d = -(bvec()[i]);
     const double yi = y[i];

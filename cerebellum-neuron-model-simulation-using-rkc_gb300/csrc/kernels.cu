@@ -139,15 +139,6 @@ __global__ void __launch_bounds__(MEGA_BLOCK, 1) k_mega(const __grid_constant__ 
     case GR:
       // single-lane granule systems on the CTA's first warps
       if ((int)(threadIdx.x >> 5) < M.lane_warps + ((int)blockIdx.x < M.lane_extra ? 1 : 0)) {
-        if constexpr (!std::is_same<R, double>::value) {
-          if (M.gr_f64) {
-            if (M.gr_nc4)
-              run_lanes_regs<GR, double, MEGA_BLOCK, 4>(M.gr64, M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
-            else
-              run_lanes<GR, double, MEGA_BLOCK>(M.gr64, M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
-            break;
-          }
-        }
         if (M.gr_nc4)
           run_lanes_regs<GR, R, MEGA_BLOCK, 4>(M.pool[GR], M.queue + GR, 0, 0, smem, t0, n_iv, iv0, init != 0);
         else
