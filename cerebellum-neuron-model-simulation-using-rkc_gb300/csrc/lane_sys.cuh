@@ -233,7 +233,16 @@ struct LaneSys {
     return true;
   }
 
-  // Sys::attempt
+  // Sys::attempt.  In mixed precision (R = float) the controller's scalar
+  // chain runs in FP32: the error terms' quotients, their norm and its cube
+  // root, the stage count's square root and the step-size ratios.  The step
+  // size, the time, the stage recurrence and the accept/reject comparison
+  // stay FP64.  A lone granule warp is a latency-bound serial chain, and
+  // FP64 square roots, divisions and the cube root's Newton steps are its
+  // longest links; in FP32 they change the step sizes by about 1e-7
+  // relative, the size of the differences FP32 gating already makes.
+  static constexpr bool FAST = !std::is_same<R, double>::value;
+
   __device__ __forceinline__ int attempt() {
     const double hmax = H_MAX, hmin = c.hmin;
     if (c.newspc) {
@@ -245,7 +254,11 @@ struct LaneSys {
       c.absh = fabs(c.tend - c.lt);
       c.last = 1;
     }
-    const double marg = sqrt(1.54 * c.absh * c.sprad + 1.0);
+    double marg;
+    if constexpr (FAST)
+      marg = (double)sqrtf((float)(1.54 * c.absh * c.sprad + 1.0));
+    else
+      marg = sqrt(1.54 * c.absh * c.sprad + 1.0);
     if (!(marg < 1.0e9)) {
       c.status |= ST_NAN;
       return Sys<CT, R, BlockTeam>::ATT_FAIL;
@@ -260,8 +273,27 @@ struct LaneSys {
     if (h <= hmin) h = hmin;
     if (!step(h, m)) return Sys<CT, R, BlockTeam>::ATT_FAIL;
     c.n_steps++;
-    double err;
-    {
+    double err, cr;
+    if constexpr (FAST) {
+      const double h04 = 0.4 * h;
+      float q[NC];
+#pragma unroll
+      for (int i = 0; i < NC; i++) {
+        const double f = rhs(y, i);
+        v1[i] = f;
+        const double ay = fabs(y[i]), ayn = fabs(yn[i]);
+        const double wt = fma(c.tol, (ay > ayn) ? ay : ayn, c.tol);
+        const double est = fma(h04, fn[i] + f, 0.8 * (yn[i] - y[i]));
+        const float qv = (float)est / (float)wt;
+        q[i] = qv * qv;
+      }
+      float e2 = q[0];
+#pragma unroll
+      for (int i = 1; i < NC; i++) e2 += q[i];
+      const float ef = sqrtf(e2 * (1.0f / (float)NC));
+      err = (double)ef;
+      cr = (double)cbrtf(ef);
+    } else {
       const double h04 = 0.4 * h;
       double q[NC];
 #pragma unroll
@@ -275,18 +307,22 @@ struct LaneSys {
         q[i] = qv * qv;
       }
       err = tree_regs<NC>(q);
+      if ((NC & (NC - 1)) == 0)
+        err = sqrt(err * (1.0 / (double)NC));
+      else
+        err = sqrt(err / (double)NC);
+      cr = 0.0;
     }
-    if ((NC & (NC - 1)) == 0)
-      err = sqrt(err * (1.0 / (double)NC));
-    else
-      err = sqrt(err / (double)NC);
     if (!(err == err)) {
       c.status |= ST_NAN;
       return Sys<CT, R, BlockTeam>::ATT_FAIL;
     }
-    const double cr = cm_cbrt(err);
+    if constexpr (!FAST) cr = cm_cbrt(err);
     if (err > 1.0) {
-      c.absh = 0.8 * c.absh / cr;
+      if constexpr (FAST)
+        c.absh = c.absh * (double)(0.8f / (float)cr);
+      else
+        c.absh = 0.8 * c.absh / cr;
       c.n_rej++;
       if (c.absh < hmin) {
         c.idid = 4;
@@ -317,17 +353,30 @@ struct LaneSys {
       yn[i] = y[i];
       y[i] = t;
     }
-    double fac = 10.0, temp1, temp2;
-    if (c.naccpt == 1) {
-      temp2 = cr;
-      if (0.8 < fac * temp2) fac = 0.8 / temp2;
+    if constexpr (FAST) {
+      float fac = 10.0f;
+      const float crf = (float)cr;
+      if (c.naccpt == 1) {
+        if (0.8f < fac * crf) fac = 0.8f / crf;
+      } else {
+        const float temp1 = 0.8f * (float)c.absh * (float)c.cbrt_errold;
+        const float temp2 = fabsf((float)c.hold) * (crf * crf);
+        if (temp1 < fac * temp2) fac = temp1 / temp2;
+      }
+      c.absh = (double)((0.1f > fac) ? 0.1f : fac) * c.absh;
     } else {
-      temp1 = 0.8 * c.absh * c.cbrt_errold;
-      temp2 = fabs(c.hold) * (cr * cr);
-      if (temp1 < fac * temp2) fac = temp1 / temp2;
+      double fac = 10.0, temp1, temp2;
+      if (c.naccpt == 1) {
+        temp2 = cr;
+        if (0.8 < fac * temp2) fac = 0.8 / temp2;
+      } else {
+        temp1 = 0.8 * c.absh * c.cbrt_errold;
+        temp2 = fabs(c.hold) * (cr * cr);
+        if (temp1 < fac * temp2) fac = temp1 / temp2;
+      }
+      c.absh = ((0.1 > fac) ? 0.1 : fac) * c.absh;
     }
     c.cbrt_errold = cr;
-    c.absh = ((0.1 > fac) ? 0.1 : fac) * c.absh;
     {
       const double mn = fmin(hmax, c.absh);
       c.absh = (hmin > mn) ? hmin : mn;
