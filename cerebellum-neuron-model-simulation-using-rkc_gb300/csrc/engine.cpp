@@ -663,9 +663,7 @@ bool grid_team_fits(const gbrkc_engine *E, const PoolHost &P) {
 // barrier); within the reduction's limits (at most GRID_MAX_BLOCKS chunks of
 // bw elements, GRID_MAX_ROWS per thread).  GBRKC_GRID_BW and GBRKC_GRID_CTAS
 // fix either.  Returns false when no shape fits.
-bool grid_shape(long nc, int cap, int *bw_out, int *ctas_out) {
-  const char *eb = getenv("GBRKC_GRID_BW"), *ec = getenv("GBRKC_GRID_CTAS");
-  const int want_bw = (eb && eb[0]) ? atoi(eb) : 0, want_ctas = (ec && ec[0]) ? atoi(ec) : 0;
+bool grid_shape_rule(long nc, int cap, int want_bw, int want_ctas, int *bw_out, int *ctas_out) {
   long best_load = -1;
   for (int bw = 32; bw <= GRID_BLOCK; bw *= 2) {
     if (want_bw > 0 && bw != want_bw) continue;
@@ -684,6 +682,11 @@ bool grid_shape(long nc, int cap, int *bw_out, int *ctas_out) {
     }
   }
   return best_load > 0;
+}
+bool grid_shape(long nc, int cap, int *bw_out, int *ctas_out) {
+  const char *eb = getenv("GBRKC_GRID_BW"), *ec = getenv("GBRKC_GRID_CTAS");
+  const int want_bw = (eb && eb[0]) ? atoi(eb) : 0, want_ctas = (ec && ec[0]) ? atoi(ec) : 0;
+  return grid_shape_rule(nc, cap, want_bw, want_ctas, bw_out, ctas_out);
 }
 
 // Output compartments per cell: the voltage record (the soma; the
@@ -2044,6 +2047,15 @@ extern "C" int gbrkc_launch_layout(gbrkc_engine *E, int *ctas_per_type) {
   for (int t = 0; t < NTYPES; t++)
     ctas_per_type[t] = E->mega ? E->role_ctas[t] : E->pools[t].systems.empty() ? 0 : E->pools[t].grid;
   return E->mega ? 1 : 0;
+}
+extern "C" int gbrkc_grid_shape(long long nc, int max_ctas, int *threads_per_cta, int *ctas) {
+  if (nc <= 0 || max_ctas <= 0 || !threads_per_cta || !ctas) return fail(GBRKC_EINVAL, "bad arguments");
+  int bw = 0, n = 0;
+  if (!grid_shape_rule((long)nc, max_ctas, 0, 0, &bw, &n))
+    return fail(GBRKC_EINVAL, "no grid-team shape holds %lld compartments", nc);
+  *threads_per_cta = bw;
+  *ctas = n;
+  return 0;
 }
 extern "C" int gbrkc_type_team(gbrkc_engine *E, int type) {
   if (!E || type < 0 || type >= NTYPES) return fail(GBRKC_EINVAL, "bad arguments");

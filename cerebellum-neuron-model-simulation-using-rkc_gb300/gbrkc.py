@@ -128,6 +128,7 @@ def lib() -> C.CDLL:
         L.gbrkc_autotune.argtypes = [P, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.gbrkc_launch_layout.argtypes = [P, C.POINTER(C.c_int)]
         L.gbrkc_type_team.argtypes = [P, C.c_int]
+        L.gbrkc_grid_shape.argtypes = [C.c_longlong, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.gbrkc_compartment_updates.argtypes = [P, C.c_int]
         L.gbrkc_compartment_updates.restype = C.c_longlong
         L.gbrkc_systems_reset.argtypes = [P, C.c_int, C.c_int, C.POINTER(ResetDesc)]
@@ -458,6 +459,14 @@ def system_bytes(precision: int, cell_type: int, ncomp: int, ncell: int) -> int:
     if b < 0:
         _check(int(b))
     return int(b)
+
+
+def grid_shape(nc: int, max_ctas: int):
+    """The grid team's launch shape for a lone system of nc compartments on at
+    most max_ctas CTAs: (threads per CTA, CTAs).  Host only."""
+    bw, n = C.c_int(), C.c_int()
+    _check(lib().gbrkc_grid_shape(nc, max_ctas, C.byref(bw), C.byref(n)))
+    return bw.value, n.value
 
 
 def _scheck(rc: int) -> None:

@@ -164,6 +164,15 @@ int gbrkc_launch_layout(gbrkc_engine *e, int *ctas_per_type);
 enum { GBRKC_TEAM_MEGA = 1, GBRKC_TEAM_GRID = 2, GBRKC_TEAM_CLUSTER = 3, GBRKC_TEAM_POOL = 4 };
 int gbrkc_type_team(gbrkc_engine *e, int cell_type);
 
+/* The grid team's launch shape for a lone system of nc compartments on at
+ * most max_ctas co-resident CTAs (the engine uses the device's SM count):
+ * CTAs of threads_per_cta threads (a power of two, 32..256), each thread
+ * owning elements i with i mod (ctas * threads_per_cta) its index.  The rule
+ * minimises the busiest CTA's elements, then the CTA count, within 256
+ * chunks of threads_per_cta elements and 8 elements a thread.  Host only
+ * (no device needed); GBRKC_EINVAL when no shape holds nc. */
+int gbrkc_grid_shape(long long nc, int max_ctas, int *threads_per_cta, int *ctas);
+
 /* ---- chemical synapses (network mode) ----------------------------------
  * The reference's RKC network path (syn.cu; main.cu:300-305 with
  * network_sim true): mossy fibre -> granule (Poisson input), granule ->
